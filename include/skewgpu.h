@@ -1,0 +1,118 @@
+/*
+ * skewgpu.h -- C ABI of libskewgpu.so, the GB300 (sm_103a) FP64 implementation of
+ * SkewLinearAlgebra.jl's skew-Householder pipeline.
+ *
+ * Every pointer argument that refers to matrix or vector data is a DEVICE pointer
+ * owned by the caller (e.g. pointer(A.data) of a CuArray).  Matrices are
+ * column-major (Julia layout) with a leading dimension.  Calls are asynchronous
+ * with respect to the host and ordered on the handle's stream.  Each entry point
+ * returns a skew_status_t for argument/launch errors; conditions that are only
+ * known on the device (non-convergence, a singular matrix, a matrix that is not
+ * skew) are written to the caller's device-side `info`/`status` integers.
+ *
+ * Reference interfaces each entry point replaces are cited by file:line of
+ * SkewLinearAlgebra.jl (v1.1.0).
+ */
+#ifndef SKEWGPU_H
+#define SKEWGPU_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define SKEW_API __attribute__((visibility("default")))
+#else
+#define SKEW_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* skew_stream_t; /* == cudaStream_t */
+
+typedef enum {
+  SKEW_OK = 0,
+  SKEW_NOT_SKEW = 1,        /* ArgumentError("Pfaffian requires a skew-Hermitian matrix"), pfaffian.jl:255 */
+  SKEW_NO_CONVERGENCE = 2,  /* error("Maximum number of iterations reached"), skeweigen.jl:154 */
+  SKEW_BAD_ARG = 3,
+  SKEW_CUDA_ERROR = 4,
+  SKEW_SINGULAR = 5,        /* Pf(A) == 0: log|Pf| = -Inf, gradient not finite (odd n, pfaffian.jl:169) */
+  SKEW_UNSUPPORTED = 6,
+  SKEW_NO_MEMORY = 7,
+  SKEW_FALLBACK_USED = 8    /* QR stagnated; values from the symmetric-tridiagonal fallback (skeweigen.jl:132-137) */
+} skew_status_t;
+
+typedef struct skew_handle_st* skew_handle_t;
+typedef struct skew_batch_plan_st* skew_batch_plan_t;
+
+/* Library handle: owns the stream binding and cached workspaces (one per stream). */
+SKEW_API int skew_create(skew_handle_t* handle);
+SKEW_API int skew_destroy(skew_handle_t handle);
+SKEW_API int skew_set_stream(skew_handle_t handle, skew_stream_t stream);
+SKEW_API const char* skew_status_string(int status);
+SKEW_API int skew_version(void);
+
+/* ---------------------------------------------------------------------------
+ * Single-matrix entry points (real Float64).
+ * ------------------------------------------------------------------------- */
+
+/* LA.hessenberg!(A::SkewHermitian{Float64})  hessenberg.jl:5-13 (skewblockedhess! :144-173).
+ * In place: on exit A holds the reflectors below the subdiagonal (v[1] = 1 stored on
+ * the subdiagonal, as the reference stores them), tau[n-1] the reflector scalars and
+ * ev[n-1] the subdiagonal of H = SkewHermTridiagonal(ev). */
+SKEW_API int skew_hessenberg_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev, int* info);
+
+/* logabspfaffian!(A::SkewHermitian{Float64})  pfaffian.jl:167-179, :235.
+ * In place.  logpf[0] = log|Pf(A)|, sign[0] = sign of Pf(A) (odd n: -Inf, 0).
+ * check != 0 verifies A == -A^T exactly first (pfaffian.jl:254-256) -> info = SKEW_NOT_SKEW. */
+SKEW_API int skew_logabspf_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* sign, int check,
+                    int* info);
+
+/* rrule(logabspfaffian) forward + pullback seed 1: as skew_logabspf_d, and
+ * G = d log|Pf(A)| / dA = 1/2 A^{-T}, formed as Q (1/2 T^{-T}) Q^T from the reflectors.
+ * (No reference counterpart: the spec adjoint.) */
+SKEW_API int skew_logabspf_grad_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* sign,
+                         double* G, int64_t ldg, int* info);
+
+/* LA.eigvals!(A::SkewHermitian{Float64})  eigen.jl:2-6 -> skeweigvals! :312-318 ->
+ * skewtrieigvals! skeweigen.jl:105-156.  vals_im[n] = imaginary parts of the eigenvalues
+ * in the reference's order (eigenvalue k is i*vals_im[k]).  A is destroyed. */
+SKEW_API int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info);
+
+/* LA.eigen!(A::SkewHermitian{Float64})  eigen.jl:338-360 (skeweigen! + skewtrieigen_divided!).
+ * vals_im[n]; eigenvectors V = Vr + i*Vi (n x n each, leading dimension ldv).  A is destroyed. */
+SKEW_API int skew_eigen_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,
+                 int64_t ldv, int* info);
+
+/* Base.exp(A::SkewHermitian{Float64})  exp.jl:3-35, :48.  E (n x n, lde) = exp(A). A destroyed. */
+SKEW_API int skew_exp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, int64_t lde, int* info);
+
+/* Base.cis(A::SkewHermitian{Float64})  exp.jl:99-110, :204.  C = cis(A) = exp(iA), Hermitian,
+ * ComplexF64 interleaved (re, im), leading dimension ldc in complex elements. A destroyed. */
+SKEW_API int skew_cis_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* C, int64_t ldc, int* info);
+
+/* ---------------------------------------------------------------------------
+ * Batched entry points: many independent real skew matrices of uneven size.
+ * A plan fixes the sizes (host array n[count]), sorts them largest first, picks a
+ * kernel configuration per size bucket and owns the device workspace.
+ * ------------------------------------------------------------------------- */
+SKEW_API int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, skew_batch_plan_t* plan);
+SKEW_API int skew_batch_plan_destroy(skew_batch_plan_t plan);
+
+/* logabspfaffian for every matrix; A[b] (device array of device pointers) is read only,
+ * leading dimension n[b].  grad may be NULL; otherwise grad[b] receives 1/2 A_b^{-T}
+ * (leading dimension n[b]).  status[b] is a skew_status_t per matrix. */
+SKEW_API int skew_batch_logabspf_d(skew_batch_plan_t plan, const double* const* A, double* logpf, double* sign,
+                          double* const* grad, int* status);
+
+/* eigvals for every matrix: vals_im[b] (device pointers) receives n[b] values. */
+SKEW_API int skew_batch_eigvals_d(skew_batch_plan_t plan, const double* const* A, double* const* vals_im, int* status);
+
+/* Diagnostics: measured FP64 DFMA throughput of the current device in TFLOP/s
+ * (runs a short microbenchmark on the handle's stream and synchronizes). */
+SKEW_API int skew_measure_fp64_peak(skew_handle_t h, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SKEWGPU_H */

@@ -1,0 +1,383 @@
+// C ABI of libskewgpu (declared in include/skewgpu.h): handles, batch plans and
+// the single-matrix entry points.  Host code only dispatches and owns
+// workspaces; every numerical step runs in the kernels of the other units.
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <algorithm>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <vector>
+
+#include "../../include/skewgpu.h"
+#include "skew_internal.h"
+
+using namespace skew;
+
+struct skew_handle_st {
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int sms = 0;
+  void* ws = nullptr;  // grow-only workspace, stream ordered
+  size_t ws_bytes = 0;
+};
+
+struct Bucket {
+  int begin, end, nmax, smem_matrix, grid;
+  int64_t gws_slot;  // doubles per CTA slot (global bucket)
+  size_t gws_off;    // offset of the bucket's slots in the plan workspace (doubles)
+};
+
+struct skew_batch_plan_st {
+  skew_handle_t h = nullptr;
+  int64_t count = 0;
+  std::vector<int32_t> n_host;
+  std::vector<Bucket> buckets;
+  int32_t* d_n = nullptr;
+  int32_t* d_order = nullptr;
+  int64_t* d_ev_off = nullptr;
+  unsigned* d_counters = nullptr;
+  double* d_ev = nullptr;
+  double* d_gws = nullptr;
+  int64_t ev_total = 0;
+  size_t gws_total = 0;
+};
+
+#define CK(x)                                  \
+  do {                                         \
+    cudaError_t e_ = (x);                      \
+    if (e_ != cudaSuccess) return SKEW_CUDA_ERROR; \
+  } while (0)
+
+static int ensure_ws(skew_handle_t h, size_t bytes) {
+  if (bytes <= h->ws_bytes) return SKEW_OK;
+  if (h->ws) CK(cudaFreeAsync(h->ws, h->stream));
+  h->ws = nullptr;
+  h->ws_bytes = 0;
+  CK(cudaMallocAsync(&h->ws, bytes, h->stream));
+  h->ws_bytes = bytes;
+  return SKEW_OK;
+}
+
+extern "C" {
+
+int skew_version(void) { return 100; }
+
+const char* skew_status_string(int s) {
+  switch (s) {
+    case SKEW_OK: return "ok";
+    case SKEW_NOT_SKEW: return "matrix is not skew-symmetric";
+    case SKEW_NO_CONVERGENCE: return "maximum number of iterations reached, the algorithm didn't converge";
+    case SKEW_BAD_ARG: return "bad argument";
+    case SKEW_CUDA_ERROR: return "CUDA error";
+    case SKEW_SINGULAR: return "singular (Pfaffian is zero)";
+    case SKEW_UNSUPPORTED: return "unsupported";
+    case SKEW_NO_MEMORY: return "out of memory";
+    case SKEW_FALLBACK_USED: return "QR stagnated; symmetric tridiagonal fallback used";
+    default: return "unknown status";
+  }
+}
+
+int skew_create(skew_handle_t* handle) {
+  if (!handle) return SKEW_BAD_ARG;
+  skew_handle_st* h = new (std::nothrow) skew_handle_st();
+  if (!h) return SKEW_NO_MEMORY;
+  if (cudaGetDevice(&h->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) {
+    delete h;
+    return SKEW_CUDA_ERROR;
+  }
+  *handle = h;
+  return SKEW_OK;
+}
+
+int skew_destroy(skew_handle_t h) {
+  if (!h) return SKEW_BAD_ARG;
+  if (h->ws) {
+    cudaFreeAsync(h->ws, h->stream);
+    cudaStreamSynchronize(h->stream);
+  }
+  delete h;
+  return SKEW_OK;
+}
+
+int skew_set_stream(skew_handle_t h, skew_stream_t s) {
+  if (!h) return SKEW_BAD_ARG;
+  if (h->ws && (cudaStream_t)s != h->stream) {  // keep the workspace ordered on the new stream
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(ev, h->stream));
+    CK(cudaStreamWaitEvent((cudaStream_t)s, ev, 0));
+    CK(cudaEventDestroy(ev));
+  }
+  h->stream = (cudaStream_t)s;
+  return SKEW_OK;
+}
+
+// Largest n handled by the one-CTA single-matrix kernel.
+static const int64_t kSingleMax = 1024;
+
+static int single(skew_handle_t h, double* A, int64_t n, int64_t lda, double* G, int64_t ldg, double* logpf,
+                  double* sign, double* ev, double* tau, int* info, int check, int want_pf) {
+  if (!h || n < 0 || (n > 0 && !A) || lda < (n > 0 ? n : 1)) return SKEW_BAD_ARG;
+  if (n > kSingleMax) return SKEW_UNSUPPORTED;
+  SingleParams P;
+  P.A = A;
+  P.lda = lda;
+  P.n = (int)n;
+  P.G = G;
+  P.ldg = ldg;
+  P.logpf = logpf;
+  P.sign = sign;
+  P.ev = ev;
+  P.tau = tau;
+  P.info = info;
+  P.check = check;
+  P.want_pf = want_pf;
+  CK(launch_single(P, h->stream));
+  return SKEW_OK;
+}
+
+int skew_hessenberg_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev, int* info) {
+  if (n > 1 && (!tau || !ev)) return SKEW_BAD_ARG;
+  return single(h, A, n, lda, nullptr, 0, nullptr, nullptr, n > 1 ? ev : nullptr, n > 1 ? tau : nullptr, info, 0,
+                0);
+}
+
+int skew_logabspf_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* sign, int check,
+                    int* info) {
+  if (!logpf || !sign) return SKEW_BAD_ARG;
+  return single(h, A, n, lda, nullptr, 0, logpf, sign, nullptr, nullptr, info, check, 1);
+}
+
+int skew_logabspf_grad_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* sign, double* G,
+                         int64_t ldg, int* info) {
+  if (!logpf || !sign || (n > 0 && (!G || ldg < n))) return SKEW_BAD_ARG;
+  return single(h, A, n, lda, G, ldg, logpf, sign, nullptr, nullptr, info, 0, 1);
+}
+
+int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info) {
+  if (!h || n < 0 || (n > 0 && (!A || !vals_im))) return SKEW_BAD_ARG;
+  if (n == 0) return SKEW_OK;
+  if (n == 1) {  // skeweigvals! n == 1 returns [A[1,1]] (eigen.jl:314)
+    CK(cudaMemcpyAsync(vals_im, A, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+    return SKEW_OK;
+  }
+  int st = ensure_ws(h, sizeof(double) * (size_t)(n + 2));
+  if (st) return st;
+  double* ev = (double*)h->ws;
+  st = single(h, A, n, lda, nullptr, 0, nullptr, nullptr, ev, nullptr, info, 0, 0);
+  if (st) return st;
+  CK(launch_tridiag_bisect(ev, (int)n, vals_im, ev + n, h->stream));
+  return SKEW_OK;
+}
+
+int skew_eigen_d(skew_handle_t, double*, int64_t, int64_t, double*, double*, double*, int64_t, int*) {
+  return SKEW_UNSUPPORTED;
+}
+int skew_exp_d(skew_handle_t, double*, int64_t, int64_t, double*, int64_t, int*) { return SKEW_UNSUPPORTED; }
+int skew_cis_d(skew_handle_t, double*, int64_t, int64_t, double*, int64_t, int*) { return SKEW_UNSUPPORTED; }
+
+// ---------------------------------------------------------------------------
+// Batched plans
+// ---------------------------------------------------------------------------
+
+// Size buckets: the working copy stays in shared memory up to n = 160 (205 KB);
+// larger matrices work in a per-CTA global slot (L2 resident).
+static const int kBucketEdges[] = {32, 64, 96, 128, 160};
+
+int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, skew_batch_plan_t* plan) {
+  if (!h || !plan || count < 0 || (count > 0 && !n)) return SKEW_BAD_ARG;
+  for (int64_t b = 0; b < count; b++)
+    if (n[b] < 0 || n[b] > kSingleMax) return SKEW_BAD_ARG;
+  skew_batch_plan_st* P = new (std::nothrow) skew_batch_plan_st();
+  if (!P) return SKEW_NO_MEMORY;
+  P->h = h;
+  P->count = count;
+  P->n_host.resize(count);
+  for (int64_t b = 0; b < count; b++) P->n_host[b] = (int32_t)n[b];
+  std::vector<int32_t> order(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) { return P->n_host[a] > P->n_host[b]; });
+  std::vector<int64_t> ev_off(count);
+  int64_t acc = 0;
+  for (int64_t b = 0; b < count; b++) {
+    ev_off[b] = acc;
+    acc += std::max<int32_t>(P->n_host[b], 1);
+  }
+  P->ev_total = acc;
+  // buckets over the sorted order
+  auto edge_of = [](int nn) {
+    for (int e : kBucketEdges)
+      if (nn <= e) return e;
+    return 1 << 30;
+  };
+  size_t gws_total = 0;
+  for (int64_t t = 0; t < count;) {
+    const int e = edge_of(P->n_host[order[t]]);
+    int64_t u = t;
+    while (u < count && edge_of(P->n_host[order[u]]) == e) u++;
+    Bucket B;
+    B.begin = (int)t;
+    B.end = (int)u;
+    B.nmax = std::max<int32_t>(P->n_host[order[t]], 1);
+    const size_t smem_full = batch_smem_bytes(B.nmax, true);
+    B.smem_matrix = (smem_full <= 220 * 1024) ? 1 : 0;
+    const size_t smem = batch_smem_bytes(B.nmax, B.smem_matrix != 0);
+    const int occ = batch_occupancy(smem);
+    B.grid = (int)std::min<int64_t>((int64_t)h->sms * occ, u - t);
+    B.gws_slot = B.smem_matrix ? 0 : (int64_t)B.nmax * (B.nmax | 1);
+    B.gws_off = gws_total;
+    gws_total += (size_t)B.gws_slot * B.grid;
+    P->buckets.push_back(B);
+    t = u;
+  }
+  P->gws_total = gws_total;
+  cudaStream_t st = h->stream;
+  bool ok = true;
+  ok &= cudaMallocAsync(&P->d_n, sizeof(int32_t) * std::max<int64_t>(count, 1), st) == cudaSuccess;
+  ok &= cudaMallocAsync(&P->d_order, sizeof(int32_t) * std::max<int64_t>(count, 1), st) == cudaSuccess;
+  ok &= cudaMallocAsync(&P->d_ev_off, sizeof(int64_t) * std::max<int64_t>(count, 1), st) == cudaSuccess;
+  ok &= cudaMallocAsync(&P->d_counters, sizeof(unsigned) * std::max<size_t>(P->buckets.size(), 1), st) ==
+        cudaSuccess;
+  ok &= cudaMallocAsync(&P->d_ev, sizeof(double) * std::max<int64_t>(P->ev_total, 1), st) == cudaSuccess;
+  if (gws_total) ok &= cudaMallocAsync(&P->d_gws, sizeof(double) * gws_total, st) == cudaSuccess;
+  if (ok && count) {
+    ok &= cudaMemcpyAsync(P->d_n, P->n_host.data(), sizeof(int32_t) * count, cudaMemcpyHostToDevice, st) ==
+          cudaSuccess;
+    ok &= cudaMemcpyAsync(P->d_order, order.data(), sizeof(int32_t) * count, cudaMemcpyHostToDevice, st) ==
+          cudaSuccess;
+    ok &= cudaMemcpyAsync(P->d_ev_off, ev_off.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, st) ==
+          cudaSuccess;
+    ok &= cudaStreamSynchronize(st) == cudaSuccess;  // host vectors go out of scope
+  }
+  if (!ok) {
+    skew_batch_plan_destroy(P);
+    return SKEW_CUDA_ERROR;
+  }
+  *plan = P;
+  return SKEW_OK;
+}
+
+int skew_batch_plan_destroy(skew_batch_plan_t P) {
+  if (!P) return SKEW_BAD_ARG;
+  cudaStream_t st = P->h ? P->h->stream : nullptr;
+  if (P->d_n) cudaFreeAsync(P->d_n, st);
+  if (P->d_order) cudaFreeAsync(P->d_order, st);
+  if (P->d_ev_off) cudaFreeAsync(P->d_ev_off, st);
+  if (P->d_counters) cudaFreeAsync(P->d_counters, st);
+  if (P->d_ev) cudaFreeAsync(P->d_ev, st);
+  if (P->d_gws) cudaFreeAsync(P->d_gws, st);
+  cudaStreamSynchronize(st);
+  delete P;
+  return SKEW_OK;
+}
+
+static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logpf, double* sign,
+                       double* const* grad, int* status, bool tridiag_only) {
+  cudaStream_t st = P->h->stream;
+  CK(cudaMemsetAsync(P->d_counters, 0, sizeof(unsigned) * std::max<size_t>(P->buckets.size(), 1), st));
+  for (size_t i = 0; i < P->buckets.size(); i++) {
+    const Bucket& B = P->buckets[i];
+    BatchParams bp;
+    bp.A = A;
+    bp.n = P->d_n;
+    bp.order = P->d_order;
+    bp.begin = B.begin;
+    bp.end = B.end;
+    bp.nmax = B.nmax;
+    bp.smem_matrix = B.smem_matrix;
+    bp.check = 0;
+    bp.gws = P->d_gws ? P->d_gws + B.gws_off : nullptr;
+    bp.gws_slot = B.gws_slot;
+    bp.counter = P->d_counters + i;
+    bp.logpf = logpf;
+    bp.sign = sign;
+    bp.grad = grad;
+    bp.ev_out = tridiag_only ? P->d_ev : nullptr;
+    bp.ev_off = P->d_ev_off;
+    bp.status = status;
+    CK(launch_batch_pf(bp, B.grid, st, tridiag_only));
+  }
+  return SKEW_OK;
+}
+
+int skew_batch_logabspf_d(skew_batch_plan_t P, const double* const* A, double* logpf, double* sign,
+                          double* const* grad, int* status) {
+  if (!P || (P->count > 0 && (!A || !logpf || !sign || !status))) return SKEW_BAD_ARG;
+  if (P->count == 0) return SKEW_OK;
+  return run_buckets(P, A, logpf, sign, grad, status, false);
+}
+
+int skew_batch_eigvals_d(skew_batch_plan_t P, const double* const* A, double* const* vals_im, int* status) {
+  if (!P || (P->count > 0 && (!A || !vals_im))) return SKEW_BAD_ARG;
+  if (P->count == 0) return SKEW_OK;
+  int s = run_buckets(P, A, nullptr, nullptr, nullptr, nullptr, true);
+  if (s) return s;
+  TrieigParams tp;
+  tp.ev_all = P->d_ev;
+  tp.ev_off = P->d_ev_off;
+  tp.n = P->d_n;
+  tp.order = P->d_order;
+  tp.count = (int32_t)P->count;
+  tp.evwork = P->d_ev;
+  tp.vals = vals_im;
+  tp.status = status;
+  CK(launch_batch_trieig(tp, P->h->stream));
+  return SKEW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// FP64 peak probe
+// ---------------------------------------------------------------------------
+int skew_measure_fp64_peak(skew_handle_t h, double* tflops) {
+  if (!h || !tflops) return SKEW_BAD_ARG;
+  const int blocks = h->sms * 4, iters = 4096;
+  int st = ensure_ws(h, sizeof(double) * (size_t)blocks * 128);
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(launch_dfma_probe((double*)h->ws, blocks, iters, h->stream));  // warm-up
+  float best = 1e30f;
+  for (int r = 0; r < 5; r++) {
+    CK(cudaEventRecord(e0, h->stream));
+    CK(launch_dfma_probe((double*)h->ws, blocks, iters, h->stream));
+    CK(cudaEventRecord(e1, h->stream));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    best = std::min(best, ms);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  const double flops = 2.0 * 8.0 * iters * (double)blocks * 128.0;
+  *tflops = flops / (best * 1e-3) / 1e12;
+  return SKEW_OK;
+}
+
+}  // extern "C"
+
+namespace skew {
+// Eight independent FMA chains per thread keep the FP64 pipe of every
+// sub-partition busy; the result is stored so nothing is optimised away.
+__global__ void dfma_probe_kernel(double* out, int iters, double a, double b) {
+  double x[8];
+#pragma unroll
+  for (int i = 0; i < 8; i++) x[i] = threadIdx.x * 1e-3 + i;
+  for (int it = 0; it < iters; it++) {
+#pragma unroll
+    for (int i = 0; i < 8; i++) x[i] = fma(x[i], a, b);
+  }
+  double s = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) s += x[i];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+cudaError_t launch_dfma_probe(double* out, int blocks, int iters, cudaStream_t st) {
+  dfma_probe_kernel<<<blocks, 128, 0, st>>>(out, iters, 1.0000001, 1e-9);
+  return cudaGetLastError();
+}
+}  // namespace skew

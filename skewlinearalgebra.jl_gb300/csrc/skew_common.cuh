@@ -1,0 +1,94 @@
+// Shared device helpers for libskewgpu (sm_103a, FP64).
+//
+// Cost model this code is written against (measured on GB300): the FP64 pipe of
+// an SM sub-partition retires one warp-wide DFMA every 64 cycles (1.19 TFLOP/s
+// per GPU), whatever the number of active lanes; a double divide or square
+// root costs about ten DFMAs.  So: every FP64 instruction should carry 32
+// useful lanes, scalar FP64 work stays off the critical path where it can, and
+// integer index arithmetic, loads and shuffles are close to free.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/skewgpu.h"
+
+namespace skew {
+
+constexpr int WARP = 32;
+
+// Negation by flipping the sign bit on the integer pipe (keeps the FP64 pipe free).
+__device__ __forceinline__ double neg(double x) {
+  return __hiloint2double(__double2hiint(x) ^ 0x80000000, __double2loint(x));
+}
+
+__device__ __forceinline__ double warp_sum(double x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  return x;
+}
+
+// Block-wide sum for a block of NW warps; red must hold NW doubles. All threads
+// get the result.  Contains two __syncthreads().
+template <int NW>
+__device__ __forceinline__ double block_sum(double x, double* red) {
+  x = warp_sum(x);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = x;
+  __syncthreads();
+  double s = 0;
+#pragma unroll
+  for (int i = 0; i < NW; i++) s += red[i];
+  __syncthreads();
+  return s;
+}
+
+// Householder reflector parameters following hessenberg.jl:26-44 (householder!):
+// beta = -sign(alpha) * hypot(alpha, |x|), tau = 1 - alpha/beta, v = [1; x/(alpha-beta)].
+// ss = |x|^2 (sum of squares of the part below alpha); xnorm_scaled >= 0 is |x|
+// computed with scaling, supplied by the caller only when ss over/underflowed
+// (then hypot is used, as the reference does).  One division is shared by tau
+// and the scale: with d = alpha - beta and r = 1/(beta*d), 1/beta = d*r and
+// 1/d = beta*r.
+struct Reflector {
+  double tau, beta, scale;
+};
+__device__ __forceinline__ bool ss_needs_scaling(double ss) { return !(ss < 1e290) || (ss > 0.0 && ss < 1e-290); }
+
+__device__ __forceinline__ Reflector make_reflector(double alpha, double ss, double xnorm_scaled) {
+  Reflector R;
+  if (ss == 0.0 && alpha == 0.0) {  // :38-41
+    R.tau = 0.0;
+    R.beta = 0.0;
+    R.scale = 0.0;
+    return R;
+  }
+  double h;
+  if (xnorm_scaled < 0.0 && fabs(alpha) < 1e145) {
+    h = sqrt(fma(alpha, alpha, ss));
+  } else {
+    h = hypot(alpha, xnorm_scaled < 0.0 ? sqrt(ss) : xnorm_scaled);
+  }
+  const double beta = alpha > 0.0 ? neg(h) : h;  // :33
+  const double d = alpha - beta;                 // never cancels: beta has the opposite sign
+  if (fabs(h) < 1e150 && fabs(h) > 1e-150) {
+    const double r = 1.0 / (beta * d);
+    R.tau = neg(d * (d * r));  // 1 - alpha/beta = -d/beta
+    R.scale = beta * r;        // 1/(alpha - beta)
+  } else {
+    R.tau = 1.0 - alpha / beta;
+    R.scale = 1.0 / d;
+  }
+  R.beta = beta;
+  return R;
+}
+
+// Bounded spin on a device flag: returns false if `limit` polls pass first.
+__device__ __forceinline__ bool spin_until_geq(const volatile unsigned* flag, unsigned target, long long limit) {
+  for (long long it = 0; it < limit; it++) {
+    if (*flag >= target) return true;
+    __nanosleep(64);
+  }
+  return false;
+}
+
+}  // namespace skew

@@ -1,0 +1,69 @@
+// Internal declarations shared by the libskewgpu translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace skew {
+
+// Batched one-CTA-per-matrix launches (skew_batch.cu).
+struct BatchParams {
+  const double* const* A;  // [count] device pointers, original order
+  const int32_t* n;        // [count] sizes, original order
+  const int32_t* order;    // processing order -> original index (largest first)
+  int32_t begin, end;      // slice of `order` handled by this launch
+  int32_t nmax;            // largest n in the slice
+  int32_t smem_matrix;     // 1: working copy in shared memory; 0: global slot
+  int32_t check;           // verify A == -A^T
+  double* gws;             // global workspace (one slot per CTA) when !smem_matrix
+  int64_t gws_slot;        // doubles per slot
+  unsigned* counter;       // work counter, zero before the launch
+  double* logpf;           // [count] or null
+  double* sign;            // [count] or null
+  double* const* grad;     // [count] device pointers or null
+  double* ev_out;          // packed ev (n-1 per matrix) or null
+  const int64_t* ev_off;   // offsets into ev_out
+  int* status;             // [count] or null
+};
+
+struct SingleParams {
+  double* A;
+  int64_t lda;
+  int n;
+  double* G;
+  int64_t ldg;
+  double* logpf;
+  double* sign;
+  double* ev;
+  double* tau;
+  int* info;
+  int check;
+  int want_pf;
+};
+
+size_t batch_smem_bytes(int nmax, bool smem_matrix);
+cudaError_t launch_batch_pf(const BatchParams& P, int grid, cudaStream_t st, bool tridiag_only);
+cudaError_t launch_single(const SingleParams& P, cudaStream_t st);
+int batch_threads();
+int batch_occupancy(size_t smem_bytes);  // resident CTAs per SM
+
+// Skew tridiagonal eigenvalues (skew_qr.cu).
+struct TrieigParams {
+  const double* ev_all;    // packed subdiagonals (n-1 per matrix)
+  const int64_t* ev_off;   // [count]
+  const int32_t* n;        // [count]
+  const int32_t* order;    // [count] processing order
+  int32_t count;
+  double* evwork;          // packed scratch, same layout as ev_all
+  double* const* vals;     // [count] device pointers (n[b] each)
+  int* status;             // [count] or null
+};
+cudaError_t launch_batch_trieig(const TrieigParams& P, cudaStream_t st);
+
+// Eigenvalues of one skew tridiagonal by bisection on the equivalent zero-diagonal
+// symmetric tridiagonal; vals_im sorted descending.
+cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, double* scratch2, cudaStream_t st);
+
+// FP64 DFMA microbenchmark kernel (skew_api.cu).
+cudaError_t launch_dfma_probe(double* out, int blocks, int iters, cudaStream_t st);
+
+}  // namespace skew

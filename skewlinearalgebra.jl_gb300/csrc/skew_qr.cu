@@ -1,0 +1,264 @@
+// Skew-symmetric tridiagonal eigenvalues.
+//
+// Batched path: the implicit-QR iteration of skewtrieigvals!
+// (skeweigen.jl:105-156) with its exact tolerances, shift, deflation order and
+// stagnation rule, one matrix per thread.  The iteration is a serial chain of
+// Givens rotations; since the FP64 pipe charges a warp instruction the same
+// whether one lane or 32 are active, 32 matrices share each warp (matrices are
+// sorted by size, so warp-mates run similar trip counts).
+//
+// Single large matrix: bisection with Sturm counts on the equivalent
+// zero-diagonal symmetric tridiagonal SymTridiagonal(0, ev), one eigenvalue per
+// thread across the whole GPU.  Values come out sorted descending, the order the
+// reference itself returns from its fallback (skeweigen.jl:134-137, 463-468).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "skew_common.cuh"
+#include "skew_internal.h"
+
+namespace skew {
+
+// getgivens (skeweigen.jl:3-7): c = a/hypot(a,b), s = b/hypot(a,b); (1, 0) if both
+// vanish.  One reciprocal square root in the common exponent range.
+__device__ __forceinline__ void givens(double a, double b, double& c, double& s) {
+  const int ea = (__double2hiint(a) >> 20) & 0x7ff, eb = (__double2hiint(b) >> 20) & 0x7ff;
+  const int em = max(ea, eb);
+  if (em >= 600 && em <= 1500) {
+    const double r = rsqrt(fma(a, a, b * b));
+    c = a * r;
+    s = b * r;
+  } else if (a == 0.0 && b == 0.0) {
+    c = 1.0;
+    s = 0.0;
+  } else {
+    const double nm = hypot(a, b);
+    c = a / nm;
+    s = b / nm;
+  }
+}
+
+// reducetozero (skeweigen.jl:11-47) for odd sizes; n = N-1 (even), G unused for values.
+__device__ void reducetozero_dev(double* ev, int n) {
+  if (n == 0) return;
+  double bulge = 0.0, c, s;
+  if (n > 2) {
+    const double a = ev[n - 3], b = ev[n - 2], g = ev[n - 1];
+    givens(-b, g, c, s);
+    ev[n - 3] *= c;
+    ev[n - 2] = c * b - s * g;
+    ev[n - 1] = 0.0;
+    bulge = -s * a;
+    for (int i = n - 2; i >= 4; i -= 2) {
+      const double a2 = ev[i - 3], b2 = ev[i - 2];
+      givens(-b2, bulge, c, s);
+      ev[i - 3] *= c;
+      ev[i - 2] = c * b2 - s * bulge;
+      bulge = -s * a2;
+    }
+  }
+  const double b = (n == 2 ? ev[1] : bulge);
+  const double a = ev[0];
+  givens(-a, b, c, s);
+  ev[0] = c * a - s * b;
+  if (n == 2) ev[1] = s * a + b * c;
+}
+
+// implicitstep_novec (skeweigen.jl:73-103); n = active size - 1, start 1-based.
+__device__ int implicitstep_dev(double* ev, int n, int start) {
+  double bulge = 0.0;
+  const double shift = ev[n - 1] * ev[n - 1];
+  const double tol = 2.220446049250313e-16;  // eps(Float64)
+  for (int i = start; i <= n - 1; i++) {
+    const double a = (i > start ? ev[i - 2] : 0.0);
+    const double b = ev[i - 1];
+    const double g = ev[i];
+    double c, s;
+    if (i > start) {
+      givens(a, bulge, c, s);
+    } else {
+      const double x1 = fma(-a, a, fma(-b, b, shift));
+      const double x2 = fma(-a, bulge, b * g);
+      givens(x1, x2, c, s);
+    }
+    if (i > 1) ev[i - 2] = fma(c, a, s * bulge);
+    ev[i - 1] = fma(c, b, -(s * g));
+    ev[i] = fma(s, b, c * g);
+    if (i < n - 1) {
+      const double z = ev[i + 1];
+      ev[i + 1] = z * c;
+      bulge = s * z;
+      if (fabs(bulge) < tol && fabs(ev[i - 1]) < tol) return i + 1;
+    }
+  }
+  return start;
+}
+
+// Number of eigenvalues of SymTridiagonal(0, e) (size n) smaller than x.
+__device__ int sturm_count(const double* e, int n, double x, double pivmin) {
+  double q = -x;
+  int c = (q < 0.0);
+  for (int i = 1; i < n; i++) {
+    if (fabs(q) <= pivmin) q = -pivmin;
+    const double ei = e[i - 1];
+    q = -x - (ei * ei) / q;
+    c += (q < 0.0);
+  }
+  return c;
+}
+
+// Descending eigenvalues of SymTridiagonal(0, e) by serial bisection (fallback
+// path inside the batched QR; rare).
+__device__ void bisect_serial(const double* e, int n, double* out) {
+  double bound = 0.0, emax2 = 0.0;
+  for (int i = 0; i < n; i++) {
+    const double l = (i > 0 ? fabs(e[i - 1]) : 0.0), r = (i + 1 < n ? fabs(e[i]) : 0.0);
+    bound = fmax(bound, l + r);
+    if (i + 1 < n) emax2 = fmax(emax2, e[i] * e[i]);
+  }
+  const double pivmin = 2.2250738585072014e-308 * fmax(1.0, emax2);
+  bound = bound * (1.0 + 1e-14) + 1e-300;
+  for (int k = 0; k < n; k++) {  // k-th largest = (n-1-k)-th smallest
+    double lo = -bound, hi = bound;
+    for (int it = 0; it < 120 && hi - lo > 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300; it++) {
+      const double mid = 0.5 * (lo + hi);
+      if (sturm_count(e, n, mid, pivmin) <= n - 1 - k)
+        lo = mid;
+      else
+        hi = mid;
+    }
+    out[k] = 0.5 * (lo + hi);
+  }
+}
+
+// skewtrieigvals! (skeweigen.jl:105-156).  ev (N-1 entries) is destroyed;
+// vals[N] receives the imaginary parts in the reference's order.
+__device__ int skewtrieigvals_dev(double* ev, int N, double* vals) {
+  int n = N;
+  for (int i = 0; i < N; i++) vals[i] = 0.0;
+  if (n & 1) {
+    n -= 1;
+    reducetozero_dev(ev, n);
+  }
+  const double tol = 10.0 * 2.220446049250313e-16;
+  const int max_iter = 30 * n;
+  int iter = 0, count_static = 0, start = 1;
+  double mem = 1.0;
+  while (n > 2 && iter < max_iter) {
+    start = implicitstep_dev(ev, n - 1, start);
+    while (n > 2 && fabs(ev[n - 2]) <= tol) {
+      vals[n - 1] = 0.0;
+      n -= 1;
+    }
+    while (n > 2 && fabs(ev[n - 3]) <= tol * fabs(ev[n - 2])) {
+      vals[n - 2] = ev[n - 2];
+      vals[n - 1] = neg(ev[n - 2]);
+      n -= 2;
+    }
+    if (start > n - 2) start = 1;
+    if (n > 1 && fabs(mem - ev[n - 2]) < 0.0001 * fabs(ev[n - 2])) {
+      count_static += 1;
+      if (count_static > 4) {  // stagnation: symmetric tridiagonal fallback (:134-137)
+        bisect_serial(ev, n, vals);
+        return SKEW_FALLBACK_USED;
+      }
+    } else {
+      count_static = 0;
+    }
+    mem = (n > 1 ? ev[n - 2] : 0.0);
+    iter += 1;
+  }
+  if (n == 2) {
+    vals[0] = ev[0];
+    vals[1] = neg(ev[0]);
+    return SKEW_OK;
+  }
+  if (n <= 1) {
+    if (n == 1) vals[0] = 0.0;
+    return SKEW_OK;
+  }
+  return SKEW_NO_CONVERGENCE;
+}
+
+__global__ void batch_trieig_kernel(TrieigParams P) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= P.count) return;
+  const int b = P.order[t];
+  const int N = P.n[b];
+  double* ev = P.evwork + P.ev_off[b];
+  if (P.evwork != P.ev_all)
+    for (int i = 0; i + 1 < N; i++) ev[i] = P.ev_all[P.ev_off[b] + i];
+  const int st = (N >= 1) ? skewtrieigvals_dev(ev, N, P.vals[b]) : SKEW_OK;
+  if (P.status) P.status[b] = st;
+}
+
+cudaError_t launch_batch_trieig(const TrieigParams& P, cudaStream_t st) {
+  if (P.count <= 0) return cudaSuccess;
+  const int bs = 32;
+  batch_trieig_kernel<<<(P.count + bs - 1) / bs, bs, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+// Gershgorin bound and pivmin in one small kernel so the host never waits.
+__global__ void bisect_prep_kernel(const double* __restrict__ e, int n, double* __restrict__ out2) {
+  __shared__ double red[2][32];
+  double bound = 0.0, emax2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double l = (i > 0 ? fabs(e[i - 1]) : 0.0), r = (i + 1 < n ? fabs(e[i]) : 0.0);
+    bound = fmax(bound, l + r);
+    if (i + 1 < n) emax2 = fmax(emax2, e[i] * e[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    bound = fmax(bound, __shfl_xor_sync(0xffffffffu, bound, o));
+    emax2 = fmax(emax2, __shfl_xor_sync(0xffffffffu, emax2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = bound;
+    red[1][threadIdx.x >> 5] = emax2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0, m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      b = fmax(b, red[0][w]);
+      m = fmax(m, red[1][w]);
+    }
+    out2[0] = b * (1.0 + 1e-14) + 1e-300;
+    out2[1] = 2.2250738585072014e-308 * fmax(1.0, m);
+  }
+}
+
+// One positive eigenvalue per thread: the k-th largest of SymTridiagonal(0, e).
+__global__ void bisect_kernel_dev(const double* __restrict__ e, int n, const double* __restrict__ bp,
+                                  double* __restrict__ vals) {
+  const int h = n / 2;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= h) {
+    if (k == h && (n & 1)) vals[h] = 0.0;
+    return;
+  }
+  const double bound = bp[0], pivmin = bp[1];
+  double lo = 0.0, hi = bound;
+  for (int it = 0; it < 120 && hi - lo > 2.220446049250313e-16 * hi + 1e-300; it++) {
+    const double mid = 0.5 * (lo + hi);
+    if (sturm_count(e, n, mid, pivmin) <= n - 1 - k)
+      lo = mid;
+    else
+      hi = mid;
+  }
+  const double x = 0.5 * (lo + hi);
+  vals[k] = x;
+  vals[n - 1 - k] = neg(x);
+}
+
+cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, double* scratch2, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  bisect_prep_kernel<<<1, 256, 0, st>>>(ev, n, scratch2);
+  const int h = n / 2 + 1;
+  const int bs = 128;
+  bisect_kernel_dev<<<(h + bs - 1) / bs, bs, 0, st>>>(ev, n, scratch2, vals_im);
+  return cudaGetLastError();
+}
+
+}  // namespace skew

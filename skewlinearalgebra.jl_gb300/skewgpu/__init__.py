@@ -1,0 +1,277 @@
+"""skewgpu -- host-side mirror of SkewLinearAlgebra.jl's skew-Householder API over
+the GB300 C ABI (libskewgpu.so).
+
+Names, argument meaning and error behaviour follow the Julia package:
+
+==========================  =====================================================
+Julia (SkewLinearAlgebra)   here
+==========================  =====================================================
+``SkewHermitian(A)``        :class:`SkewHermitian` (checks A == -A^T, skewhermitian.jl:23-26)
+``hessenberg(A)``           :func:`hessenberg` -> :class:`Hessenberg` (hessenberg.jl:5-15)
+``logabspfaffian(A)``       :func:`logabspfaffian` (pfaffian.jl:235-263)
+``logabspfaffian!(A)``      :func:`logabspfaffian_` (in place)
+``pfaffian(A)``             :func:`pfaffian` (real inputs: sign * exp(log|Pf|))
+``eigvals(A)``              :func:`eigvals` (eigen.jl:2-6)
+``rrule(logabspfaffian,A)`` :func:`logabspfaffian_rrule` (no reference counterpart)
+==========================  =====================================================
+
+Batched work goes through :class:`BatchPlan` (skew_batch_* in the C ABI).
+
+Matrices live on the GPU in Julia's column-major layout.  A torch tensor ``T``
+of shape (n, n) holds matrix ``A`` when ``T = A^T`` in torch's row-major sense
+(``T[j, i] == A[i, j]``); :func:`to_device` and :func:`from_device` convert.
+PyTorch is used only for device memory and streams; every computation runs in
+libskewgpu's kernels, and there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+from typing import List, Optional, Sequence, Tuple
+
+import numpy as np
+import torch
+
+from . import _lib
+from ._lib import SkewError, check
+
+__all__ = [
+    "SkewHermitian", "Hessenberg", "BatchPlan", "SkewError", "to_device", "from_device", "hessenberg",
+    "logabspfaffian", "logabspfaffian_", "pfaffian", "eigvals", "logabspfaffian_rrule", "handle",
+    "measure_fp64_peak",
+]
+
+_lib.load()  # fail loudly at import if the CUDA library is missing
+
+
+class _Handle:
+    def __init__(self):
+        h = ctypes.c_void_p()
+        check(_lib.load().skew_create(ctypes.byref(h)), "skew_create")
+        self.h = h
+        self.stream = None
+
+    def bind(self, stream: Optional[torch.cuda.Stream] = None) -> ctypes.c_void_p:
+        s = stream if stream is not None else torch.cuda.current_stream()
+        if self.stream != s.cuda_stream:
+            check(_lib.load().skew_set_stream(self.h, ctypes.c_void_p(s.cuda_stream)), "skew_set_stream")
+            self.stream = s.cuda_stream
+        return self.h
+
+
+_handles = {}
+
+
+def handle(device: Optional[int] = None) -> _Handle:
+    d = torch.cuda.current_device() if device is None else device
+    if d not in _handles:
+        with torch.cuda.device(d):
+            _handles[d] = _Handle()
+    return _handles[d]
+
+
+def _ptr(t: Optional[torch.Tensor]) -> ctypes.c_void_p:
+    return ctypes.c_void_p(0 if t is None else t.data_ptr())
+
+
+def to_device(A, device="cuda") -> torch.Tensor:
+    """Host matrix -> device tensor holding it column-major (T = A^T row-major)."""
+    A = np.asarray(A, dtype=np.float64)
+    return torch.from_numpy(np.ascontiguousarray(A.T)).to(device)
+
+
+def from_device(T: torch.Tensor) -> np.ndarray:
+    return T.detach().cpu().numpy().T.copy()
+
+
+class SkewHermitian:
+    """A real skew-symmetric Float64 matrix on the GPU (column-major storage).
+
+    ``SkewHermitian(A)`` verifies A == -A^T exactly like the reference
+    constructor (skewhermitian.jl:23-26) and raises ``ValueError`` otherwise.
+    """
+
+    def __init__(self, data, check_skew: bool = True):
+        if not isinstance(data, torch.Tensor):
+            data = to_device(data)
+        if data.dtype != torch.float64 or data.dim() != 2 or data.shape[0] != data.shape[1]:
+            raise ValueError("SkewHermitian expects a square float64 matrix")
+        if not data.is_cuda:
+            data = data.cuda()
+        self.data = data.contiguous()
+        if check_skew and not bool(torch.equal(self.data, -self.data.T)):
+            raise ValueError("Matrix is not skew-hermitian")
+
+    @property
+    def n(self) -> int:
+        return self.data.shape[0]
+
+    def copy(self) -> "SkewHermitian":
+        return SkewHermitian(self.data.clone(), check_skew=False)
+
+    def numpy(self) -> np.ndarray:
+        return from_device(self.data)
+
+
+def _as_skew(A) -> SkewHermitian:
+    return A if isinstance(A, SkewHermitian) else SkewHermitian(A)
+
+
+@dataclass
+class Hessenberg:
+    """Result of hessenberg(A): factors (reflectors below the subdiagonal, column
+    major as in ``F.factors``), tau and the subdiagonal ``ev`` of H."""
+
+    factors: torch.Tensor
+    tau: torch.Tensor
+    ev: torch.Tensor
+
+    def H(self) -> np.ndarray:
+        """Dense SkewHermTridiagonal(ev) on the host."""
+        e = self.ev.cpu().numpy()
+        n = len(e) + 1
+        T = np.zeros((n, n))
+        T[np.arange(1, n), np.arange(n - 1)] = e
+        T[np.arange(n - 1), np.arange(1, n)] = -e
+        return T
+
+
+def _info_tensor(k: int = 1) -> torch.Tensor:
+    return torch.zeros(k, dtype=torch.int32, device="cuda")
+
+
+def hessenberg(A) -> Hessenberg:
+    """LA.hessenberg(A::SkewHermitian) -- copy, then reduce in place on the GPU."""
+    S = _as_skew(A).copy()
+    n = S.n
+    tau = torch.zeros(max(n - 1, 0), dtype=torch.float64, device="cuda")
+    ev = torch.zeros(max(n - 1, 0), dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_hessenberg_d(h, _ptr(S.data), n, n, _ptr(tau), _ptr(ev), _ptr(info)), "hessenberg")
+    return Hessenberg(S.data, tau, ev)
+
+
+def logabspfaffian_(A, check_skew: bool = False) -> Tuple[float, float]:
+    """logabspfaffian!(A): in place, returns (log|Pf(A)|, sign)."""
+    S = _as_skew(A) if not isinstance(A, torch.Tensor) else SkewHermitian(A, check_skew=False)
+    n = S.n
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_logabspf_d(h, _ptr(S.data), n, n, ctypes.c_void_p(out.data_ptr()),
+                                      ctypes.c_void_p(out.data_ptr() + 8), int(check_skew), _ptr(info)),
+          "logabspfaffian")
+    st = int(info.item())
+    if st == _lib.SKEW_NOT_SKEW:
+        raise ValueError("Pfaffian requires a skew-Hermitian matrix")
+    lp, sg = out.tolist()
+    return lp, sg
+
+
+def logabspfaffian(A) -> Tuple[float, float]:
+    """logabspfaffian(A) (pfaffian.jl:236, :246): (log|Pf(A)|, sign); A is not modified.
+    Plain matrices are checked for exact skew-symmetry first (pfaffian.jl:255)."""
+    if isinstance(A, SkewHermitian):
+        return logabspfaffian_(A.copy())
+    S = SkewHermitian(A, check_skew=False)
+    return logabspfaffian_(S.copy(), check_skew=True)
+
+
+def pfaffian(A) -> float:
+    """pfaffian(A) for real A, returned as sign * exp(log|Pf|) (pfaffian.jl:74-84)."""
+    lp, sg = logabspfaffian(A)
+    return float(sg * np.exp(lp))
+
+
+def logabspfaffian_rrule(A):
+    """Forward (log|Pf|, sign) and a pullback: pullback(dlogpf) -> dA = dlogpf * 1/2 A^{-T}.
+
+    Gradient convention: entries are treated as independent, so G = 1/2 A^{-T}; for a
+    skew-constrained perturbation (A_ij += h, A_ji -= h) the derivative is
+    G_ij - G_ji = (A^{-T})_ij.
+    """
+    S = _as_skew(A).copy()
+    n = S.n
+    G = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_logabspf_grad_d(h, _ptr(S.data), n, n, ctypes.c_void_p(out.data_ptr()),
+                                           ctypes.c_void_p(out.data_ptr() + 8), _ptr(G), n, _ptr(info)),
+          "logabspfaffian_rrule")
+    lp, sg = out.tolist()
+
+    def pullback(dy: float = 1.0) -> torch.Tensor:
+        return G * dy  # column-major storage, like every device matrix here
+
+    return (lp, sg), pullback
+
+
+def eigvals(A) -> np.ndarray:
+    """eigvals(A::SkewHermitian{Float64}) -> complex numpy vector (0 + i*vals)."""
+    S = _as_skew(A).copy()
+    n = S.n
+    vals = torch.zeros(n, dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_eigvals_d(h, _ptr(S.data), n, n, _ptr(vals), _ptr(info)), "eigvals")
+    return 1j * vals.cpu().numpy()
+
+
+def measure_fp64_peak() -> float:
+    t = ctypes.c_double()
+    check(_lib.load().skew_measure_fp64_peak(handle().bind(), ctypes.byref(t)), "measure_fp64_peak")
+    return t.value
+
+
+class BatchPlan:
+    """A batch of real skew matrices of sizes ``sizes`` (skew_batch_plan_create).
+
+    Inputs are passed as device tensors (column-major storage, one per matrix)."""
+
+    def __init__(self, sizes: Sequence[int]):
+        self.sizes = np.asarray(sizes, dtype=np.int64)
+        self.count = len(self.sizes)
+        arr = (ctypes.c_int64 * max(self.count, 1))(*self.sizes.tolist())
+        p = ctypes.c_void_p()
+        self._h = handle()
+        check(_lib.load().skew_batch_plan_create(self._h.bind(), arr, self.count, ctypes.byref(p)),
+              "skew_batch_plan_create")
+        self.plan = p
+
+    def close(self):
+        if getattr(self, "plan", None) is not None and self.plan.value:
+            _lib.load().skew_batch_plan_destroy(self.plan)
+            self.plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @staticmethod
+    def pointer_array(tensors: Sequence[torch.Tensor]) -> torch.Tensor:
+        return torch.tensor([t.data_ptr() for t in tensors], dtype=torch.int64, device="cuda")
+
+    def logabspfaffian(self, A_ptrs: torch.Tensor, grad_ptrs: Optional[torch.Tensor] = None,
+                       logpf: Optional[torch.Tensor] = None, sign: Optional[torch.Tensor] = None,
+                       status: Optional[torch.Tensor] = None):
+        """Launch the batched log|Pf| (+ gradient) on the current stream.  A_ptrs /
+        grad_ptrs are device int64 tensors of device pointers (see pointer_array)."""
+        dev = "cuda"
+        logpf = torch.empty(self.count, dtype=torch.float64, device=dev) if logpf is None else logpf
+        sign = torch.empty(self.count, dtype=torch.float64, device=dev) if sign is None else sign
+        status = torch.empty(self.count, dtype=torch.int32, device=dev) if status is None else status
+        self._h.bind()
+        check(_lib.load().skew_batch_logabspf_d(self.plan, _ptr(A_ptrs), _ptr(logpf), _ptr(sign), _ptr(grad_ptrs),
+                                                _ptr(status)), "skew_batch_logabspf_d")
+        return logpf, sign, status
+
+    def eigvals(self, A_ptrs: torch.Tensor, val_ptrs: torch.Tensor, status: Optional[torch.Tensor] = None):
+        status = torch.empty(self.count, dtype=torch.int32, device="cuda") if status is None else status
+        self._h.bind()
+        check(_lib.load().skew_batch_eigvals_d(self.plan, _ptr(A_ptrs), _ptr(val_ptrs), _ptr(status)),
+              "skew_batch_eigvals_d")
+        return status
