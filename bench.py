@@ -1,0 +1,381 @@
+"""Benchmark: batched log|Pf| + gradient over uneven skew matrices on GB300.
+
+Workload (one step): 4096 real skew-symmetric Float64 matrices with even sizes n
+drawn uniformly from {16, 18, ..., 256}, entries (B - B^T)/2 with B iid
+N(0, 1/n) (seeded, synthetic); for every matrix log|Pf(A)|, its sign and the
+gradient 1/2 A^{-T} through the batched C-ABI entry point.  The inputs (766 MB)
+and gradients (766 MB) are each larger than L2, so no flush is needed between
+steps.
+
+value: matrices/s with inputs resident in HBM.  e2e: the same through the public
+API with pinned host buffers, the H2D copy of the inputs and the D2H copy of
+log|Pf|, sign and gradients inside the timed region.
+
+Multi-GPU (torchrun): every rank solves its own batch (weak scaling, no
+collective on the data path); value = all matrices / max-over-ranks time.
+
+--impl reference: the reference's CPU algorithm (the oracle's FP64 restatement of
+SkewLinearAlgebra.jl, since Julia is not available on the box) on the host
+cores, on a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "skewlinearalgebra.jl_gb300"))
+
+METRIC = "batched log|Pf|+grad matrices/s & n=8192 hessenberg GFLOP/s vs plain GPU, err≤1e-11"
+UNIT = "matrices/s"
+COUNT = 4096
+NMIN, NMAX = 16, 256
+SEED = 20261203
+
+
+def workload_sizes(count=COUNT, seed=SEED, rank=0):
+    rng = np.random.default_rng(seed + 7919 * rank)
+    return (2 * rng.integers(NMIN // 2, NMAX // 2 + 1, count)).astype(np.int64)
+
+
+def packed_inputs(sizes, seed=SEED, rank=0):
+    """Column-major matrices back to back; returns (buffer, offsets)."""
+    offs = np.zeros(len(sizes), dtype=np.int64)
+    offs[1:] = np.cumsum(sizes[:-1].astype(np.int64) ** 2)
+    total = int(offs[-1] + sizes[-1] ** 2)
+    buf = np.empty(total, dtype=np.float64)
+    rng = np.random.default_rng(seed + 104729 * (rank + 1))
+    for b, n in enumerate(sizes):
+        B = rng.standard_normal((n, n)) / np.sqrt(n)
+        buf[offs[b]:offs[b] + n * n] = ((B - B.T) / 2).ravel(order="F")
+    return buf, offs
+
+
+def flops_per_matrix(n):
+    """Algorithmic FP64 work: Householder tridiagonalisation 4/3 n^3 plus the
+    gradient Q (-1/2 T^{-1}) Q^T by two-sided reflector application 2 n^3."""
+    n = np.asarray(n, dtype=np.float64)
+    return 4.0 / 3.0 * n ** 3 + 2.0 * n ** 3
+
+
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_reference(sizes_all, steps, warmup, sample, nthreads, rank):
+    """The reference's CPU algorithm (oracle FP64 restatement) on a bounded sample."""
+    from oracle import oracle as O
+
+    sizes = sizes_all[:sample]
+    buf, offs = packed_inputs(sizes, rank=rank)
+    for _ in range(warmup):
+        O.batch_logabspfaffian_grad_packed(buf, offs, sizes, nthreads)
+    times = []
+    out = None
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        out = O.batch_logabspfaffian_grad_packed(buf, offs, sizes, nthreads)
+        times.append(time.perf_counter() - t0)
+    return len(sizes) / float(np.mean(times)), out, float(np.mean(times))
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    nthreads = os.cpu_count() or 1
+    sizes = workload_sizes()
+    sample = args.cpu_sample
+    value, _, sec = cpu_reference(sizes, max(1, args.steps), min(args.warmup, 1), sample, nthreads, 0)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"batched_logabspf_grad_{COUNT}x_even_n{NMIN}-{NMAX}", "count": COUNT,
+                   "n_range": [NMIN, NMAX], "sample": sample},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
+                         "sample": f"first {sample} matrices of the workload per step; Julia is absent on the box, "
+                                   "so the oracle's FP64 restatement of SkewLinearAlgebra.jl (logabspfaffian) "
+                                   "plus an FP64 Gauss-Jordan inverse for the gradient, OpenMP over matrices"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-sample", type=int, default=1024)
+    ap.add_argument("--plain-sample", type=int, default=256)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    import skewgpu
+
+    sizes = workload_sizes(rank=rank)
+    buf, offs = packed_inputs(sizes, rank=rank)
+    total = buf.size
+    h_in = torch.from_numpy(buf).pin_memory()
+    d_in = h_in.to("cuda")
+    d_grad = torch.empty(total, dtype=torch.float64, device="cuda")
+    base_in, base_g = d_in.data_ptr(), d_grad.data_ptr()
+    a_ptrs = torch.tensor((base_in + 8 * offs).tolist(), dtype=torch.int64, device="cuda")
+    g_ptrs = torch.tensor((base_g + 8 * offs).tolist(), dtype=torch.int64, device="cuda")
+    plan = skewgpu.BatchPlan(sizes)
+    logpf = torch.empty(COUNT, dtype=torch.float64, device="cuda")
+    sign = torch.empty_like(logpf)
+    status = torch.empty(COUNT, dtype=torch.int32, device="cuda")
+    stream = torch.cuda.current_stream()
+    fp64_peak = skewgpu.measure_fp64_peak()
+
+    def step():
+        plan.logabspfaffian(a_ptrs, g_ptrs, logpf, sign, status)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    barrier()
+    st = status.cpu().numpy()
+    clocks = ClockSampler(local)
+    clocks.start()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    t0 = time.perf_counter()
+    ev0.record(stream)
+    for _ in range(args.steps):
+        step()
+    ev1.record(stream)
+    barrier()
+    wall = time.perf_counter() - t0
+    ms_dev = ev0.elapsed_time(ev1)
+    sec = ms_dev / 1e3
+    if dist is not None:
+        t = torch.tensor([sec], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        sec = float(t.item())
+    value = world * COUNT * args.steps / sec
+
+    # e2e through the public API: pinned host in -> device, results -> pinned host
+    h_lp = torch.empty(COUNT, dtype=torch.float64).pin_memory()
+    h_sg = torch.empty_like(h_lp).pin_memory()
+    h_g = torch.empty(total, dtype=torch.float64).pin_memory()
+    e2e_steps = max(1, min(args.steps, 5))
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        d_in.copy_(h_in, non_blocking=True)
+        step()
+        h_lp.copy_(logpf, non_blocking=True)
+        h_sg.copy_(sign, non_blocking=True)
+        h_g.copy_(d_grad, non_blocking=True)
+    e1.record(stream)
+    barrier()
+    clk = clocks.stop()
+    e2e_sec = e0.elapsed_time(e1) / 1e3
+    if dist is not None:
+        t = torch.tensor([e2e_sec], device="cuda", dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_sec = float(t.item())
+    e2e_value = world * COUNT * e2e_steps / e2e_sec
+
+    # roofline of the dominant kernel (batch_pf_kernel: every launch of a step)
+    flops = float(flops_per_matrix(sizes).sum())
+    achieved_tflops = flops / (ms_dev / args.steps / 1e3) / 1e12
+
+    # plain per-matrix GPU path: single-matrix C-ABI call looped over a sample
+    plain = None
+    if args.plain_sample > 0:
+        idx = np.arange(min(args.plain_sample, COUNT))
+        mats = [d_in[offs[b]:offs[b] + sizes[b] ** 2].view(int(sizes[b]), int(sizes[b])) for b in idx]
+        gbuf = [torch.empty_like(m) for m in mats]
+        import ctypes
+
+        L = skewgpu._lib.load()
+        h = skewgpu.handle().bind()
+        work = [m.clone() for m in mats]
+        outs = torch.empty(2 * len(idx), dtype=torch.float64, device="cuda")
+        info = torch.empty(len(idx), dtype=torch.int32, device="cuda")
+
+        def refill():
+            for k in range(len(idx)):
+                work[k].copy_(mats[k])
+
+        def plain_pass():
+            for k, b in enumerate(idx):
+                L.skew_logabspf_grad_d(h, ctypes.c_void_p(work[k].data_ptr()), int(sizes[b]), int(sizes[b]),
+                                       ctypes.c_void_p(outs.data_ptr() + 16 * k),
+                                       ctypes.c_void_p(outs.data_ptr() + 16 * k + 8),
+                                       ctypes.c_void_p(gbuf[k].data_ptr()), int(sizes[b]),
+                                       ctypes.c_void_p(info.data_ptr() + 4 * k))
+
+        refill()
+        plain_pass()
+        refill()
+        torch.cuda.synchronize()
+        p0, p1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        p0.record(stream)
+        plain_pass()
+        p1.record(stream)
+        torch.cuda.synchronize()
+        plain_val = len(idx) / (p0.elapsed_time(p1) / 1e3)
+        # same sample through the batched path (a plan over the sample only)
+        splan = skewgpu.BatchPlan(sizes[idx])
+        sa = a_ptrs[: len(idx)]
+        sg_ = g_ptrs[: len(idx)]
+        slp = torch.empty(len(idx), dtype=torch.float64, device="cuda")
+        ssg = torch.empty_like(slp)
+        sst = torch.empty(len(idx), dtype=torch.int32, device="cuda")
+        splan.logabspfaffian(sa, sg_, slp, ssg, sst)
+        torch.cuda.synchronize()
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        for _ in range(3):
+            splan.logabspfaffian(sa, sg_, slp, ssg, sst)
+        q1.record(stream)
+        torch.cuda.synchronize()
+        batched_sample_val = 3 * len(idx) / (q0.elapsed_time(q1) / 1e3)
+        splan.close()
+        plain = {"value": plain_val, "unit": UNIT, "sample": int(len(idx)),
+                 "batched_same_sample": batched_sample_val, "speedup_full_batch": value / world / plain_val,
+                 "speedup_same_sample": batched_sample_val / plain_val}
+
+    cpu = None
+    check = None
+    if rank == 0 and not args.no_cpu:
+        nthreads = os.cpu_count() or 1
+        cval, (clp, csg, cgrad), _ = cpu_reference(sizes, 1, 0, args.cpu_sample, nthreads, rank)
+        cpu = {"value": cval, "unit": UNIT, "cores": nthreads, "kind": "port",
+               "sample": f"first {args.cpu_sample} matrices of the workload, one pass; oracle FP64 restatement of "
+                         "logabspfaffian + FP64 Gauss-Jordan gradient, OpenMP over matrices"}
+        k = args.cpu_sample
+        glp = logpf[:k].cpu().numpy()
+        gsg = sign[:k].cpu().numpy()
+        rel = np.abs(glp - clp) / np.maximum(1.0, np.abs(clp))
+        gg = d_grad[: int(offs[k - 1] + sizes[k - 1] ** 2)].cpu().numpy()
+        gerr = 0.0
+        for b in range(k):
+            a, e = int(offs[b]), int(offs[b] + sizes[b] ** 2)
+            gerr = max(gerr, float(np.abs(gg[a:e] - cgrad[a:e]).max() / np.abs(cgrad[a:e]).max()))
+        check = {"max_rel_logpf_vs_cpu": float(rel.max()), "sign_mismatches": int((gsg != csg).sum()),
+                 "max_rel_grad_vs_cpu": gerr, "matrices": k, "status_nonzero": int((st != 0).sum())}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": ms_dev / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
+            "config": {"workload": f"batched_logabspf_grad_{COUNT}x_even_n{NMIN}-{NMAX}", "count": COUNT,
+                       "n_range": [NMIN, NMAX], "entries": "(B-B^T)/2, B~N(0,1/n)",
+                       "l2": "inputs and gradients each 766 MB > L2; no flush", "parallelism": f"replica x{world}"},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(total * 8),
+                    "d2h_bytes_per_step": int(total * 8 + COUNT * 16), "steps": e2e_steps},
+            "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
+                         "frac": achieved_tflops / fp64_peak, "traffic": None,
+                         "peak_source": "FP64 DFMA peak measured live by skew_measure_fp64_peak "
+                                        "(MEASURED_PEAKS.json has no FP64 figure)",
+                         "algorithmic_flops_per_step": flops, "kernel": "batch_pf_kernel"},
+            "gpu_launches": int(args.steps * len(set(_bucket_ids(sizes)))),
+            "clocks": clk,
+            "wall_s": wall,
+        }
+        if cpu:
+            line["cpu_baseline"] = cpu
+        if check:
+            line["check"] = check
+        if plain:
+            line["plain_gpu"] = plain
+        print(json.dumps(line), flush=True)
+    plan.close()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def _bucket_ids(sizes):
+    edges = [32, 64, 96, 128, 160]
+    out = []
+    for n in sizes:
+        out.append(next((e for e in edges if n <= e), 1 << 30))
+    return out
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -70,6 +70,8 @@ def lib():
         _lib.orc_symtri_eigvals_q.argtypes = [_D, _D, _I64, _D]
         _lib.orc_batch_logabspf_d.argtypes = [_D, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _I64, _D, _D,
                                               ctypes.c_int]
+        _lib.orc_batch_logabspf_grad_d.argtypes = [_D, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _I64, _D, _D,
+                                                   _D, ctypes.c_int]
     return _lib
 
 
@@ -265,6 +267,18 @@ def batch_logabspfaffian_packed(buf, offs, ns, nthreads: int = 1):
     lib().orc_batch_logabspf_d(_p(buf), offs.ctypes.data_as(ctypes.POINTER(_I64)),
                                ns.ctypes.data_as(ctypes.POINTER(_I64)), count, _p(lp), _p(sg), int(nthreads))
     return lp, sg
+
+
+def batch_logabspfaffian_grad_packed(buf, offs, ns, nthreads: int = 1):
+    """FP64 log|Pf| + 1/2 A^{-T} over a packed batch (OpenMP across matrices)."""
+    count = len(ns)
+    lp = np.zeros(count)
+    sg = np.zeros(count)
+    grad = np.zeros_like(buf)
+    lib().orc_batch_logabspf_grad_d(_p(buf), offs.ctypes.data_as(ctypes.POINTER(_I64)),
+                                    ns.ctypes.data_as(ctypes.POINTER(_I64)), count, _p(lp), _p(sg), _p(grad),
+                                    int(nthreads))
+    return lp, sg, grad
 
 
 # ---------------------------------------------------------------------------

@@ -1097,4 +1097,26 @@ void orc_batch_logabspf_d(const double* A, const int64_t* off, const int64_t* n,
   (void)nthreads;
 }
 
+// Batched FP64 log|Pf| + gradient (the CPU baseline for the batched adjoint
+// workload): the restated logabspfaffian plus 1/2 A^{-T} from an FP64
+// Gauss-Jordan inverse, OpenMP across matrices.  grad has the same packing as A.
+void orc_batch_logabspf_grad_d(const double* A, const int64_t* off, const int64_t* n, int64_t count, double* logpf,
+                               double* sign, double* grad, int nthreads) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+  for (int64_t b = 0; b < count; b++) {
+    const int64_t m = n[b];
+    logabspf<double>(A + off[b], m, logpf + b, sign + b);
+    std::vector<double> B(A + off[b], A + off[b] + m * m), X;
+    if (gj_inverse<double>(B, m, X) == 0) {
+      for (int64_t j = 0; j < m; j++)
+        for (int64_t i = 0; i < m; i++) grad[off[b] + i + j * m] = 0.5 * X[j + i * m];
+    } else {
+      for (int64_t k = 0; k < m * m; k++) grad[off[b] + k] = std::numeric_limits<double>::quiet_NaN();
+    }
+  }
+  (void)nthreads;
+}
+
 }  // extern "C"

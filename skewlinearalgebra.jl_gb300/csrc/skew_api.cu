@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <numeric>
@@ -120,7 +121,7 @@ static const int64_t kSingleMax = 1024;
 
 static int single(skew_handle_t h, double* A, int64_t n, int64_t lda, double* G, int64_t ldg, double* logpf,
                   double* sign, double* ev, double* tau, int* info, int check, int want_pf) {
-  if (!h || n < 0 || (n > 0 && !A) || lda < (n > 0 ? n : 1)) return SKEW_BAD_ARG;
+  if (!h || n < 0 || (n > 0 && (!A || lda < n))) return SKEW_BAD_ARG;
   if (n > kSingleMax) return SKEW_UNSUPPORTED;
   SingleParams P;
   P.A = A;
@@ -188,6 +189,15 @@ int skew_cis_d(skew_handle_t, double*, int64_t, int64_t, double*, int64_t, int*)
 // larger matrices work in a per-CTA global slot (L2 resident).
 static const int kBucketEdges[] = {32, 64, 96, 128, 160};
 
+// Tunables (environment overrides for sweeps): largest n whose working copy is
+// kept in shared memory, and resident CTAs per SM for the global-memory bucket
+// (each holds an n x n working copy; 2 per SM keeps 152 * 2 * 0.5 MB in L2).
+static int env_int(const char* name, int dflt) {
+  const char* v = getenv(name);
+  if (!v || !*v) return dflt;
+  return atoi(v);
+}
+
 int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, skew_batch_plan_t* plan) {
   if (!h || !plan || count < 0 || (count > 0 && !n)) return SKEW_BAD_ARG;
   for (int64_t b = 0; b < count; b++)
@@ -224,9 +234,10 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
     B.end = (int)u;
     B.nmax = std::max<int32_t>(P->n_host[order[t]], 1);
     const size_t smem_full = batch_smem_bytes(B.nmax, true);
-    B.smem_matrix = (smem_full <= 220 * 1024) ? 1 : 0;
+    B.smem_matrix = (smem_full <= 220 * 1024 && B.nmax <= env_int("SKEW_BATCH_SMEM_NMAX", 160)) ? 1 : 0;
     const size_t smem = batch_smem_bytes(B.nmax, B.smem_matrix != 0);
-    const int occ = batch_occupancy(smem);
+    int occ = batch_occupancy(smem);
+    if (!B.smem_matrix) occ = std::max(1, std::min(occ, env_int("SKEW_BATCH_GLOBAL_CTAS_PER_SM", 2)));
     B.grid = (int)std::min<int64_t>((int64_t)h->sms * occ, u - t);
     B.gws_slot = B.smem_matrix ? 0 : (int64_t)B.nmax * (B.nmax | 1);
     B.gws_off = gws_total;

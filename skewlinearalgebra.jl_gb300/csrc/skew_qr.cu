@@ -95,14 +95,18 @@ __device__ int implicitstep_dev(double* ev, int n, int start) {
   return start;
 }
 
-// Number of eigenvalues of SymTridiagonal(0, e) (size n) smaller than x.
+// Number of eigenvalues of SymTridiagonal(0, e) (size n) smaller than x: the
+// count of negative pivots of the LDL^T factorisation of (T - x I), a pivot
+// smaller than pivmin in magnitude being replaced by -pivmin before it is
+// counted and used.
 __device__ int sturm_count(const double* e, int n, double x, double pivmin) {
   double q = -x;
+  if (fabs(q) <= pivmin) q = -pivmin;
   int c = (q < 0.0);
   for (int i = 1; i < n; i++) {
-    if (fabs(q) <= pivmin) q = -pivmin;
     const double ei = e[i - 1];
     q = -x - (ei * ei) / q;
+    if (fabs(q) <= pivmin) q = -pivmin;
     c += (q < 0.0);
   }
   return c;
