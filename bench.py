@@ -41,9 +41,9 @@ NMIN, NMAX = 16, 256
 SEED = 20261203
 
 
-def workload_sizes(count=COUNT, seed=SEED, rank=0):
+def workload_sizes(count=COUNT, seed=SEED, rank=0, nmin=NMIN, nmax=NMAX):
     rng = np.random.default_rng(seed + 7919 * rank)
-    return (2 * rng.integers(NMIN // 2, NMAX // 2 + 1, count)).astype(np.int64)
+    return (2 * rng.integers(nmin // 2, nmax // 2 + 1, count)).astype(np.int64)
 
 
 def packed_inputs(sizes, seed=SEED, rank=0):
@@ -166,6 +166,9 @@ def main():
     ap.add_argument("--cpu-sample", type=int, default=1024)
     ap.add_argument("--plain-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--count", type=int, default=COUNT, help="matrices per step (profiling cases)")
+    ap.add_argument("--nmin", type=int, default=NMIN)
+    ap.add_argument("--nmax", type=int, default=NMAX)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -184,7 +187,8 @@ def main():
 
     import skewgpu
 
-    sizes = workload_sizes(rank=rank)
+    count = args.count
+    sizes = workload_sizes(count, rank=rank, nmin=args.nmin, nmax=args.nmax)
     buf, offs = packed_inputs(sizes, rank=rank)
     total = buf.size
     h_in = torch.from_numpy(buf).pin_memory()
@@ -194,9 +198,9 @@ def main():
     a_ptrs = torch.tensor((base_in + 8 * offs).tolist(), dtype=torch.int64, device="cuda")
     g_ptrs = torch.tensor((base_g + 8 * offs).tolist(), dtype=torch.int64, device="cuda")
     plan = skewgpu.BatchPlan(sizes)
-    logpf = torch.empty(COUNT, dtype=torch.float64, device="cuda")
+    logpf = torch.empty(count, dtype=torch.float64, device="cuda")
     sign = torch.empty_like(logpf)
-    status = torch.empty(COUNT, dtype=torch.int32, device="cuda")
+    status = torch.empty(count, dtype=torch.int32, device="cuda")
     stream = torch.cuda.current_stream()
     fp64_peak = skewgpu.measure_fp64_peak()
 
@@ -230,10 +234,10 @@ def main():
         t = torch.tensor([sec], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         sec = float(t.item())
-    value = world * COUNT * args.steps / sec
+    value = world * count * args.steps / sec
 
     # e2e through the public API: pinned host in -> device, results -> pinned host
-    h_lp = torch.empty(COUNT, dtype=torch.float64).pin_memory()
+    h_lp = torch.empty(count, dtype=torch.float64).pin_memory()
     h_sg = torch.empty_like(h_lp).pin_memory()
     h_g = torch.empty(total, dtype=torch.float64).pin_memory()
     e2e_steps = max(1, min(args.steps, 5))
@@ -254,7 +258,7 @@ def main():
         t = torch.tensor([e2e_sec], device="cuda", dtype=torch.float64)
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_sec = float(t.item())
-    e2e_value = world * COUNT * e2e_steps / e2e_sec
+    e2e_value = world * count * e2e_steps / e2e_sec
 
     # roofline of the dominant kernel (batch_pf_kernel: every launch of a step)
     flops = float(flops_per_matrix(sizes).sum())
@@ -263,7 +267,7 @@ def main():
     # plain per-matrix GPU path: single-matrix C-ABI call looped over a sample
     plain = None
     if args.plain_sample > 0:
-        idx = np.arange(min(args.plain_sample, COUNT))
+        idx = np.arange(min(args.plain_sample, count))
         mats = [d_in[offs[b]:offs[b] + sizes[b] ** 2].view(int(sizes[b]), int(sizes[b])) for b in idx]
         gbuf = [torch.empty_like(m) for m in mats]
         import ctypes
@@ -342,11 +346,11 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": ms_dev / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
-            "config": {"workload": f"batched_logabspf_grad_{COUNT}x_even_n{NMIN}-{NMAX}", "count": COUNT,
-                       "n_range": [NMIN, NMAX], "entries": "(B-B^T)/2, B~N(0,1/n)",
+            "config": {"workload": f"batched_logabspf_grad_{count}x_even_n{args.nmin}-{args.nmax}", "count": count,
+                       "n_range": [args.nmin, args.nmax], "entries": "(B-B^T)/2, B~N(0,1/n)",
                        "l2": "inputs and gradients each 766 MB > L2; no flush", "parallelism": f"replica x{world}"},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(total * 8),
-                    "d2h_bytes_per_step": int(total * 8 + COUNT * 16), "steps": e2e_steps},
+                    "d2h_bytes_per_step": int(total * 8 + count * 16), "steps": e2e_steps},
             "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": achieved_tflops / fp64_peak, "traffic": None,
                          "peak_source": "FP64 DFMA peak measured live by skew_measure_fp64_peak "

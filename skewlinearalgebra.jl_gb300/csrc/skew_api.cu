@@ -235,8 +235,7 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
     B.nmax = std::max<int32_t>(P->n_host[order[t]], 1);
     const size_t smem_full = batch_smem_bytes(B.nmax, true);
     B.smem_matrix = (smem_full <= 220 * 1024 && B.nmax <= env_int("SKEW_BATCH_SMEM_NMAX", 160)) ? 1 : 0;
-    const size_t smem = batch_smem_bytes(B.nmax, B.smem_matrix != 0);
-    int occ = batch_occupancy(smem);
+    int occ = batch_occupancy(B.nmax, B.smem_matrix != 0);
     if (!B.smem_matrix) occ = std::max(1, std::min(occ, env_int("SKEW_BATCH_GLOBAL_CTAS_PER_SM", 2)));
     B.grid = (int)std::min<int64_t>((int64_t)h->sms * occ, u - t);
     B.gws_slot = B.smem_matrix ? 0 : (int64_t)B.nmax * (B.nmax | 1);

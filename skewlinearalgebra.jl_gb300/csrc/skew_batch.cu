@@ -2,33 +2,31 @@
 //
 // Working copy.  A CTA works on a full-storage copy W of its matrix (both
 // triangles kept, W[j,i] = -W[i,j]).  In the batched path W lives in dynamic
-// shared memory when the size bucket fits, otherwise in a per-CTA slot of a
-// global workspace; in the single-matrix path W is the caller's matrix itself
-// (in place, as hessenberg!/logabspfaffian! are).  The code is the same for all
-// three (generic addressing).  Leading dimensions of private copies are odd so
-// that transposed stores do not conflict in shared-memory banks.
+// shared memory when the size bucket fits (template SM = true: every access is
+// a shared-memory instruction), otherwise in a per-CTA slot of a global
+// workspace; in the single-matrix path W is the caller's matrix itself (in
+// place, as hessenberg!/logabspfaffian! are).  Leading dimensions of private
+// copies are odd so transposed stores do not conflict in shared-memory banks.
 //
-// Reduction step k (reflector acting on indices k+1..n-1, m = n-k-1):
-//   1. ss = |W[k+2:n, k]|^2                        (block reduction)
-//   2. beta, tau, scale as householder! does (hessenberg.jl:26-44); every
-//      thread computes them redundantly, which costs the FP64 pipe no more
-//      than one thread would and saves a broadcast barrier
-//   3. v = [1; W[k+2:n,k]*scale], stored back into column k (the reflector,
-//      v[1] = 1 on the subdiagonal as the reference stores it)
-//   4. p = tau * W[k+1:n, k+1:n] v                 (full-row products)
-//   5. W[i,j] += v_i p_j - p_i v_j for k < j < i, mirrored to W[j,i]
-// Step 5 is the two-sided application H W H = W + v p^T - p v^T, exact for a
-// skew W because v^T W v = 0.  Steps 4 and 5 cost m^2 FMAs each, the minimum for
-// this reduction (4/3 n^3 flops in total); the reference's unblocked tail
-// (skewhess!, hessenberg.jl:70-90) spends 4 m^2 on the same step.  The elements
-// of step 5 are dealt out from the flattened lower triangle so every FP64
-// instruction carries 32 useful lanes.
+// Forward reduction, step k (reflector acting on indices k+1..n-1):
+//   1. p = tau_k * W[k+1:n, k+1:n] v_k       (full-row products, lanes = rows)
+//   2. W[i,j] += v_i p_j - p_i v_j, k < j < i, mirrored (two-sided H W H; exact
+//      for skew W since v^T W v = 0).  While warps 1.. update the bulk, warp 0
+//      updates column k+1 first and builds reflector k+1 from it (householder!,
+//      hessenberg.jl:26-44), so the serial norm/sqrt/divide chain of the next
+//      step is hidden behind this step's update.
+// Steps 1 and 2 cost m^2 FMAs each (4/3 n^3 flops in total).
 //
 // Gradient (the spec adjoint; the reference has no rrule):
 // d log|Pf(A)|/dA = 1/2 A^{-T} = -1/2 A^{-1} = Q (-1/2 T^{-1}) Q^T with
 // Q = H_0 H_1 ... H_{n-3}.  Starting from M = -1/2 T^{-1}, the reflectors are
-// applied innermost first with the same two-sided update, now over all n rows
-// (2 n m FMAs per reflector, 2 n^3 flops in total).
+// applied innermost first in blocks of GNB.  A block Q_b = I - V T_b V^T
+// (compact WY, T_b upper triangular) acts as one skew rank-2*GNB update:
+//   X = M V,  Z = X T_b^T,  K = V^T X,  C = T_b K T_b^T,  Z' = Z - 1/2 V C,
+//   Q_b M Q_b^T = M + V Z'^T - Z' V^T,
+// which is the same 2 n m FMAs per reflector as applying them one at a time, but
+// as register-tiled products that read M once per block instead of once per
+// reflector.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -38,49 +36,67 @@
 
 namespace skew {
 
-constexpr int BT = 128;  // threads per CTA
-constexpr int NW = BT / WARP;
+constexpr int GNB = 8;  // reflectors per block in the gradient
 
-// Shared vectors (nmax entries each) carved from dynamic shared memory.
-struct Vecs {
-  double* v;      // reflector
-  double* p;      // tau * W v
-  double* ypart;  // NW partial row products, stride nmax
-  double* ev;     // subdiagonal of T
-  double* tau;    // reflector scalars
-  double* red;    // NW doubles of scratch for block reductions
+// ---------------------------------------------------------------------------
+// Matrix accessors: shared-memory (offset into the dynamic shared array) or
+// global (pointer).  Distinct types so shared accesses compile to shared-memory
+// instructions.
+// ---------------------------------------------------------------------------
+extern __shared__ __align__(16) double dsm[];
+
+struct SMat {
+  int off, ld;
+  __device__ __forceinline__ double& at(int i, int j) const { return dsm[off + i + j * ld]; }
+};
+struct GMat {
+  double* p;
+  int64_t ld;
+  __device__ __forceinline__ double& at(int i, int j) const { return p[i + (int64_t)j * ld]; }
+};
+
+// ---------------------------------------------------------------------------
+// Shared-memory layout (doubles)
+// ---------------------------------------------------------------------------
+struct Smem {
+  double *ev, *tau, *red, *T, *P, *K, *C;
+  double *vb0, *vb1, *p, *ypart;  // forward view of the union
+  double *Vs, *Zs, *Xp;           // gradient view of the union
   int nmax;
 };
 
-__host__ __device__ constexpr int vec_doubles(int nmax) { return (4 + NW) * nmax + 2 * NW; }
+__host__ __device__ inline int union_doubles(int nmax, int nw) {
+  const int f = (3 + nw) * nmax;
+  const int g = 2 * GNB * nmax + nw * 32 * GNB;
+  return f > g ? f : g;
+}
+__host__ __device__ inline int fixed_doubles(int nmax) { return 2 * nmax + 64 + 4 * GNB * GNB; }
+__host__ __device__ inline int smem_doubles(int nmax, int nw) {
+  return fixed_doubles(nmax) + union_doubles(nmax, nw);
+}
 
-__device__ __forceinline__ Vecs carve(double* base, int nmax) {
-  Vecs s;
-  s.v = base;
-  s.p = base + nmax;
-  s.ypart = base + 2 * nmax;
-  s.ev = base + (2 + NW) * nmax;
-  s.tau = base + (3 + NW) * nmax;
-  s.red = base + (4 + NW) * nmax;
+__device__ __forceinline__ Smem carve(int nmax) {
+  Smem s;
   s.nmax = nmax;
+  s.ev = dsm;
+  s.tau = dsm + nmax;
+  s.red = dsm + 2 * nmax;
+  s.T = s.red + 64;
+  s.P = s.T + GNB * GNB;
+  s.K = s.P + GNB * GNB;
+  s.C = s.K + GNB * GNB;
+  double* u = s.C + GNB * GNB;
+  s.vb0 = u;
+  s.vb1 = u + nmax;
+  s.p = u + 2 * nmax;
+  s.ypart = u + 3 * nmax;
+  s.Vs = u;
+  s.Zs = u + GNB * nmax;
+  s.Xp = u + 2 * GNB * nmax;
   return s;
 }
 
-// Copy A (lda) into W (ldw).  With check, verifies A == -A^T exactly
-// (isskewhermitian, skewhermitian.jl:84-94).  Returns false if not skew.
-__device__ bool copy_in(const double* __restrict__ A, int64_t lda, double* W, int64_t ldw, int n, bool check) {
-  int bad = 0;
-  const int64_t total = (int64_t)n * n;
-  for (int64_t e = threadIdx.x; e < total; e += BT) {
-    const int j = (int)(e / n), i = (int)(e - (int64_t)j * n);
-    const double a = A[i + (int64_t)j * lda];
-    if (W != A) W[i + (int64_t)j * ldw] = a;
-    if (check) bad |= !(a == -A[j + (int64_t)i * lda]);
-  }
-  return __syncthreads_or(bad) == 0;
-}
-
-// Block-wide max of |x| (for the scaled-norm fallback).
+template <int NW>
 __device__ double block_maxabs(double x, double* red) {
   x = fabs(x);
 #pragma unroll
@@ -95,123 +111,236 @@ __device__ double block_maxabs(double x, double* red) {
   return s;
 }
 
-// p_i = tau * sum_{j in [c0, n)} W[i,j] v_j for rows i in [r0, n).  Each warp
-// takes one of NW column chunks; partial sums meet in shared memory.  Ends with
-// p visible to the whole block.
-__device__ void rowprod(const double* W, int64_t ldw, int n, int r0, int c0, const Vecs& s, double tau) {
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-  const int m = n - c0;
-  const int chunk = (m + NW - 1) / NW;
-  const int cb = c0 + w * chunk;
-  const int ce = min(n, cb + chunk);
-  double* yp = s.ypart + (size_t)w * s.nmax;
-  for (int i0 = r0; i0 < n; i0 += WARP) {
-    const int i = i0 + l;
+// Sum over the 32 lanes of 32 per-lane values at once (butterfly transpose):
+// on return lane L holds sum_lanes v[L].  31 adds instead of 32 x 5.
+__device__ __forceinline__ double warp_transpose_sum32(double (&v)[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool up = lane & s;
+#pragma unroll
+    for (int i = 0; i < s; i++) {
+      const double send = up ? v[i] : v[i + s];
+      const double keep = up ? v[i + s] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+    }
+  }
+  return v[0];
+}
+
+// ---------------------------------------------------------------------------
+// Copy-in with the exact skew check (isskewhermitian, skewhermitian.jl:84-94)
+// ---------------------------------------------------------------------------
+template <int NT, class MW>
+__device__ bool copy_in(const double* __restrict__ A, int64_t lda, const MW& W, bool inplace, int n, bool check) {
+  int bad = 0;
+  const int64_t total = (int64_t)n * n;
+  for (int64_t e = threadIdx.x; e < total; e += NT) {
+    const int j = (int)(e / n), i = (int)(e - (int64_t)j * n);
+    const double a = A[i + (int64_t)j * lda];
+    if (!inplace) W.at(i, j) = a;
+    if (check) bad |= !(a == -A[j + (int64_t)i * lda]);
+  }
+  return __syncthreads_or(bad) == 0;
+}
+
+// ---------------------------------------------------------------------------
+// Forward reduction
+// ---------------------------------------------------------------------------
+
+// Reflector for column c computed by the whole block (first column only).
+template <int NT, class MW>
+__device__ void reflector_block(const MW& W, int n, int c, const Smem& s, double* vout) {
+  constexpr int NW = NT / 32;
+  double part = 0.0;
+  for (int r = c + 2 + (int)threadIdx.x; r < n; r += NT) {
+    const double x = W.at(r, c);
+    part = fma(x, x, part);
+  }
+  const double ss = block_sum<NW>(part, s.red);
+  double xn = -1.0;
+  if (ss_needs_scaling(ss)) {  // block-uniform rare path: norm with scaling
+    double mx = 0.0;
+    for (int r = c + 2 + (int)threadIdx.x; r < n; r += NT) mx = fmax(mx, fabs(W.at(r, c)));
+    mx = block_maxabs<NW>(mx, s.red);
+    double q = 0.0;
+    if (mx > 0.0)
+      for (int r = c + 2 + (int)threadIdx.x; r < n; r += NT) {
+        const double x = W.at(r, c) / mx;
+        q = fma(x, x, q);
+      }
+    q = block_sum<NW>(q, s.red);
+    xn = mx * sqrt(q);
+  }
+  const Reflector R = make_reflector(W.at(c + 1, c), ss, xn);
+  if (threadIdx.x == 0) {
+    s.ev[c] = R.beta;
+    s.tau[c] = R.tau;
+  }
+  for (int r = c + 1 + (int)threadIdx.x; r < n; r += NT) {
+    const double vr = (R.tau == 0.0) ? 0.0 : (r == c + 1 ? 1.0 : W.at(r, c) * R.scale);
+    vout[r] = vr;
+    W.at(r, c) = vr;
+  }
+  __syncthreads();
+}
+
+// Warp 0 during step k: update column k+1 with (v_k, p_k), then build reflector
+// k+1 from it into vout, ev[k+1], tau[k+1] and column k+1 of W.
+template <class MW>
+__device__ void lookahead_warp(const MW& W, int n, int k, const double* v, const double* p, double tauk,
+                               const Smem& s, double* vout) {
+  const int lane = threadIdx.x & 31;
+  const int c = k + 1;
+  const double vc = v[c], pc = p[c];
+  double part = 0.0;
+  for (int r = c + 1 + lane; r < n; r += 32) {
+    double a = W.at(r, c);
+    if (tauk != 0.0) a = fma(v[r], pc, fma(neg(p[r]), vc, a));
+    W.at(r, c) = a;
+    if (r >= c + 2) part = fma(a, a, part);
+  }
+  __syncwarp();
+  const double ss = warp_sum(part);
+  double xn = -1.0;
+  if (ss_needs_scaling(ss)) {  // warp-uniform rare path
+    double mx = 0.0;
+    for (int r = c + 2 + lane; r < n; r += 32) mx = fmax(mx, fabs(W.at(r, c)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    double q = 0.0;
+    if (mx > 0.0)
+      for (int r = c + 2 + lane; r < n; r += 32) {
+        const double x = W.at(r, c) / mx;
+        q = fma(x, x, q);
+      }
+    xn = mx * sqrt(warp_sum(q));
+  }
+  const Reflector R = make_reflector(W.at(c + 1, c), ss, xn);
+  if (lane == 0) {
+    s.ev[c] = R.beta;
+    s.tau[c] = R.tau;
+  }
+  for (int r = c + 1 + lane; r < n; r += 32) {
+    const double vr = (R.tau == 0.0) ? 0.0 : (r == c + 1 ? 1.0 : W.at(r, c) * R.scale);
+    vout[r] = vr;
+    W.at(r, c) = vr;
+  }
+}
+
+// p_i = tau * sum_{j >= c0} W[i,j] v_j for i >= r0.  Lanes are rows; warps take
+// (row strip, column chunk) items so that every warp has work when the block is
+// small.  Ends with p visible to the whole block.
+template <int NT, class MW>
+__device__ void rowprod(const MW& W, int n, int r0, int c0, const double* v, double tau, const Smem& s) {
+  constexpr int NW = NT / 32;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int mr = n - r0, mc = n - c0;
+  const int S = (mr + 31) >> 5;
+  const int C = S >= NW ? 1 : NW / S;
+  const int chunk = (mc + C - 1) / C;
+  for (int item = w; item < S * C; item += NW) {
+    const int si = item / C, ci = item - si * C;
+    const int i = r0 + si * 32 + lane;
+    const int cb = c0 + ci * chunk, ce = min(n, cb + chunk);
     if (i < n) {
-      const double* row = W + i;
       double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
       int j = cb;
       for (; j + 3 < ce; j += 4) {
-        a0 = fma(row[(int64_t)j * ldw], s.v[j], a0);
-        a1 = fma(row[(int64_t)(j + 1) * ldw], s.v[j + 1], a1);
-        a2 = fma(row[(int64_t)(j + 2) * ldw], s.v[j + 2], a2);
-        a3 = fma(row[(int64_t)(j + 3) * ldw], s.v[j + 3], a3);
+        const double w0 = W.at(i, j), w1 = W.at(i, j + 1), w2 = W.at(i, j + 2), w3 = W.at(i, j + 3);
+        a0 = fma(w0, v[j], a0);
+        a1 = fma(w1, v[j + 1], a1);
+        a2 = fma(w2, v[j + 2], a2);
+        a3 = fma(w3, v[j + 3], a3);
       }
-      for (; j < ce; j++) a0 = fma(row[(int64_t)j * ldw], s.v[j], a0);
-      yp[i] = (a0 + a1) + (a2 + a3);
+      for (; j < ce; j++) a0 = fma(W.at(i, j), v[j], a0);
+      const double y = (a0 + a1) + (a2 + a3);
+      if (C == 1)
+        s.p[i] = tau * y;
+      else
+        s.ypart[ci * s.nmax + i] = y;
     }
   }
   __syncthreads();
-  for (int i = r0 + (int)threadIdx.x; i < n; i += BT) {
-    double y = s.ypart[i];
-#pragma unroll
-    for (int q = 1; q < NW; q++) y += s.ypart[(size_t)q * s.nmax + i];
-    s.p[i] = tau * y;
+  if (C > 1) {
+    for (int i = r0 + (int)threadIdx.x; i < n; i += NT) {
+      double y = s.ypart[i];
+      for (int c = 1; c < C; c++) y += s.ypart[c * s.nmax + i];
+      s.p[i] = tau * y;
+    }
+    __syncthreads();
   }
-  __syncthreads();
 }
 
-// Two-sided update W += v p^T - p v^T on the region {i in [o, n), j < i, j >= j0}
-// (lower triangle only, mirrored to the upper).  v_j = 0 for j < o, so the
-// rectangle j in [j0, o) needs one FMA per element and the triangle two.
-// Elements are dealt out column by column from the flattened region.
-__device__ void skew_update(double* W, int64_t ldw, int n, int o, int j0, const Vecs& s) {
-  // column j holds rows max(j+1, o) .. n-1
-  auto collen = [&](int j) { return n - max(j + 1, o); };
-  int j = j0, r = threadIdx.x;
-  while (j < n - 1 && r >= collen(j)) {
-    r -= collen(j);
+// Rank-2 skew update of the lower triangle {jstart <= j < i <= n-1}, mirrored.
+// Participating thread t of T; elements dealt from the flattened triangle,
+// four per iteration so four loads are in flight.
+template <class MW>
+__device__ void update_tri(const MW& W, int n, int jstart, const double* v, const double* p, int t, int T) {
+  int j = jstart, r = t;
+  while (j < n - 1 && r >= n - 1 - j) {
+    r -= n - 1 - j;
     j++;
   }
   while (j < n - 1) {
-    const int i = max(j + 1, o) + r;
-    double* pij = W + i + (int64_t)j * ldw;
-    double a = *pij;
-    const double vi = s.v[i];
-    const double pj = s.p[j];
-    if (j >= o) a = fma(neg(s.p[i]), s.v[j], a);
-    a = fma(vi, pj, a);
-    *pij = a;
-    W[j + (int64_t)i * ldw] = neg(a);
-    r += BT;
-    while (j < n - 1 && r >= collen(j)) {
-      r -= collen(j);
-      j++;
+    int jj[4], ii[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      jj[q] = j;
+      ii[q] = j + 1 + r;
+      if (j < n - 1) {
+        r += T;
+        while (j < n - 1 && r >= n - 1 - j) {
+          r -= n - 1 - j;
+          j++;
+        }
+      }
     }
+    double a[4];
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (jj[q] < n - 1) a[q] = W.at(ii[q], jj[q]);
+#pragma unroll
+    for (int q = 0; q < 4; q++)
+      if (jj[q] < n - 1) {
+        const int i = ii[q], jc = jj[q];
+        const double x = fma(v[i], p[jc], fma(neg(p[i]), v[jc], a[q]));
+        W.at(i, jc) = x;
+        W.at(jc, i) = neg(x);
+      }
   }
 }
 
-// Householder reduction of the n x n skew matrix in W to tridiagonal form.
-// Fills s.ev[0..n-2], s.tau[0..n-2]; W keeps the reflectors in its lower part.
-__device__ void reduce(double* W, int64_t ldw, int n, const Vecs& s) {
-  for (int k = 0; k + 2 < n; k++) {
-    // (1) sum of squares below the subdiagonal
-    double part = 0.0;
-    for (int r = k + 2 + (int)threadIdx.x; r < n; r += BT) {
-      const double x = W[r + (int64_t)k * ldw];
-      part = fma(x, x, part);
-    }
-    const double ss = block_sum<NW>(part, s.red);
-    const double alpha = W[(k + 1) + (int64_t)k * ldw];
-    double xn = -1.0;
-    if (ss_needs_scaling(ss)) {  // block-uniform rare path: norm with scaling
-      double mx = 0.0;
-      for (int r = k + 2 + (int)threadIdx.x; r < n; r += BT) mx = fmax(mx, fabs(W[r + (int64_t)k * ldw]));
-      mx = block_maxabs(mx, s.red);
-      double q = 0.0;
-      for (int r = k + 2 + (int)threadIdx.x; r < n; r += BT) {
-        const double x = W[r + (int64_t)k * ldw] / mx;
-        q = fma(x, x, q);
-      }
-      q = block_sum<NW>(q, s.red);
-      xn = mx * sqrt(q);
-    }
-    // (2) reflector, computed redundantly by every thread
-    const Reflector R = make_reflector(alpha, ss, xn);
+template <int NT, class MW>
+__device__ void forward(const MW& W, int n, const Smem& s) {
+  if (n <= 1) return;
+  if (n == 2) {
     if (threadIdx.x == 0) {
-      s.ev[k] = R.beta;
-      s.tau[k] = R.tau;
-    }
-    // (3) v into shared memory and back into column k
-    for (int r = k + 1 + (int)threadIdx.x; r < n; r += BT) {
-      double vr;
-      if (R.tau == 0.0)
-        vr = 0.0;  // zero column: x .= 0 (hessenberg.jl:40)
-      else
-        vr = (r == k + 1) ? 1.0 : W[r + (int64_t)k * ldw] * R.scale;
-      s.v[r] = vr;
-      W[r + (int64_t)k * ldw] = vr;
+      s.ev[0] = W.at(1, 0);  // final real 1x1 step: tau = 0, beta = x (hessenberg.jl:27-29)
+      s.tau[0] = 0.0;
     }
     __syncthreads();
-    if (R.tau == 0.0) continue;
-    // (4) p = tau * W22 v
-    rowprod(W, ldw, n, k + 1, k + 1, s, R.tau);
-    // (5) W22 += v p^T - p v^T
-    skew_update(W, ldw, n, k + 1, k + 1, s);
+    return;
+  }
+  reflector_block<NT>(W, n, 0, s, s.vb0);
+  for (int k = 0; k + 2 < n; k++) {
+    const double* v = (k & 1) ? s.vb1 : s.vb0;
+    double* vn = (k & 1) ? s.vb0 : s.vb1;
+    const double tauk = s.tau[k];
+    if (tauk != 0.0) rowprod<NT>(W, n, k + 1, k + 1, v, tauk, s);
+    const int w = threadIdx.x >> 5;
+    if (k + 1 <= n - 3) {
+      if (w == 0)
+        lookahead_warp(W, n, k, v, s.p, tauk, s, vn);
+      else if (tauk != 0.0)
+        update_tri(W, n, k + 2, v, s.p, (int)threadIdx.x - 32, NT - 32);
+    } else if (tauk != 0.0) {
+      update_tri(W, n, k + 1, v, s.p, (int)threadIdx.x, NT);
+    }
     __syncthreads();
   }
-  if (n >= 2 && threadIdx.x == 0) {  // final real 1x1 step: tau = 0, beta = x (hessenberg.jl:27-29)
-    s.ev[n - 2] = W[(n - 1) + (int64_t)(n - 2) * ldw];
+  if (threadIdx.x == 0) {
+    s.ev[n - 2] = W.at(n - 1, n - 2);
     s.tau[n - 2] = 0.0;
   }
   __syncthreads();
@@ -219,18 +348,19 @@ __device__ void reduce(double* W, int64_t ldw, int n, const Vecs& s) {
 
 // log|Pf| and sign from ev and tau (pfaffian.jl:167-179):
 //   log|Pf| = sum_{odd i} log|ev_i|, sign = prod sign(-ev_i) * (-1)^{#tau != 0}.
-__device__ void pfaffian_from_tridiag(int n, const Vecs& s, double* logpf, double* sign) {
+template <int NT>
+__device__ void pfaffian_from_tridiag(int n, const Smem& s, double* logpf, double* sign) {
+  constexpr int NW = NT / 32;
   const int h = n / 2;
   double lp = 0.0;
   int npos = 0, nzero = 0, ntau = 0;
-  for (int a = threadIdx.x; a < h; a += BT) {
+  for (int a = threadIdx.x; a < h; a += NT) {
     const double e = s.ev[2 * a];
     lp += log(fabs(e));
     npos += (e > 0.0);
     nzero += (e == 0.0);
   }
-  for (int a = threadIdx.x; a < n - 1; a += BT) ntau += (s.tau[a] != 0.0);
-  // parity of (#ev_odd > 0) + (#tau != 0), summed over threads on the integer pipe
+  for (int a = threadIdx.x; a < n - 1; a += NT) ntau += (s.tau[a] != 0.0);
   const int tflip = __syncthreads_count((npos + ntau) & 1);
   const int tzero = __syncthreads_count(nzero > 0);
   const double total = block_sum<NW>(lp, s.red);
@@ -240,60 +370,284 @@ __device__ void pfaffian_from_tridiag(int n, const Vecs& s, double* logpf, doubl
   }
 }
 
-// M = -1/2 T^{-1} (even n, all odd-position ev nonzero), full storage in G.
+// ---------------------------------------------------------------------------
+// Gradient
+// ---------------------------------------------------------------------------
+
+// M = -1/2 T^{-1} (even n, all odd-position ev nonzero), full storage.
 // With O = even 0-based indices and E = odd ones, T = [[0, B], [-B^T, 0]] where
-// B is lower bidiagonal (diag d_a = -ev[2a], sub s_a = ev[2a-1]), and
+// B is lower bidiagonal (diag d_a = -ev[2a], sub s_a = ev[2a-1]) and
 // T^{-1} = [[0, -B^{-T}], [B^{-1}, 0]]:  T^{-1}[2a+1, 2b] = (B^{-1})_{ab}
 //   = (1/d_b) prod_{c=b+1..a} (-s_c/d_c)   for a >= b, zero otherwise.
-__device__ void tinv_init(double* G, int64_t ldg, int n, const Vecs& s) {
+template <int NT>
+__device__ void tinv_init(const GMat& G, int n, const Smem& s) {
   const int64_t total = (int64_t)n * n;
-  for (int64_t e = threadIdx.x; e < total; e += BT) {
+  for (int64_t e = threadIdx.x; e < total; e += NT) {
     const int j = (int)(e / n), i = (int)(e - (int64_t)j * n);
-    G[i + (int64_t)j * ldg] = 0.0;
+    G.at(i, j) = 0.0;
   }
   const int h = n / 2;
-  // ratios -s_c/d_c = ev[2c-1]/ev[2c] into s.p[c], 1 <= c < h
-  for (int c = 1 + (int)threadIdx.x; c < h; c += BT) s.p[c] = s.ev[2 * c - 1] / s.ev[2 * c];
+  double* ratio = s.Vs;  // -s_c/d_c = ev[2c-1]/ev[2c], 1 <= c < h
+  for (int c = 1 + (int)threadIdx.x; c < h; c += NT) ratio[c] = s.ev[2 * c - 1] / s.ev[2 * c];
   __syncthreads();
-  for (int b = threadIdx.x; b < h; b += BT) {
-    double x = 0.5 / s.ev[2 * b];  // -1/2 * (1/d_b) = -1/2 * (-1/ev[2b])
+  for (int b = threadIdx.x; b < h; b += NT) {
+    double x = 0.5 / s.ev[2 * b];  // -1/2 * (1/d_b)
     for (int a = b; a < h; a++) {
-      G[(2 * a + 1) + (int64_t)(2 * b) * ldg] = x;
-      G[(2 * b) + (int64_t)(2 * a + 1) * ldg] = neg(x);
-      if (a + 1 < h) x *= s.p[a + 1];
+      G.at(2 * a + 1, 2 * b) = x;
+      G.at(2 * b, 2 * a + 1) = neg(x);
+      if (a + 1 < h) x *= ratio[a + 1];
     }
   }
   __syncthreads();
 }
 
-// G = Q M Q^T with M already in G, reflectors k = n-3..0 taken from W.
-__device__ void backapply(double* G, int64_t ldg, const double* W, int64_t ldw, int n, const Vecs& s) {
-  for (int k = n - 3; k >= 0; k--) {
-    const double tau = s.tau[k];
-    if (tau == 0.0) continue;
-    for (int r = k + 1 + (int)threadIdx.x; r < n; r += BT) s.v[r] = W[r + (int64_t)k * ldw];
+// Reduce per-thread partial values part[0..npair) (npair <= 32) over the block
+// into out[0..npair); scratch holds NW*32 doubles.
+template <int NT>
+__device__ void block_reduce_pairs(double (&part)[32], int npair, double* scratch, double* out) {
+  constexpr int NW = NT / 32;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double mine = warp_transpose_sum32(part);  // lane L holds the warp's sum for slot L
+  scratch[w * 32 + lane] = mine;
+  __syncthreads();
+  if ((int)threadIdx.x < npair) {
+    double acc = 0.0;
+#pragma unroll
+    for (int q = 0; q < NW; q++) acc += scratch[q * 32 + threadIdx.x];
+    out[threadIdx.x] = acc;
+  }
+  __syncthreads();
+}
+
+// Pair (l1 < l2) -> slot; for GNB = 8 there are 28 slots.
+__device__ __forceinline__ int pair_slot(int l1, int l2) { return l1 * GNB - (l1 * (l1 + 1)) / 2 + (l2 - l1 - 1); }
+
+// G <- Q G Q^T, G holding -1/2 T^{-1} on entry; reflectors from W's lower part.
+template <int NT, class MW>
+__device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
+  constexpr int NW = NT / 32;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int nref = n - 2;  // reflectors 0..n-3 (reflector n-2 is the trivial 1x1)
+  double* Vs = s.Vs;       // V block, row-major: Vs[(r - k0 - 1) * GNB + l]
+  double* Zs = s.Zs;       // X, then Z', row-major: Zs[i * GNB + l]
+  double* Xp = s.Xp;       // partial products / reduction scratch
+  for (int kend = nref; kend > 0; kend -= GNB) {
+    const int k0 = max(0, kend - GNB), nb = kend - k0;
+    const int r0 = k0 + 1, m = n - r0;
+    // 1. stage V (m x GNB; columns past nb are zero)
+    for (int idx = tid; idx < m * GNB; idx += NT) {
+      const int rr = idx / GNB, l = idx - rr * GNB;
+      const int r = r0 + rr, kk = k0 + l;
+      double val = 0.0;
+      if (l < nb) val = (r < kk + 1) ? 0.0 : (r == kk + 1 ? 1.0 : W.at(r, kk));
+      Vs[idx] = val;
+    }
     __syncthreads();
-    rowprod(G, ldg, n, 0, k + 1, s, tau);
-    skew_update(G, ldg, n, k + 1, 0, s);
+    // 2. Gram P = V^T V (pairs l1 < l2), then T_b (forward, columnwise)
+    {
+      double part[32];
+#pragma unroll
+      for (int q = 0; q < 32; q++) part[q] = 0.0;
+      for (int rr = tid; rr < m; rr += NT) {
+        double vr[GNB];
+#pragma unroll
+        for (int l = 0; l < GNB; l++) vr[l] = Vs[rr * GNB + l];
+#pragma unroll
+        for (int l1 = 0; l1 < GNB; l1++)
+#pragma unroll
+          for (int l2 = l1 + 1; l2 < GNB; l2++) part[pair_slot(l1, l2)] = fma(vr[l1], vr[l2], part[pair_slot(l1, l2)]);
+      }
+      block_reduce_pairs<NT>(part, 28, Xp, s.P);
+      if (w == 0) {  // T[l][l] = tau_l, T[0:l, l] = -tau_l T[0:l, 0:l] P[0:l, l]
+        for (int q = lane; q < GNB * GNB; q += 32) s.T[q] = 0.0;
+        __syncwarp();
+        for (int l = 0; l < nb; l++) {
+          const double tl = s.tau[k0 + l];
+          double acc = 0.0;
+          if (lane < l)
+            for (int j = lane; j < l; j++) acc = fma(s.T[lane * GNB + j], s.P[pair_slot(j, l)], acc);
+          __syncwarp();
+          if (lane < l) s.T[lane * GNB + l] = neg(tl * acc);
+          if (lane == l) s.T[l * GNB + l] = tl;
+          __syncwarp();
+        }
+      }
+      __syncthreads();
+    }
+    // 3. X = G[:, r0:n] V  (n x GNB), lanes = rows, (strip, chunk) items
+    {
+      const int S = (n + 31) >> 5;
+      const int C = S >= NW ? 1 : NW / S;
+      const int chunk = (m + C - 1) / C;
+      for (int item = w; item < S * C; item += NW) {
+        const int si = item / C, ci = item - si * C;
+        const int i = si * 32 + lane;
+        const int cb = r0 + ci * chunk, ce = min(n, cb + chunk);
+        double acc[GNB];
+#pragma unroll
+        for (int l = 0; l < GNB; l++) acc[l] = 0.0;
+        if (i < n) {
+          for (int j = cb; j < ce; j++) {
+            const double g = G.at(i, j);
+            const double* vj = Vs + (j - r0) * GNB;
+#pragma unroll
+            for (int l = 0; l < GNB; l++) acc[l] = fma(g, vj[l], acc[l]);
+          }
+          if (C == 1) {
+#pragma unroll
+            for (int l = 0; l < GNB; l++) Zs[i * GNB + l] = acc[l];
+          } else {
+#pragma unroll
+            for (int l = 0; l < GNB; l++) Xp[(item * 32 + lane) * GNB + l] = acc[l];
+          }
+        }
+      }
+      __syncthreads();
+      if (C > 1) {
+        for (int idx = tid; idx < n * GNB; idx += NT) {
+          const int i = idx / GNB, l = idx - i * GNB;
+          const int si = i >> 5, ln = i & 31;
+          double x = 0.0;
+          for (int c = 0; c < C; c++) x += Xp[((si * C + c) * 32 + ln) * GNB + l];
+          Zs[idx] = x;
+        }
+        __syncthreads();
+      }
+    }
+    // 4. K = V^T X over the rows of V (skew: pairs l1 < l2); Ch = -1/2 T K T^T
+    {
+      double part[32];
+#pragma unroll
+      for (int q = 0; q < 32; q++) part[q] = 0.0;
+      for (int rr = tid; rr < m; rr += NT) {
+        double vr[GNB], xr[GNB];
+#pragma unroll
+        for (int l = 0; l < GNB; l++) {
+          vr[l] = Vs[rr * GNB + l];
+          xr[l] = Zs[(r0 + rr) * GNB + l];
+        }
+#pragma unroll
+        for (int l1 = 0; l1 < GNB; l1++)
+#pragma unroll
+          for (int l2 = l1 + 1; l2 < GNB; l2++) part[pair_slot(l1, l2)] = fma(vr[l1], xr[l2], part[pair_slot(l1, l2)]);
+      }
+      block_reduce_pairs<NT>(part, 28, Xp, s.K);
+      if (w == 0) {
+        double* Kf = s.C;  // full skew K
+        for (int q = lane; q < GNB * GNB; q += 32) {
+          const int l1 = q / GNB, l2 = q - l1 * GNB;
+          Kf[q] = (l1 < l2) ? s.K[pair_slot(l1, l2)] : (l1 > l2 ? neg(s.K[pair_slot(l2, l1)]) : 0.0);
+        }
+        __syncwarp();
+        for (int q = lane; q < GNB * GNB; q += 32) {  // TK = T Kf (into P, free now)
+          const int a = q / GNB, b = q - a * GNB;
+          double acc = 0.0;
+          for (int c = a; c < GNB; c++) acc = fma(s.T[a * GNB + c], Kf[c * GNB + b], acc);
+          s.P[q] = acc;
+        }
+        __syncwarp();
+        for (int q = lane; q < GNB * GNB; q += 32) {  // Ch = -1/2 (T K) T^T (into K)
+          const int a = q / GNB, b = q - a * GNB;
+          double acc = 0.0;
+          for (int c = b; c < GNB; c++) acc = fma(s.P[a * GNB + c], s.T[b * GNB + c], acc);
+          s.K[q] = -0.5 * acc;
+        }
+      }
+      __syncthreads();
+    }
+    // 5. Z' = X T^T + V Ch  (only rows of V get the V Ch term)
+    for (int i = tid; i < n; i += NT) {
+      double x[GNB], z[GNB];
+#pragma unroll
+      for (int l = 0; l < GNB; l++) x[l] = Zs[i * GNB + l];
+#pragma unroll
+      for (int l = 0; l < GNB; l++) {
+        double acc = 0.0;
+#pragma unroll
+        for (int c = l; c < GNB; c++) acc = fma(x[c], s.T[l * GNB + c], acc);
+        z[l] = acc;
+      }
+      if (i >= r0) {
+        double vr[GNB];
+#pragma unroll
+        for (int l = 0; l < GNB; l++) vr[l] = Vs[(i - r0) * GNB + l];
+#pragma unroll
+        for (int l = 0; l < GNB; l++) {
+          double acc = z[l];
+#pragma unroll
+          for (int c = 0; c < GNB; c++) acc = fma(vr[c], s.K[c * GNB + l], acc);
+          z[l] = acc;
+        }
+      }
+#pragma unroll
+      for (int l = 0; l < GNB; l++) Zs[i * GNB + l] = z[l];
+    }
     __syncthreads();
+    // 6. G[i,j] += V_i . Z'_j - Z'_i . V_j for i >= r0, j < i; mirrored.
+    //    Items: (row strip of 32, column block of 32) on or below the diagonal.
+    {
+      const int S = (m + 31) >> 5;
+      int total = 0;
+      for (int si = 0; si < S; si++) total += (min(n, r0 + 32 * (si + 1)) - 1 + 31) / 32;
+      for (int item = w; item < total; item += NW) {
+        int si = 0, rem = item;
+        for (;;) {
+          const int nbk = (min(n, r0 + 32 * (si + 1)) - 1 + 31) / 32;
+          if (rem < nbk) break;
+          rem -= nbk;
+          si++;
+        }
+        const int i = r0 + 32 * si + lane;
+        const int jb = rem * 32;
+        const int je = min(jb + 32, min(n, r0 + 32 * (si + 1)) - 1);
+        if (i < n) {
+          double vi[GNB], zi[GNB];
+#pragma unroll
+          for (int l = 0; l < GNB; l++) {
+            vi[l] = Vs[(i - r0) * GNB + l];
+            zi[l] = Zs[i * GNB + l];
+          }
+          for (int j = jb; j < je && j < i; j++) {
+            const double* zj = Zs + j * GNB;
+            double a0 = G.at(i, j), a1 = 0.0;
+#pragma unroll
+            for (int l = 0; l < GNB; l += 2) {
+              a0 = fma(vi[l], zj[l], a0);
+              a1 = fma(vi[l + 1], zj[l + 1], a1);
+            }
+            if (j >= r0) {
+              const double* vj = Vs + (j - r0) * GNB;
+#pragma unroll
+              for (int l = 0; l < GNB; l += 2) {
+                a0 = fma(neg(zi[l]), vj[l], a0);
+                a1 = fma(neg(zi[l + 1]), vj[l + 1], a1);
+              }
+            }
+            const double a = a0 + a1;
+            G.at(i, j) = a;
+            G.at(j, i) = neg(a);
+          }
+        }
+      }
+      __syncthreads();
+    }
   }
 }
 
-__device__ void fill(double* G, int64_t ldg, int n, double val) {
+template <int NT>
+__device__ void fill(const GMat& G, int n, double val) {
   const int64_t total = (int64_t)n * n;
-  for (int64_t e = threadIdx.x; e < total; e += BT) {
+  for (int64_t e = threadIdx.x; e < total; e += NT) {
     const int j = (int)(e / n), i = (int)(e - (int64_t)j * n);
-    G[i + (int64_t)j * ldg] = val;
+    G.at(i, j) = val;
   }
 }
 
-// One matrix, start to finish.  W may alias A (in-place single-matrix path).
+// One matrix, start to finish.
 struct Job {
   const double* A;
   int64_t lda;
   int n;
-  double* W;
-  int64_t ldw;
   double* G;  // gradient output or null
   int64_t ldg;
   double* logpf;
@@ -305,16 +659,18 @@ struct Job {
   bool want_pf;
 };
 
-__device__ void run_job(const Job& J, const Vecs& s) {
+template <int NT, class MW>
+__device__ void run_job(const Job& J, const MW& W, bool inplace, const Smem& s) {
   const int n = J.n;
-  const bool ok = copy_in(J.A, J.lda, J.W, J.ldw, n, J.check);
+  const bool ok = copy_in<NT>(J.A, J.lda, W, inplace, n, J.check);
+  const GMat G{J.G, J.ldg};
   if (!ok) {
     if (threadIdx.x == 0) {
       if (J.logpf) *J.logpf = nan("");
       if (J.sign) *J.sign = nan("");
       if (J.status) *J.status = SKEW_NOT_SKEW;
     }
-    if (J.G) fill(J.G, J.ldg, n, nan(""));
+    if (J.G) fill<NT>(G, n, nan(""));
     __syncthreads();
     return;
   }
@@ -325,13 +681,13 @@ __device__ void run_job(const Job& J, const Vecs& s) {
       *J.sign = 0.0;
       if (J.status) *J.status = SKEW_SINGULAR;
     }
-    if (J.G) fill(J.G, J.ldg, n, nan(""));
+    if (J.G) fill<NT>(G, n, nan(""));
     __syncthreads();
     if (!J.ev_out) return;
   }
-  reduce(J.W, J.ldw, n, s);
+  forward<NT>(W, n, s);
   if (J.ev_out || J.tau_out)
-    for (int a = threadIdx.x; a < n - 1; a += BT) {
+    for (int a = threadIdx.x; a < n - 1; a += NT) {
       if (J.ev_out) J.ev_out[a] = s.ev[a];
       if (J.tau_out) J.tau_out[a] = s.tau[a];
     }
@@ -341,7 +697,7 @@ __device__ void run_job(const Job& J, const Vecs& s) {
     return;
   }
   __shared__ double s_lp, s_sg;
-  pfaffian_from_tridiag(n, s, &s_lp, &s_sg);
+  pfaffian_from_tridiag<NT>(n, s, &s_lp, &s_sg);
   __syncthreads();
   const double lp = s_lp, sg = s_sg;
   if (threadIdx.x == 0) {
@@ -351,10 +707,10 @@ __device__ void run_job(const Job& J, const Vecs& s) {
   }
   if (J.G) {
     if (sg == 0.0) {
-      fill(J.G, J.ldg, n, nan(""));
+      fill<NT>(G, n, nan(""));
     } else {
-      tinv_init(J.G, J.ldg, n, s);
-      backapply(J.G, J.ldg, J.W, J.ldw, n, s);
+      tinv_init<NT>(G, n, s);
+      gradient<NT>(W, G, n, s);
     }
   }
   __syncthreads();
@@ -366,10 +722,10 @@ __device__ void run_job(const Job& J, const Vecs& s) {
 
 // Persistent batched kernel over order[begin:end) (matrices sorted largest
 // first); CTAs take the next matrix from an atomic counter.
-__global__ void __launch_bounds__(BT) batch_pf_kernel(BatchParams P) {
-  extern __shared__ __align__(16) double dsm[];
-  const Vecs s = carve(dsm, P.nmax);
-  double* smat = dsm + vec_doubles(P.nmax);
+template <int NT, bool SM>
+__global__ void __launch_bounds__(NT) batch_kernel(BatchParams P, int tridiag_only) {
+  const Smem s = carve(P.nmax);
+  const int woff = smem_doubles(P.nmax, NT / 32);
   __shared__ int s_next;
   for (;;) {
     if (threadIdx.x == 0) s_next = (int)atomicAdd(P.counter, 1u) + P.begin;
@@ -383,64 +739,33 @@ __global__ void __launch_bounds__(BT) batch_pf_kernel(BatchParams P) {
     J.A = P.A[b];
     J.lda = n;
     J.n = n;
-    J.ldw = n | 1;
-    J.W = P.smem_matrix ? smat : P.gws + (size_t)blockIdx.x * P.gws_slot;
-    J.G = P.grad ? P.grad[b] : nullptr;
+    J.G = tridiag_only ? nullptr : (P.grad ? P.grad[b] : nullptr);
     J.ldg = n;
-    J.logpf = P.logpf + b;
-    J.sign = P.sign + b;
+    J.logpf = tridiag_only ? nullptr : P.logpf + b;
+    J.sign = tridiag_only ? nullptr : P.sign + b;
     J.ev_out = P.ev_out ? P.ev_out + P.ev_off[b] : nullptr;
     J.tau_out = nullptr;
-    J.status = P.status + b;
+    J.status = tridiag_only ? nullptr : P.status + b;
     J.check = P.check != 0;
-    J.want_pf = true;
-    run_job(J, s);
-  }
-}
-
-// Batched reduction to tridiagonal form only (eigvals front end): ev_out[b].
-__global__ void __launch_bounds__(BT) batch_tridiag_kernel(BatchParams P) {
-  extern __shared__ __align__(16) double dsm[];
-  const Vecs s = carve(dsm, P.nmax);
-  double* smat = dsm + vec_doubles(P.nmax);
-  __shared__ int s_next;
-  for (;;) {
-    if (threadIdx.x == 0) s_next = (int)atomicAdd(P.counter, 1u) + P.begin;
-    __syncthreads();
-    const int t = s_next;
-    __syncthreads();
-    if (t >= P.end) break;
-    const int b = P.order[t];
-    const int n = P.n[b];
-    Job J;
-    J.A = P.A[b];
-    J.lda = n;
-    J.n = n;
-    J.ldw = n | 1;
-    J.W = P.smem_matrix ? smat : P.gws + (size_t)blockIdx.x * P.gws_slot;
-    J.G = nullptr;
-    J.ldg = n;
-    J.logpf = nullptr;
-    J.sign = nullptr;
-    J.ev_out = P.ev_out + P.ev_off[b];
-    J.tau_out = nullptr;
-    J.status = nullptr;
-    J.check = P.check != 0;
-    J.want_pf = false;
-    run_job(J, s);
+    J.want_pf = !tridiag_only;
+    if constexpr (SM) {
+      const SMat W{woff, n | 1};
+      run_job<NT>(J, W, false, s);
+    } else {
+      const GMat W{P.gws + (size_t)blockIdx.x * P.gws_slot, (int64_t)(n | 1)};
+      run_job<NT>(J, W, false, s);
+    }
   }
 }
 
 // Single matrix, in place (W = A), one CTA.
-__global__ void __launch_bounds__(BT) single_kernel(SingleParams P) {
-  extern __shared__ __align__(16) double dsm[];
-  const Vecs s = carve(dsm, P.n > 0 ? P.n : 1);
+template <int NT>
+__global__ void __launch_bounds__(NT) single_kernel(SingleParams P) {
+  const Smem s = carve(P.n > 0 ? P.n : 1);
   Job J;
   J.A = P.A;
   J.lda = P.lda;
   J.n = P.n;
-  J.W = P.A;
-  J.ldw = P.lda;
   J.G = P.G;
   J.ldg = P.ldg;
   J.logpf = P.logpf;
@@ -450,51 +775,72 @@ __global__ void __launch_bounds__(BT) single_kernel(SingleParams P) {
   J.status = P.info;
   J.check = P.check != 0;
   J.want_pf = P.want_pf != 0;
-  run_job(J, s);
+  const GMat W{P.A, P.lda};
+  run_job<NT>(J, W, true, s);
 }
 
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
+constexpr int NT_SMALL = 128;  // shared-memory buckets up to n = 96
+constexpr int NT_LARGE = 256;
+
+static int threads_for(int nmax, bool smem_matrix) { return (smem_matrix && nmax <= 96) ? NT_SMALL : NT_LARGE; }
+
 size_t batch_smem_bytes(int nmax, bool smem_matrix) {
-  size_t b = sizeof(double) * (size_t)vec_doubles(nmax);
+  const int nt = threads_for(nmax, smem_matrix);
+  size_t b = sizeof(double) * (size_t)smem_doubles(nmax, nt / 32);
   if (smem_matrix) b += sizeof(double) * (size_t)nmax * (size_t)(nmax | 1);
   return b;
 }
 
-cudaError_t launch_batch_pf(const BatchParams& P, int grid, cudaStream_t st, bool tridiag_only) {
-  const size_t smem = batch_smem_bytes(P.nmax, P.smem_matrix != 0);
-  cudaError_t e;
-  if (tridiag_only) {
-    e = cudaFuncSetAttribute(batch_tridiag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    batch_tridiag_kernel<<<grid, BT, smem, st>>>(P);
-  } else {
-    e = cudaFuncSetAttribute(batch_pf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    if (e != cudaSuccess) return e;
-    batch_pf_kernel<<<grid, BT, smem, st>>>(P);
-  }
+template <int NT, bool SM>
+static cudaError_t launch_t(const BatchParams& P, int grid, size_t smem, cudaStream_t st, int tridiag_only) {
+  cudaError_t e = cudaFuncSetAttribute(batch_kernel<NT, SM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  batch_kernel<NT, SM><<<grid, NT, smem, st>>>(P, tridiag_only);
   return cudaGetLastError();
+}
+
+cudaError_t launch_batch_pf(const BatchParams& P, int grid, cudaStream_t st, bool tridiag_only) {
+  const bool sm = P.smem_matrix != 0;
+  const size_t smem = batch_smem_bytes(P.nmax, sm);
+  const int nt = threads_for(P.nmax, sm);
+  if (sm && nt == NT_SMALL) return launch_t<NT_SMALL, true>(P, grid, smem, st, tridiag_only);
+  if (sm) return launch_t<NT_LARGE, true>(P, grid, smem, st, tridiag_only);
+  return launch_t<NT_LARGE, false>(P, grid, smem, st, tridiag_only);
 }
 
 cudaError_t launch_single(const SingleParams& P, cudaStream_t st) {
-  const size_t smem = batch_smem_bytes(P.n > 0 ? P.n : 1, false);
-  cudaError_t e = cudaFuncSetAttribute(single_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const int nmax = P.n > 0 ? P.n : 1;
+  const size_t smem = sizeof(double) * (size_t)smem_doubles(nmax, NT_LARGE / 32);
+  cudaError_t e =
+      cudaFuncSetAttribute(single_kernel<NT_LARGE>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
-  single_kernel<<<1, BT, smem, st>>>(P);
+  single_kernel<NT_LARGE><<<1, NT_LARGE, smem, st>>>(P);
   return cudaGetLastError();
 }
 
-int batch_threads() { return BT; }
+int batch_threads() { return NT_LARGE; }
 
-int batch_occupancy(size_t smem) {
+template <int NT, bool SM>
+static int occ_t(size_t smem) {
   int occ = 0;
-  if (cudaFuncSetAttribute(batch_pf_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess ||
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_pf_kernel, BT, smem) != cudaSuccess || occ < 1) {
+  cudaError_t e = cudaFuncSetAttribute(batch_kernel<NT, SM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<NT, SM>, NT, smem);
+  if (e != cudaSuccess || occ < 1) {
     cudaGetLastError();
     return 1;
   }
   return occ;
+}
+
+int batch_occupancy(int nmax, bool smem_matrix) {
+  const size_t smem = batch_smem_bytes(nmax, smem_matrix);
+  const int nt = threads_for(nmax, smem_matrix);
+  if (smem_matrix && nt == NT_SMALL) return occ_t<NT_SMALL, true>(smem);
+  if (smem_matrix) return occ_t<NT_LARGE, true>(smem);
+  return occ_t<NT_LARGE, false>(smem);
 }
 
 }  // namespace skew

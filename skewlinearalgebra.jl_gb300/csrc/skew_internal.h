@@ -44,7 +44,7 @@ size_t batch_smem_bytes(int nmax, bool smem_matrix);
 cudaError_t launch_batch_pf(const BatchParams& P, int grid, cudaStream_t st, bool tridiag_only);
 cudaError_t launch_single(const SingleParams& P, cudaStream_t st);
 int batch_threads();
-int batch_occupancy(size_t smem_bytes);  // resident CTAs per SM
+int batch_occupancy(int nmax, bool smem_matrix);  // resident CTAs per SM
 
 // Skew tridiagonal eigenvalues (skew_qr.cu).
 struct TrieigParams {
