@@ -79,6 +79,18 @@ SKEW_API int skew_logabspf_grad_d(skew_handle_t h, double* A, int64_t n, int64_t
  * in the reference's order (eigenvalue k is i*vals_im[k]).  A is destroyed. */
 SKEW_API int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info);
 
+/* eigvals without any device allocation.  No counterpart in the reference.
+ * For callers that cannot call cudaMalloc (a host that owns all device memory
+ * through its own pool, or a path where an allocation's synchronisation or
+ * failure is not acceptable): same result as skew_eigvals_d, but its scratch
+ * (n+1 doubles) is a fixed array inside the library instead of the handle's
+ * workspace, and the stream is passed directly (no handle).  n <= 1024, else
+ * SKEW_UNSUPPORTED.  The first call on each device looks up the array's device
+ * address, so make it before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller. */
+SKEW_API int skew_eigvals_noalloc_d(double* A, int64_t n, int64_t lda, double* vals_im, int* info,
+                                    skew_stream_t stream);
+
 /* LA.eigen!(A::SkewHermitian{Float64})  eigen.jl:338-360 (skeweigen! + skewtrieigen_divided!).
  * vals_im[n]; eigenvectors V = Vr + i*Vi (n x n each, leading dimension ldv).  A is destroyed. */
 SKEW_API int skew_eigen_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,

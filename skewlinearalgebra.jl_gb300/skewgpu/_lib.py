@@ -36,6 +36,7 @@ SIGNATURES = {
     "skew_logabspf_d": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _int, _vp]),
     "skew_logabspf_grad_d": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _i64, _vp]),
     "skew_eigvals_d": (_int, [_vp, _vp, _i64, _i64, _vp, _vp]),
+    "skew_eigvals_noalloc_d": (_int, [_vp, _i64, _i64, _vp, _vp, _vp]),
     "skew_eigen_d": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _i64, _vp]),
     "skew_exp_d": (_int, [_vp, _vp, _i64, _i64, _vp, _i64, _vp]),
     "skew_cis_d": (_int, [_vp, _vp, _i64, _i64, _vp, _i64, _vp]),
