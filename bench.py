@@ -169,9 +169,20 @@ def main():
     ap.add_argument("--count", type=int, default=COUNT, help="matrices per step (profiling cases)")
     ap.add_argument("--nmin", type=int, default=NMIN)
     ap.add_argument("--nmax", type=int, default=NMAX)
+    ap.add_argument("--large-n", type=int, default=8192, help="single-matrix hessenberg leg (0 = skip)")
+    ap.add_argument("--only-large", action="store_true", help="run only the single-matrix hessenberg leg")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_large:
+        import torch
+
+        import skewgpu
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"hessenberg": bench_hessenberg_large(args.large_n, max(1, args.steps),
+                                                               skewgpu.measure_fp64_peak())}), flush=True)
+        return 0
 
     import torch
 
@@ -341,6 +352,10 @@ def main():
         check = {"max_rel_logpf_vs_cpu": float(rel.max()), "sign_mismatches": int((gsg != csg).sum()),
                  "max_rel_grad_vs_cpu": gerr, "matrices": k, "status_nonzero": int((st != 0).sum())}
 
+    large = None
+    if rank == 0 and args.large_n > 0:
+        large = bench_hessenberg_large(args.large_n, 2, fp64_peak)
+
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -366,11 +381,56 @@ def main():
             line["check"] = check
         if plain:
             line["plain_gpu"] = plain
+        if large:
+            line[f"hessenberg_n{args.large_n}"] = large
         print(json.dumps(line), flush=True)
     plan.close()
     if dist is not None:
         dist.destroy_process_group()
     return 0
+
+
+def bench_hessenberg_large(n, reps, fp64_peak):
+    """Single dense skew matrix: blocked Householder tridiagonalisation on the
+    whole GPU (skew_hessenberg_d), timed with CUDA events per call; the input is
+    restored from a pristine device copy outside the timed region."""
+    import ctypes
+
+    import torch
+
+    import skewgpu
+
+    rng = np.random.default_rng(SEED + 8192)
+    B = rng.standard_normal((n, n))
+    A = (B - B.T) / 2
+    del B
+    pristine = skewgpu.to_device(A)
+    work = torch.empty_like(pristine)
+    tau = torch.empty(n - 1, dtype=torch.float64, device="cuda")
+    ev = torch.empty(n - 1, dtype=torch.float64, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    L = skewgpu._lib.load()
+    h = skewgpu.handle().bind()
+    stream = torch.cuda.current_stream()
+    times = []
+    for r in range(reps + 1):
+        work.copy_(pristine)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = L.skew_hessenberg_d(h, ctypes.c_void_p(work.data_ptr()), n, n, ctypes.c_void_p(tau.data_ptr()),
+                                 ctypes.c_void_p(ev.data_ptr()), ctypes.c_void_p(info.data_ptr()))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        assert st == 0, st
+        if r > 0:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    sec = float(np.median(times))
+    flops = 4.0 / 3.0 * n ** 3
+    e = ev.cpu().numpy()
+    fro_rel = abs(np.sqrt(2.0 * np.sum(e * e)) - np.linalg.norm(A)) / np.linalg.norm(A)
+    return {"n": n, "ms": sec * 1e3, "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
+            "algorithmic_flops": flops, "reps": reps, "check_frobenius_rel": float(fro_rel)}
 
 
 def _bucket_ids(sizes):

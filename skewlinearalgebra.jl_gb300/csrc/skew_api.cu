@@ -116,8 +116,14 @@ int skew_set_stream(skew_handle_t h, skew_stream_t s) {
   return SKEW_OK;
 }
 
-// Largest n handled by the one-CTA single-matrix kernel.
+// Largest n handled by the one-CTA single-matrix kernel, and the size above
+// which single-matrix calls use the multi-CTA blocked reduction instead
+// (override with SKEW_BLOCKED_MIN_N).
 static const int64_t kSingleMax = 1024;
+static int64_t blocked_min_n() {
+  const char* v = getenv("SKEW_BLOCKED_MIN_N");
+  return (v && *v) ? atoll(v) : 192;
+}
 
 static int single(skew_handle_t h, double* A, int64_t n, int64_t lda, double* G, int64_t ldg, double* logpf,
                   double* sign, double* ev, double* tau, int* info, int check, int want_pf) {
@@ -140,8 +146,27 @@ static int single(skew_handle_t h, double* A, int64_t n, int64_t lda, double* G,
   return SKEW_OK;
 }
 
+// Blocked reduction of a large matrix into tau/ev (device); A in place.
+static int blocked(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev, int* info,
+                   size_t extra_doubles, double** extra) {
+  if (!h || !A || lda < n || n > (1LL << 15)) return n > (1LL << 15) ? SKEW_UNSUPPORTED : SKEW_BAD_ARG;
+  const size_t wsd = blocked_ws_doubles((int)n);
+  int st = ensure_ws(h, sizeof(double) * (wsd + extra_doubles));
+  if (st) return st;
+  double* ws = (double*)h->ws;
+  if (extra) *extra = ws + wsd;
+  if (!tau || !ev) {  // caller wants only the tridiagonal: use the extra area
+    if (!extra || extra_doubles < 2 * (size_t)n) return SKEW_BAD_ARG;
+    ev = ws + wsd;
+    tau = ws + wsd + n;
+  }
+  CK(blocked_hessenberg(A, lda, (int)n, tau, ev, info, ws, h->sms, h->stream));
+  return SKEW_OK;
+}
+
 int skew_hessenberg_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev, int* info) {
   if (n > 1 && (!tau || !ev)) return SKEW_BAD_ARG;
+  if (n >= blocked_min_n()) return blocked(h, A, n, lda, tau, ev, info, 0, nullptr);
   return single(h, A, n, lda, nullptr, 0, nullptr, nullptr, n > 1 ? ev : nullptr, n > 1 ? tau : nullptr, info, 0,
                 0);
 }
@@ -149,6 +174,18 @@ int skew_hessenberg_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double
 int skew_logabspf_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* sign, int check,
                     int* info) {
   if (!logpf || !sign) return SKEW_BAD_ARG;
+  if (n >= blocked_min_n() && (n % 2) == 0) {
+    double* extra = nullptr;
+    // workspace layout: [blocked ws][ev (n)][tau (n)][not-skew flag]; size it before the check
+    int st = ensure_ws(h, sizeof(double) * (blocked_ws_doubles((int)n) + 2 * (size_t)n + 1));
+    if (st) return st;
+    double* flag = (double*)h->ws + blocked_ws_doubles((int)n) + 2 * (size_t)n;
+    if (check) CK(launch_check_skew(A, lda, (int)n, flag, h->sms, h->stream));
+    st = blocked(h, A, n, lda, nullptr, nullptr, info, 2 * (size_t)n + 1, &extra);
+    if (st) return st;
+    CK(launch_pf_from_tridiag(extra, extra + n, (int)n, logpf, sign, info, check ? flag : nullptr, h->stream));
+    return SKEW_OK;
+  }
   return single(h, A, n, lda, nullptr, 0, logpf, sign, nullptr, nullptr, info, check, 1);
 }
 
@@ -164,6 +201,13 @@ int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* v
   if (n == 1) {  // skeweigvals! n == 1 returns [A[1,1]] (eigen.jl:314)
     CK(cudaMemcpyAsync(vals_im, A, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+    return SKEW_OK;
+  }
+  if (n >= blocked_min_n()) {
+    double* extra = nullptr;
+    int st = blocked(h, A, n, lda, nullptr, nullptr, info, 2 * (size_t)n + 2, &extra);
+    if (st) return st;
+    CK(launch_tridiag_bisect(extra, (int)n, vals_im, extra + 2 * n, h->stream));
     return SKEW_OK;
   }
   int st = ensure_ws(h, sizeof(double) * (size_t)(n + 2));

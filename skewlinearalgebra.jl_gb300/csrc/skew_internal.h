@@ -63,6 +63,14 @@ cudaError_t launch_batch_trieig(const TrieigParams& P, cudaStream_t st);
 // symmetric tridiagonal; vals_im sorted descending.
 cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, double* scratch2, cudaStream_t st);
 
+// Multi-CTA blocked reduction of one large matrix (skew_blocked.cu).
+size_t blocked_ws_doubles(int n);
+cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, double* ev, int* info, double* ws, int sms,
+                               cudaStream_t st);
+cudaError_t launch_pf_from_tridiag(const double* ev, const double* tau, int n, double* logpf, double* sign, int* info,
+                                   const double* notskew, cudaStream_t st);
+cudaError_t launch_check_skew(const double* A, int64_t lda, int n, double* flag, int sms, cudaStream_t st);
+
 // FP64 DFMA microbenchmark kernel (skew_api.cu).
 cudaError_t launch_dfma_probe(double* out, int blocks, int iters, cudaStream_t st);
 

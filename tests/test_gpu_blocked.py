@@ -1,0 +1,83 @@
+"""GPU parity of the multi-CTA blocked reduction used for single large matrices.
+
+Moderate sizes are checked against the oracle (binary128 for n <= 384, the FP64
+restatement above).  Large sizes use size-independent properties: orthogonal
+similarity keeps the Frobenius norm (|T|_F = |A|_F), and log|Pf(A)| equals
+1/2 log|det A| (LU on the host).  Tolerances as in test_gpu_parity.py.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-11
+
+
+def skew_random(n, seed):
+    rng = np.random.default_rng(seed)
+    B = rng.standard_normal((n, n))
+    return (B - B.T) / 2
+
+
+def tridiag_dense(ev):
+    n = len(ev) + 1
+    T = np.zeros((n, n))
+    T[np.arange(1, n), np.arange(n - 1)] = ev
+    T[np.arange(n - 1), np.arange(1, n)] = -np.asarray(ev)
+    return T
+
+
+@pytest.mark.parametrize("n", [192, 193, 200, 255, 256, 300, 384])
+def test_blocked_hessenberg_vs_quad(skewgpu, oracle, n):
+    A = skew_random(n, 700 + n)
+    H = skewgpu.hessenberg(A)
+    ev = H.ev.cpu().numpy()
+    tau = H.tau.cpu().numpy()
+    _, tq, evq = oracle.hessenberg(A, quad=True)
+    scale = np.abs(evq).max()
+    np.testing.assert_allclose(ev, evq, atol=1e-12 * scale)  # same reflector convention, entrywise
+    assert np.array_equal(tau != 0, tq != 0)
+    Q = oracle.formq(skewgpu.from_device(H.factors), tau)
+    np.testing.assert_allclose(Q @ tridiag_dense(ev) @ Q.T, A, atol=1e-12 * np.abs(A).max() * np.sqrt(n))
+    np.testing.assert_allclose(Q.T @ Q, np.eye(n), atol=1e-13 * np.sqrt(n))
+
+
+@pytest.mark.parametrize("n", [192, 256, 512, 1000, 1024])
+def test_blocked_logabspf(skewgpu, oracle, n):
+    A = skew_random(n, 800 + n) / np.sqrt(n)
+    ref = oracle.logabspfaffian(A, quad=(n <= 384))
+    lp, sg = skewgpu.logabspfaffian_(skewgpu.SkewHermitian(A))
+    assert sg == ref[1]
+    assert abs(lp - ref[0]) <= RTOL * max(1.0, abs(ref[0]))
+
+
+@pytest.mark.parametrize("n", [200, 512, 1024])
+def test_blocked_eigvals(skewgpu, oracle, n):
+    A = skew_random(n, 900 + n)
+    vd, _ = oracle.eigvals(A, quad=(n <= 256))
+    vals = skewgpu.eigvals(A).imag
+    np.testing.assert_allclose(np.sort(vals), np.sort(vd), atol=RTOL * np.abs(vd).max())
+
+
+def test_blocked_large_properties(skewgpu):
+    n = 4096
+    A = skew_random(n, 4096) / np.sqrt(n)
+    H = skewgpu.hessenberg(A)
+    ev = H.ev.cpu().numpy()
+    fro_T = np.sqrt(2.0 * np.sum(ev.astype(np.float64) ** 2))
+    fro_A = np.linalg.norm(A)
+    assert abs(fro_T - fro_A) <= 1e-13 * fro_A * np.sqrt(n)
+    lp, sg = skewgpu.logabspfaffian_(skewgpu.SkewHermitian(A))
+    s, ld = np.linalg.slogdet(A)
+    assert s > 0
+    assert abs(lp - 0.5 * ld) <= 1e-11 * abs(ld) + 1e-9
+
+
+def test_blocked_determinism(skewgpu):
+    A = skew_random(640, 3)
+    r1 = skewgpu.logabspfaffian(A)
+    r2 = skewgpu.logabspfaffian(A)
+    assert r1 == r2
+    h1 = skewgpu.hessenberg(A).ev.cpu().numpy()
+    h2 = skewgpu.hessenberg(A).ev.cpu().numpy()
+    assert np.array_equal(h1, h2)
