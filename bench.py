@@ -434,7 +434,7 @@ def bench_hessenberg_large(n, reps, fp64_peak):
 
 
 def _bucket_ids(sizes):
-    edges = [32, 64, 96, 128, 160]
+    edges = [32, 64, 96, 128, 152]  # size buckets of skew_batch_plan_create
     out = []
     for n in sizes:
         out.append(next((e for e in edges if n <= e), 1 << 30))

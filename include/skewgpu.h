@@ -39,7 +39,8 @@ typedef enum {
   SKEW_SINGULAR = 5,        /* Pf(A) == 0: log|Pf| = -Inf, gradient not finite (odd n, pfaffian.jl:169) */
   SKEW_UNSUPPORTED = 6,
   SKEW_NO_MEMORY = 7,
-  SKEW_FALLBACK_USED = 8    /* QR stagnated; values from the symmetric-tridiagonal fallback (skeweigen.jl:132-137) */
+  SKEW_FALLBACK_USED = 8,   /* QR stagnated; values from the symmetric-tridiagonal fallback (skeweigen.jl:132-137) */
+  SKEW_TIMEOUT = 9          /* a bounded device-side wait gave up; outputs are not valid */
 } skew_status_t;
 
 typedef struct skew_handle_st* skew_handle_t;
@@ -74,9 +75,11 @@ SKEW_API int skew_logabspf_d(skew_handle_t h, double* A, int64_t n, int64_t lda,
 SKEW_API int skew_logabspf_grad_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* sign,
                          double* G, int64_t ldg, int* info);
 
-/* LA.eigvals!(A::SkewHermitian{Float64})  eigen.jl:2-6 -> skeweigvals! :312-318 ->
- * skewtrieigvals! skeweigen.jl:105-156.  vals_im[n] = imaginary parts of the eigenvalues
- * in the reference's order (eigenvalue k is i*vals_im[k]).  A is destroyed. */
+/* LA.eigvals!(A::SkewHermitian{Float64})  eigen.jl:2-6 -> skeweigvals! :312-318.
+ * vals_im[n] = imaginary parts of the eigenvalues (eigenvalue k is i*vals_im[k]),
+ * sorted descending: the order the reference returns from its own fallback
+ * (skeweigen.jl:134-137); the batched entry point keeps the reference's QR order
+ * (skewtrieigvals!, skeweigen.jl:105-156).  A is destroyed. */
 SKEW_API int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info);
 
 /* eigvals without any device allocation.  No counterpart in the reference.

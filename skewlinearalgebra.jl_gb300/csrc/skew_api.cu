@@ -76,6 +76,7 @@ const char* skew_status_string(int s) {
     case SKEW_UNSUPPORTED: return "unsupported";
     case SKEW_NO_MEMORY: return "out of memory";
     case SKEW_FALLBACK_USED: return "QR stagnated; symmetric tridiagonal fallback used";
+    case SKEW_TIMEOUT: return "a bounded device-side wait gave up (timeout)";
     default: return "unknown status";
   }
 }
@@ -150,7 +151,7 @@ static int single(skew_handle_t h, double* A, int64_t n, int64_t lda, double* G,
 static int blocked(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev, int* info,
                    size_t extra_doubles, double** extra) {
   if (!h || !A || lda < n || n > (1LL << 15)) return n > (1LL << 15) ? SKEW_UNSUPPORTED : SKEW_BAD_ARG;
-  const size_t wsd = blocked_ws_doubles((int)n);
+  const size_t wsd = blocked_ws_doubles((int)n) + persist_ws_extra_doubles();
   int st = ensure_ws(h, sizeof(double) * (wsd + extra_doubles));
   if (st) return st;
   double* ws = (double*)h->ws;
@@ -159,6 +160,16 @@ static int blocked(skew_handle_t h, double* A, int64_t n, int64_t lda, double* t
     if (!extra || extra_doubles < 2 * (size_t)n) return SKEW_BAD_ARG;
     ev = ws + wsd;
     tau = ws + wsd + n;
+  }
+  // one cooperative launch for all panels when v fits in shared memory; the
+  // multi-launch path otherwise (or with SKEW_BLOCKED_PERSISTENT=0)
+  const char* pv = getenv("SKEW_BLOCKED_PERSISTENT");
+  const bool persistent = n <= 24576 && !(pv && pv[0] == '0');
+  if (persistent) {
+    cudaError_t e = blocked_hessenberg_persistent(A, lda, (int)n, tau, ev, info, ws, h->sms, nullptr, h->stream);
+    if (e == cudaSuccess) return SKEW_OK;
+    if (e != cudaErrorNotSupported && e != cudaErrorCooperativeLaunchTooLarge) return SKEW_CUDA_ERROR;
+    cudaGetLastError();
   }
   CK(blocked_hessenberg(A, lda, (int)n, tau, ev, info, ws, h->sms, h->stream));
   return SKEW_OK;
@@ -177,9 +188,10 @@ int skew_logabspf_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* 
   if (n >= blocked_min_n() && (n % 2) == 0) {
     double* extra = nullptr;
     // workspace layout: [blocked ws][ev (n)][tau (n)][not-skew flag]; size it before the check
-    int st = ensure_ws(h, sizeof(double) * (blocked_ws_doubles((int)n) + 2 * (size_t)n + 1));
+    const size_t wsd = blocked_ws_doubles((int)n) + persist_ws_extra_doubles();
+    int st = ensure_ws(h, sizeof(double) * (wsd + 2 * (size_t)n + 1));
     if (st) return st;
-    double* flag = (double*)h->ws + blocked_ws_doubles((int)n) + 2 * (size_t)n;
+    double* flag = (double*)h->ws + wsd + 2 * (size_t)n;  // after blocked()'s ev/tau extra area
     if (check) CK(launch_check_skew(A, lda, (int)n, flag, h->sms, h->stream));
     st = blocked(h, A, n, lda, nullptr, nullptr, info, 2 * (size_t)n + 1, &extra);
     if (st) return st;
@@ -229,9 +241,10 @@ int skew_cis_d(skew_handle_t, double*, int64_t, int64_t, double*, int64_t, int*)
 // Batched plans
 // ---------------------------------------------------------------------------
 
-// Size buckets: the working copy stays in shared memory up to n = 160 (205 KB);
-// larger matrices work in a per-CTA global slot (L2 resident).
-static const int kBucketEdges[] = {32, 64, 96, 128, 160};
+// Size buckets: the working copy stays in shared memory up to n = 152 (227 KB
+// with the vectors and gradient scratch); larger matrices work in a per-CTA
+// global slot (L2 resident).
+static const int kBucketEdges[] = {32, 64, 96, 128, 152};
 
 // Tunables (environment overrides for sweeps): largest n whose working copy is
 // kept in shared memory, and resident CTAs per SM for the global-memory bucket
@@ -278,7 +291,7 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
     B.end = (int)u;
     B.nmax = std::max<int32_t>(P->n_host[order[t]], 1);
     const size_t smem_full = batch_smem_bytes(B.nmax, true);
-    B.smem_matrix = (smem_full <= 220 * 1024 && B.nmax <= env_int("SKEW_BATCH_SMEM_NMAX", 160)) ? 1 : 0;
+    B.smem_matrix = (smem_full <= 227 * 1024 && B.nmax <= env_int("SKEW_BATCH_SMEM_NMAX", 152)) ? 1 : 0;
     int occ = batch_occupancy(B.nmax, B.smem_matrix != 0);
     if (!B.smem_matrix) occ = std::max(1, std::min(occ, env_int("SKEW_BATCH_GLOBAL_CTAS_PER_SM", 2)));
     B.grid = (int)std::min<int64_t>((int64_t)h->sms * occ, u - t);

@@ -30,6 +30,7 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
 
 #include "skew_common.cuh"
 #include "skew_internal.h"
@@ -782,10 +783,24 @@ __global__ void __launch_bounds__(NT) single_kernel(SingleParams P) {
 // ---------------------------------------------------------------------------
 // Host launchers
 // ---------------------------------------------------------------------------
-constexpr int NT_SMALL = 128;  // shared-memory buckets up to n = 96
-constexpr int NT_LARGE = 256;
+constexpr int NT_SMALL = 128;   // shared-memory buckets up to n = 96
+constexpr int NT_LARGE = 256;   // shared-memory buckets above 96 (one CTA per SM)
+constexpr int NT_GLOBAL = 512;  // optional global-memory variant: one CTA of 16 warps per SM
 
-static int threads_for(int nmax, bool smem_matrix) { return (smem_matrix && nmax <= 96) ? NT_SMALL : NT_LARGE; }
+// Threads per CTA for global-memory working copies: 256 with two CTAs per SM
+// (measured best), or SKEW_BATCH_GLOBAL_NT=512 with one CTA per SM.
+static int global_threads() {
+  static int nt = [] {
+    const char* v = getenv("SKEW_BATCH_GLOBAL_NT");
+    return (v && atoi(v) == 512) ? NT_GLOBAL : 256;
+  }();
+  return nt;
+}
+
+static int threads_for(int nmax, bool smem_matrix) {
+  if (!smem_matrix) return global_threads();
+  return nmax <= 96 ? NT_SMALL : NT_LARGE;
+}
 
 size_t batch_smem_bytes(int nmax, bool smem_matrix) {
   const int nt = threads_for(nmax, smem_matrix);
@@ -808,7 +823,8 @@ cudaError_t launch_batch_pf(const BatchParams& P, int grid, cudaStream_t st, boo
   const int nt = threads_for(P.nmax, sm);
   if (sm && nt == NT_SMALL) return launch_t<NT_SMALL, true>(P, grid, smem, st, tridiag_only);
   if (sm) return launch_t<NT_LARGE, true>(P, grid, smem, st, tridiag_only);
-  return launch_t<NT_LARGE, false>(P, grid, smem, st, tridiag_only);
+  if (nt == NT_LARGE) return launch_t<NT_LARGE, false>(P, grid, smem, st, tridiag_only);
+  return launch_t<NT_GLOBAL, false>(P, grid, smem, st, tridiag_only);
 }
 
 cudaError_t launch_single(const SingleParams& P, cudaStream_t st) {
@@ -840,7 +856,8 @@ int batch_occupancy(int nmax, bool smem_matrix) {
   const int nt = threads_for(nmax, smem_matrix);
   if (smem_matrix && nt == NT_SMALL) return occ_t<NT_SMALL, true>(smem);
   if (smem_matrix) return occ_t<NT_LARGE, true>(smem);
-  return occ_t<NT_LARGE, false>(smem);
+  if (nt == NT_LARGE) return occ_t<NT_LARGE, false>(smem);
+  return occ_t<NT_GLOBAL, false>(smem);
 }
 
 }  // namespace skew

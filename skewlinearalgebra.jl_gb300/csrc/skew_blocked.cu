@@ -153,17 +153,36 @@ __global__ void __launch_bounds__(SYM_ROWS) sym_kernel(const double* __restrict_
     for (; j < ce; j++) a0 = fma(row[(int64_t)j * lda], sv[j - cb], a0);
     ws.ypart[(size_t)ch * n + r] = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
   }
-  // panel dot products, chunk-0 CTAs only: warp q handles dots q, q+8, ...
-  if (ch == 0 && i > 0) {
+  // panel dot products u1 = W_p^T v, u2 = A_p^T v over this tile's rows: dot d
+  // goes to chunk CTA d mod nchunk; each warp covers 32 rows of the tile.
+  if (i > 0) {
+    __shared__ double svr[SYM_ROWS];
+    __shared__ double sred[8][8];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int rb = r0 + tile * SYM_ROWS, re = min(n, rb + SYM_ROWS);
-    for (int d = w; d < 2 * i; d += 8) {
-      const int j = d < i ? d : d - i;
-      const double* col = (d < i) ? (ws.W + (size_t)j * n) : (A + (int64_t)(p + j) * lda);
-      double acc = 0.0;
-      for (int rr = rb + lane; rr < re; rr += 32) acc = fma(col[rr], vval(A, lda, c, rr, scale, tau), acc);
-      acc = warp_sum(acc);
-      if (lane == 0) ws.upart[(size_t)tile * 2 * BNB + d] = acc;
+    const int rb = r0 + tile * SYM_ROWS;
+    const int rr = rb + threadIdx.x;
+    svr[threadIdx.x] = (rr < n) ? vval(A, lda, c, rr, scale, tau) : 0.0;
+    __syncthreads();
+    const int ndots = 2 * i;
+    for (int d0 = ch * 8; d0 < ndots; d0 += nchunk * 8) {
+      // up to 8 dots at a time: warp w sums its 32 rows for each
+      const int nd = min(8, ndots - d0);
+      for (int q = 0; q < nd; q++) {
+        const int d = d0 + q;
+        const int j = d < i ? d : d - i;
+        const double* col = (d < i) ? (ws.W + (size_t)j * n) : (A + (int64_t)(p + j) * lda);
+        const double x = (rr < n) ? col[rr] * svr[threadIdx.x] : 0.0;
+        const double sw = warp_sum(x);
+        if (lane == 0) sred[q][w] = sw;
+      }
+      __syncthreads();
+      if ((int)threadIdx.x < nd) {
+        double acc = 0.0;
+#pragma unroll
+        for (int q = 0; q < 8; q++) acc += sred[threadIdx.x][q];
+        ws.upart[(size_t)tile * 2 * BNB + d0 + threadIdx.x] = acc;
+      }
+      __syncthreads();
     }
   }
 }
@@ -183,14 +202,23 @@ __global__ void __launch_bounds__(256) fin_kernel(double* __restrict__ A, int64_
   const double tau = ws.scal[3 * c + 1], scale = ws.scal[3 * c + 2];
   const int r0 = c + 1;
   const int tid = threadIdx.x;
-  // 1. u1, u2: sum the per-tile partials in a fixed order
-  for (int d = tid; d < 2 * i; d += 256) {
-    double s = 0.0;
-    for (int t = 0; t < nsymtiles; t++) s += ws.upart[(size_t)t * 2 * BNB + d];
-    if (d < i)
-      su[d] = s;
-    else
-      su[BNB + d - i] = s;
+  // 1. u1, u2: sum the per-tile partials in a fixed order (two threads per dot)
+  {
+    __shared__ double uhalf[2][2 * BNB];
+    const int d = tid & 127, half = tid >> 7;
+    if (d < 2 * i) {
+      double s = 0.0;
+      for (int t = half; t < nsymtiles; t += 2) s += ws.upart[(size_t)t * 2 * BNB + d];
+      uhalf[half][d] = s;
+    }
+    __syncthreads();
+    if (tid < 2 * i) {
+      const double s = uhalf[0][tid] + uhalf[1][tid];
+      if (tid < i)
+        su[tid] = s;
+      else
+        su[BNB + tid - i] = s;
+    }
   }
   __syncthreads();
   // 2. W[c+1, i] redundantly in every CTA (needed by the column c+1 update)
@@ -199,12 +227,10 @@ __global__ void __launch_bounds__(256) fin_kernel(double* __restrict__ A, int64_
     double acc = 0.0;
     for (int j = lane; j < i; j += 32)
       acc = fma(A[r0 + (int64_t)(p + j) * lda], su[j], fma(-ws.W[(size_t)j * n + r0], su[BNB + j], acc));
-    acc = warp_sum(acc);
-    if (lane == 0) {
-      double y = 0.0;
-      for (int q = 0; q < nchunk; q++) y += ws.ypart[(size_t)q * n + r0];
-      sWrow[i] = tau * (y + acc);
-    }
+    double y = 0.0;
+    for (int q = lane; q < nchunk; q += 32) y += ws.ypart[(size_t)q * n + r0];
+    acc = warp_sum(acc + y);
+    if (lane == 0) sWrow[i] = tau * acc;
     for (int j = lane; j < i; j += 32) {
       sWrow[j] = ws.W[(size_t)j * n + r0];
       sArow[j] = A[r0 + (int64_t)(p + j) * lda];
@@ -226,9 +252,10 @@ __global__ void __launch_bounds__(256) fin_kernel(double* __restrict__ A, int64_
   acc += __shfl_xor_sync(0xffffffffu, acc, 1);
   acc += __shfl_xor_sync(0xffffffffu, acc, 2);
   double y = 0.0;
-  if (valid && g == 0)
-    for (int q = 0; q < nchunk; q++) y += ws.ypart[(size_t)q * n + row];
-  y = __shfl_sync(0xffffffffu, y, (tid & 31) & ~3);
+  if (valid)
+    for (int q = g; q < nchunk; q += 4) y += ws.ypart[(size_t)q * n + row];
+  y += __shfl_xor_sync(0xffffffffu, y, 1);
+  y += __shfl_xor_sync(0xffffffffu, y, 2);
   double wri = tau * (y + acc);
   if (row == r0) wri = sWrow[i];  // one value for W[c+1, i] everywhere
   if (valid && g == 0) {
@@ -265,9 +292,11 @@ __global__ void __launch_bounds__(256) fin_kernel(double* __restrict__ A, int64_
   __syncthreads();
   if (!s_last) return;
   __threadfence();
-  if (tid == 0) {
+  if (tid < 32) {
     double ss = 0.0;
-    for (int t = 0; t < (int)gridDim.x; t++) ss += ((volatile double*)ws.sspart)[t];
+    for (int t = tid; t < (int)gridDim.x; t += 32) ss += ((volatile double*)ws.sspart)[t];
+    ss = warp_sum(ss);
+    if (tid != 0) return;
     *ws.ticket = 0u;
     const int c1 = c + 1;
     if (c1 <= n - 3) {
@@ -470,7 +499,7 @@ cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, doubl
       const int m = n - (c + 1);
       const int symtiles = (m + SYM_ROWS - 1) / SYM_ROWS;
       int nchunk = max((2 * sms + symtiles - 1) / symtiles, (m + 511) / 512);  // chunk <= 512 (sv stage)
-      nchunk = max(1, min(nchunk, min(ws.max_chunks, (m + 31) / 32)));
+      nchunk = max(1, min(nchunk, min(ws.max_chunks, (m + 63) / 64)));          // chunk >= 64
       const int chunk = (m + nchunk - 1) / nchunk;
       nchunk = (m + chunk - 1) / chunk;
       sym_kernel<<<dim3(symtiles, nchunk), SYM_ROWS, 0, st>>>(A, lda, n, p, c, ws, nchunk, chunk);
@@ -503,6 +532,460 @@ cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, doubl
   P.check = 0;
   P.want_pf = 0;
   return launch_single(P, st);
+}
+
+
+// ===========================================================================
+// Persistent variant: one cooperative launch runs every panel.  One CTA per SM;
+// the phases of a panel column are separated by a grid barrier instead of a
+// kernel boundary:
+//   A  v staged in shared memory; warps take work items from an atomic counter:
+//      the 2i panel dot products (one warp per dot over all rows, so u1/u2 are
+//      complete without partial sums) and the (32-row, column-chunk) tiles of
+//      y = A22 v (partial sums per chunk, summed in a fixed order in B).
+//   B  row blocks: v into column c, W[:, i], the update of column c+1 and the
+//      norm partials of column c+1.
+//   then every CTA builds reflector c+1 itself from the norm partials (same data,
+//   same order, so all CTAs agree) and no third barrier is needed.
+// After a panel, D applies the trailing update tile by tile (atomic counter).
+// Everything another CTA may have written during the kernel is read with
+// L2-only loads (__ldcg): L1 is not coherent across SMs inside one launch.
+// Grid barriers spin on a generation counter with a bounded number of polls;
+// on timeout the kernel records an error and every CTA returns.
+// ===========================================================================
+constexpr int P_NT = 256;
+constexpr int P_NW = P_NT / 32;
+constexpr long long BAR_POLL_LIMIT = 1LL << 22;  // x ~1 us per poll (L2 read + sleep): ~4 s
+
+struct PersistParams {
+  double* A;
+  int64_t lda;
+  int n, pend;  // panels cover reflector columns [0, pend)
+  double* tau;
+  double* ev;
+  double* W;       // n x BNB
+  double* ypart;   // maxck x n
+  double* u;       // 2 * BNB (u1, then u2 at BNB)
+  double* sspart;  // row-block norm partials
+  unsigned* sync;  // [0] barrier count, [1] barrier generation, [2] item counter
+  int* err;
+  int maxck;
+};
+
+__device__ __forceinline__ double ldg2(const double* p) { return __ldcg(p); }
+
+// Grid barrier; false if it gave up (error recorded) or another CTA did.
+__device__ bool gsync(const PersistParams& P) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned* gen = P.sync + 1;
+    volatile int* err = P.err;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned a = atomicAdd(P.sync, 1u);
+    int ok = 1;
+    if (a == gridDim.x - 1) {
+      atomicExch(P.sync, 0u);
+      __threadfence();
+      atomicAdd(P.sync + 1, 1u);
+    } else {
+      long long it = 0;
+      while (*gen == g) {
+        if (*err) {
+          ok = 0;
+          break;
+        }
+        if (++it > BAR_POLL_LIMIT) {
+          atomicExch(P.err, 1);
+          ok = 0;
+          break;
+        }
+        __nanosleep(100);
+      }
+    }
+    __threadfence();
+    s_ok = ok && !*err;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+struct Refl3 {
+  double beta, tau, scale;
+};
+
+// Reflector of column c from its entries, computed by the whole CTA.
+__device__ Refl3 refl_from_column(const PersistParams& P, int c, double* red) {
+  const int n = P.n;
+  const double* col = P.A + (int64_t)c * P.lda;
+  double part = 0.0;
+  for (int r = c + 2 + threadIdx.x; r < n; r += P_NT) {
+    const double x = ldg2(col + r);
+    part = fma(x, x, part);
+  }
+  const double ss = block_sum<P_NW>(part, red);
+  double xn = -1.0;
+  if (ss_needs_scaling(ss)) {
+    double mx = 0.0;
+    for (int r = c + 2 + threadIdx.x; r < n; r += P_NT) mx = fmax(mx, fabs(ldg2(col + r)));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    __shared__ double rm[P_NW];
+    if ((threadIdx.x & 31) == 0) rm[threadIdx.x >> 5] = mx;
+    __syncthreads();
+    mx = 0.0;
+    for (int q = 0; q < P_NW; q++) mx = fmax(mx, rm[q]);
+    double qq = 0.0;
+    if (mx > 0.0)
+      for (int r = c + 2 + threadIdx.x; r < n; r += P_NT) {
+        const double x = ldg2(col + r) / mx;
+        qq = fma(x, x, qq);
+      }
+    qq = block_sum<P_NW>(qq, red);
+    xn = mx * sqrt(qq);
+  }
+  const Reflector R = make_reflector(ldg2(col + c + 1), ss, xn);
+  return Refl3{R.beta, R.tau, R.scale};
+}
+
+// One 64 x 64 lower tile of the trailing update (same arithmetic as upd_kernel).
+__device__ void upd_tile(double* __restrict__ A, int64_t lda, int n, int p, int nbp, int q, const double* Wb, int t,
+                         double* sbuf) {
+  constexpr int KC = 16;
+  double (*sVR)[UPD_T] = reinterpret_cast<double (*)[UPD_T]>(sbuf);
+  double (*sWR)[UPD_T] = reinterpret_cast<double (*)[UPD_T]>(sbuf + KC * UPD_T);
+  double (*sVC)[UPD_T] = reinterpret_cast<double (*)[UPD_T]>(sbuf + 2 * KC * UPD_T);
+  double (*sWC)[UPD_T] = reinterpret_cast<double (*)[UPD_T]>(sbuf + 3 * KC * UPD_T);
+  double (*sT)[UPD_T + 1] = reinterpret_cast<double (*)[UPD_T + 1]>(sbuf);
+  int ti = (int)((sqrt(8.0 * t + 1.0) - 1.0) * 0.5);
+  while ((ti + 1) * (ti + 2) / 2 <= t) ti++;
+  while (ti * (ti + 1) / 2 > t) ti--;
+  const int tj = t - ti * (ti + 1) / 2;
+  const int R0 = q + ti * UPD_T, C0 = q + tj * UPD_T;
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) acc[a][b] = 0.0;
+  for (int k0 = 0; k0 < nbp; k0 += KC) {
+    const int kc = min(KC, nbp - k0);
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < KC * UPD_T; idx += P_NT) {
+      const int kk = idx / UPD_T, rr = idx - kk * UPD_T;
+      double vr = 0.0, wr = 0.0, vc = 0.0, wc = 0.0;
+      if (kk < kc) {
+        const int l = k0 + kk;
+        const int gr = R0 + rr, gc = C0 + rr;
+        if (gr < n) {
+          vr = ldg2(A + gr + (int64_t)(p + l) * lda);
+          wr = ldg2(Wb + (size_t)l * n + gr);
+        }
+        if (gc < n) {
+          vc = ldg2(A + gc + (int64_t)(p + l) * lda);
+          wc = ldg2(Wb + (size_t)l * n + gc);
+        }
+      }
+      sVR[kk][rr] = vr;
+      sWR[kk][rr] = wr;
+      sVC[kk][rr] = vc;
+      sWC[kk][rr] = wc;
+    }
+    __syncthreads();
+    for (int kk = 0; kk < kc; kk++) {
+      double vR[4], wR[4], vC[4], wC[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        vR[a] = sVR[kk][tx + 16 * a];
+        wR[a] = sWR[kk][tx + 16 * a];
+        vC[a] = sVC[kk][ty + 16 * a];
+        wC[a] = sWC[kk][ty + 16 * a];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) acc[a][b] = fma(vR[a], wC[b], fma(-wR[a], vC[b], acc[a][b]));
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) {
+      const int rr = tx + 16 * a, cc = ty + 16 * b;
+      const int gr = R0 + rr, gc = C0 + cc;
+      double val = 0.0;
+      if (gr < n && gc < n && gr > gc) {
+        double* pa = A + gr + (int64_t)gc * lda;
+        val = ldg2(pa) + acc[a][b];
+        *pa = val;
+      }
+      sT[rr][cc] = val;
+    }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < UPD_T * UPD_T; idx += P_NT) {
+    const int rr = idx / UPD_T, cc = idx - rr * UPD_T;
+    const int gr = R0 + rr, gc = C0 + cc;
+    if (gr < n && gc < n && gr > gc) A[gc + (int64_t)gr * lda] = neg(sT[rr][cc]);
+  }
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
+  extern __shared__ __align__(16) double psm[];  // v stage (n doubles) | update tile buffers
+  __shared__ double red[P_NW];
+  __shared__ double su[2 * BNB];
+  __shared__ double sWrow[BNB + 1], sArow[BNB + 1];
+  __shared__ int s_item;
+  const int n = P.n;
+  const int64_t lda = P.lda;
+  double* A = P.A;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int nwarps = gridDim.x * P_NW;
+  unsigned item_base = 0;  // running base of the shared item counter
+
+  Refl3 R = refl_from_column(P, 0, red);
+  if (blockIdx.x == 0 && tid == 0) {
+    P.ev[0] = R.beta;
+    P.tau[0] = R.tau;
+  }
+  int p = 0;
+  while (p < P.pend) {
+    const int nbp = min(BNB, P.pend - p);
+    for (int i = 0; i < nbp; i++) {
+      const int c = p + i, m = n - c - 1;
+      // ---- A: stage v, then items from the shared counter
+      for (int j = c + 1 + tid; j < n; j += P_NT)
+        psm[j] = (R.tau == 0.0) ? 0.0 : (j == c + 1 ? 1.0 : ldg2(A + j + (int64_t)c * lda) * R.scale);
+      __syncthreads();
+      const int nrt = (m + 31) >> 5;
+      int nck = max(1, min((4 * nwarps + nrt - 1) / nrt, (m + 31) >> 5));
+      nck = min(nck, P.maxck);
+      const int chunk = (m + nck - 1) / nck;
+      nck = (m + chunk - 1) / chunk;
+      const int ndots = 2 * i;
+      const unsigned nitems = (unsigned)(ndots + nrt * nck);
+      for (;;) {
+        unsigned it = 0;
+        if (lane == 0) it = atomicAdd(P.sync + 2, 1u) - item_base;
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= nitems) break;
+        if ((int)it < ndots) {
+          const int d = (int)it;
+          const int j = d < i ? d : d - i;
+          const double* col = (d < i) ? (P.W + (size_t)j * n) : (A + (int64_t)(p + j) * lda);
+          double a0 = 0.0, a1 = 0.0;
+          int r = c + 1 + lane;
+          for (; r + 32 < n; r += 64) {
+            a0 = fma(ldg2(col + r), psm[r], a0);
+            a1 = fma(ldg2(col + r + 32), psm[r + 32], a1);
+          }
+          if (r < n) a0 = fma(ldg2(col + r), psm[r], a0);
+          const double s = warp_sum(a0 + a1);
+          if (lane == 0) P.u[d < i ? d : BNB + j] = s;
+        } else {
+          const int qq = (int)it - ndots;
+          const int rt = qq / nck, ck = qq - rt * nck;
+          const int r = c + 1 + rt * 32 + lane;
+          const int cb = c + 1 + ck * chunk, ce = min(n, cb + chunk);
+          if (r < n) {
+            const double* row = A + r;
+            double a0 = 0, a1 = 0, a2 = 0, a3 = 0, a4 = 0, a5 = 0, a6 = 0, a7 = 0;
+            int j = cb;
+            for (; j + 7 < ce; j += 8) {
+              const double w0 = ldg2(row + (int64_t)j * lda), w1 = ldg2(row + (int64_t)(j + 1) * lda),
+                           w2 = ldg2(row + (int64_t)(j + 2) * lda), w3 = ldg2(row + (int64_t)(j + 3) * lda),
+                           w4 = ldg2(row + (int64_t)(j + 4) * lda), w5 = ldg2(row + (int64_t)(j + 5) * lda),
+                           w6 = ldg2(row + (int64_t)(j + 6) * lda), w7 = ldg2(row + (int64_t)(j + 7) * lda);
+              a0 = fma(w0, psm[j], a0);
+              a1 = fma(w1, psm[j + 1], a1);
+              a2 = fma(w2, psm[j + 2], a2);
+              a3 = fma(w3, psm[j + 3], a3);
+              a4 = fma(w4, psm[j + 4], a4);
+              a5 = fma(w5, psm[j + 5], a5);
+              a6 = fma(w6, psm[j + 6], a6);
+              a7 = fma(w7, psm[j + 7], a7);
+            }
+            for (; j < ce; j++) a0 = fma(ldg2(row + (int64_t)j * lda), psm[j], a0);
+            P.ypart[(size_t)ck * n + r] = ((a0 + a1) + (a2 + a3)) + ((a4 + a5) + (a6 + a7));
+          }
+        }
+      }
+      item_base += nitems + (unsigned)nwarps;  // every warp took exactly one failing ticket
+      if (!gsync(P)) return;
+      // ---- B: rows
+      const bool last = (i == nbp - 1);
+      for (int d = tid; d < 2 * i; d += P_NT) su[d < i ? d : BNB + d - i] = ldg2(P.u + (d < i ? d : BNB + d - i));
+      __syncthreads();
+      if (w == 0) {
+        const int r0 = c + 1;
+        double acc = 0.0;
+        for (int j = lane; j < i; j += 32)
+          acc = fma(ldg2(A + r0 + (int64_t)(p + j) * lda), su[j], fma(-ldg2(P.W + (size_t)j * n + r0), su[BNB + j], acc));
+        for (int q = lane; q < nck; q += 32) acc += ldg2(P.ypart + (size_t)q * n + r0);
+        acc = warp_sum(acc);
+        if (lane == 0) sWrow[i] = R.tau * acc;
+        for (int j = lane; j < i; j += 32) {
+          sWrow[j] = ldg2(P.W + (size_t)j * n + r0);
+          sArow[j] = ldg2(A + r0 + (int64_t)(p + j) * lda);
+        }
+        if (lane == 0) sArow[i] = (R.tau == 0.0) ? 0.0 : 1.0;
+      }
+      __syncthreads();
+      const int nfb = (m + FIN_ROWS - 1) / FIN_ROWS;
+      for (int fb = blockIdx.x; fb < nfb; fb += gridDim.x) {
+        const int row = c + 1 + fb * FIN_ROWS + (tid >> 2);
+        const int g = tid & 3;
+        const bool valid = row < n;
+        double vr = 0.0, acc = 0.0;
+        if (valid) {
+          vr = psm[row];
+          for (int j = g; j < i; j += 4)
+            acc = fma(ldg2(A + row + (int64_t)(p + j) * lda), su[j],
+                      fma(-ldg2(P.W + (size_t)j * n + row), su[BNB + j], acc));
+          for (int q = g; q < nck; q += 4) acc += ldg2(P.ypart + (size_t)q * n + row);
+        }
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        double wri = R.tau * acc;
+        if (row == c + 1) wri = sWrow[i];
+        if (valid && g == 0) {
+          P.W[(size_t)i * n + row] = wri;
+          A[row + (int64_t)c * lda] = vr;
+        }
+        double ssp = 0.0, uu = 0.0;
+        const bool doupd = valid && !last && row >= c + 2;
+        if (doupd)
+          for (int j = g; j <= i; j += 4) {
+            const double arj = (j == i) ? vr : ldg2(A + row + (int64_t)(p + j) * lda);
+            const double wrj = (j == i) ? wri : ldg2(P.W + (size_t)j * n + row);
+            uu = fma(arj, sWrow[j], fma(-wrj, sArow[j], uu));
+          }
+        uu += __shfl_xor_sync(0xffffffffu, uu, 1);
+        uu += __shfl_xor_sync(0xffffffffu, uu, 2);
+        if (doupd && g == 0) {
+          const double anew = ldg2(A + row + (int64_t)(c + 1) * lda) + uu;
+          A[row + (int64_t)(c + 1) * lda] = anew;
+          if (row >= c + 3) ssp = anew * anew;
+        }
+        const double sb = block_sum<P_NW>(ssp, red);
+        if (tid == 0) P.sspart[fb] = sb;
+      }
+      if (!gsync(P)) return;
+      if (!last) {
+        // reflector c+1, identically in every CTA
+        const int c1 = c + 1;
+        if (w == 0) {
+          double ss = 0.0;
+          for (int t = lane; t < nfb; t += 32) ss += ldg2(P.sspart + t);
+          ss = warp_sum(ss);
+          if (lane == 0) red[0] = ss;
+        }
+        __syncthreads();
+        const double ss = red[0];
+        __syncthreads();
+        if (ss_needs_scaling(ss)) {
+          R = refl_from_column(P, c1, red);
+        } else {
+          const Reflector Rf = make_reflector(ldg2(A + (c1 + 1) + (int64_t)c1 * lda), ss, -1.0);
+          R = Refl3{Rf.beta, Rf.tau, Rf.scale};
+        }
+        if (blockIdx.x == 0 && tid == 0) {
+          P.ev[c1] = R.beta;
+          P.tau[c1] = R.tau;
+        }
+      }
+    }
+    // ---- D: trailing update, tiles from the shared counter
+    const int q = p + nbp;
+    const int mt = (n - q + UPD_T - 1) / UPD_T;
+    const unsigned ntiles = (unsigned)(mt * (mt + 1) / 2);
+    for (;;) {
+      if (tid == 0) s_item = (int)(atomicAdd(P.sync + 2, 1u) - item_base);
+      __syncthreads();
+      const unsigned t = (unsigned)s_item;
+      __syncthreads();
+      if (t >= ntiles) break;
+      upd_tile(A, lda, n, p, nbp, q, P.W, (int)t, psm);
+    }
+    item_base += ntiles + gridDim.x;  // one failing ticket per CTA
+    if (!gsync(P)) return;
+    p = q;
+    if (p < P.pend) {
+      R = refl_from_column(P, p, red);
+      if (blockIdx.x == 0 && tid == 0) {
+        P.ev[p] = R.beta;
+        P.tau[p] = R.tau;
+      }
+    }
+  }
+}
+
+size_t persist_ws_extra_doubles() { return 2 * BNB + 8; }
+
+// info <- SKEW_TIMEOUT if a grid barrier of the persistent kernel gave up.
+__global__ void merge_err_kernel(const int* err, int* info) {
+  if (*err && info) *info = SKEW_TIMEOUT;
+}
+
+// Persistent driver; returns cudaErrorNotSupported when the device cannot
+// co-schedule one CTA per SM (the caller then uses the multi-launch path).
+cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double* tau, double* ev, int* info,
+                                          double* wsbase, int sms, int* err_dev, cudaStream_t st) {
+  BlockedWs ws = carve_ws(wsbase, n);
+  double* extra = wsbase + blocked_ws_doubles(n);  // u (2*BNB), 4 sync words, error flag
+  int* err_dev_local = (int*)(extra + 2 * BNB + 4);
+  if (!err_dev) err_dev = err_dev_local;
+  const size_t smem = max((size_t)n * sizeof(double), (size_t)UPD_T * (UPD_T + 1) * sizeof(double));
+  cudaError_t e = cudaFuncSetAttribute(persist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e != cudaSuccess) return e;
+  int occ = 0;
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persist_kernel, P_NT, smem);
+  if (e != cudaSuccess) return e;
+  if (occ < 1) return cudaErrorNotSupported;
+  const int grid = sms * (occ >= 2 ? 2 : 1);  // two CTAs per SM hide more load latency
+  PersistParams P;
+  P.A = A;
+  P.lda = lda;
+  P.n = n;
+  P.pend = n - TAIL;
+  P.tau = tau;
+  P.ev = ev;
+  P.W = ws.W;
+  P.ypart = ws.ypart;
+  P.u = extra;
+  P.sspart = ws.sspart;
+  P.sync = (unsigned*)(extra + 2 * BNB);
+  P.err = err_dev;
+  P.maxck = ws.max_chunks;
+  e = cudaMemsetAsync(P.sync, 0, 4 * sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
+  e = cudaMemsetAsync(err_dev, 0, sizeof(int), st);
+  if (e != cudaSuccess) return e;
+  if (P.pend > 0) {
+    void* args[] = {&P};
+    e = cudaLaunchCooperativeKernel((const void*)persist_kernel, dim3(grid), dim3(P_NT), args, smem, st);
+    if (e != cudaSuccess) return e;
+  }
+  SingleParams S;
+  const int p = P.pend > 0 ? P.pend : 0;
+  S.A = A + p + (int64_t)p * lda;
+  S.lda = lda;
+  S.n = n - p;
+  S.G = nullptr;
+  S.ldg = 0;
+  S.logpf = nullptr;
+  S.sign = nullptr;
+  S.ev = ev + p;
+  S.tau = tau + p;
+  S.info = info;
+  S.check = 0;
+  S.want_pf = 0;
+  e = launch_single(S, st);
+  if (e != cudaSuccess) return e;
+  merge_err_kernel<<<1, 1, 0, st>>>(err_dev, info);
+  return cudaGetLastError();
 }
 
 }  // namespace skew

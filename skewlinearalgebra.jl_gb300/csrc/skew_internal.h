@@ -67,6 +67,10 @@ cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, doub
 size_t blocked_ws_doubles(int n);
 cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, double* ev, int* info, double* ws, int sms,
                                cudaStream_t st);
+size_t persist_ws_extra_doubles();
+// One cooperative launch for all panels (grid barriers with bounded waits); then the tail.
+cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double* tau, double* ev, int* info,
+                                          double* ws, int sms, int* err_dev, cudaStream_t st);
 cudaError_t launch_pf_from_tridiag(const double* ev, const double* tau, int n, double* logpf, double* sign, int* info,
                                    const double* notskew, cudaStream_t st);
 cudaError_t launch_check_skew(const double* A, int64_t lda, int n, double* flag, int sms, cudaStream_t st);

@@ -20,6 +20,7 @@ SKEW_SINGULAR = 5
 SKEW_UNSUPPORTED = 6
 SKEW_NO_MEMORY = 7
 SKEW_FALLBACK_USED = 8
+SKEW_TIMEOUT = 9
 
 _vp = ctypes.c_void_p
 _i64 = ctypes.c_int64
