@@ -95,15 +95,17 @@ SKEW_API int skew_eigvals_noalloc_d(double* A, int64_t n, int64_t lda, double* v
                                     skew_stream_t stream);
 
 /* LA.eigen!(A::SkewHermitian{Float64})  eigen.jl:338-360 (skeweigen! + skewtrieigen_divided!).
- * vals_im[n]; eigenvectors V = Vr + i*Vi (n x n each, leading dimension ldv).  A is destroyed. */
+ * vals_im[n] in the reference's order; eigenvectors V = Vr + i*Vi (n x n each).  A is
+ * destroyed.  Requires lda == ldv == n and n <= 1024 (else SKEW_UNSUPPORTED). */
 SKEW_API int skew_eigen_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,
                  int64_t ldv, int* info);
 
-/* Base.exp(A::SkewHermitian{Float64})  exp.jl:3-35, :48.  E (n x n, lde) = exp(A). A destroyed. */
+/* Base.exp(A::SkewHermitian{Float64})  exp.jl:3-35, :48.  E (n x n) = exp(A). A destroyed.
+ * Requires lda == lde == n and n <= 1024. */
 SKEW_API int skew_exp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, int64_t lde, int* info);
 
 /* Base.cis(A::SkewHermitian{Float64})  exp.jl:99-110, :204.  C = cis(A) = exp(iA), Hermitian,
- * ComplexF64 interleaved (re, im), leading dimension ldc in complex elements. A destroyed. */
+ * ComplexF64 interleaved (re, im).  A destroyed.  Requires lda == ldc == n and n <= 1024. */
 SKEW_API int skew_cis_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* C, int64_t ldc, int* info);
 
 /* ---------------------------------------------------------------------------
@@ -122,6 +124,30 @@ SKEW_API int skew_batch_logabspf_d(skew_batch_plan_t plan, const double* const* 
 
 /* eigvals for every matrix: vals_im[b] (device pointers) receives n[b] values. */
 SKEW_API int skew_batch_eigvals_d(skew_batch_plan_t plan, const double* const* A, double* const* vals_im, int* status);
+
+/* eigen for every matrix (skeweigen! + skewtrieigen_divided!, eigen.jl:338-360): vals_im[b] (n),
+ * Vr[b], Vi[b] (n x n, leading dimension n) device pointers; eigenvectors are Vr + i*Vi.
+ * status[b]: SKEW_OK, SKEW_FALLBACK_USED (the reference's LAPACK fallback path,
+ * skeweigen.jl:364-371, taken on the GPU) or SKEW_NO_CONVERGENCE.  n <= 1024. */
+SKEW_API int skew_batch_eigen_d(skew_batch_plan_t plan, const double* const* A, double* const* vals_im,
+                                double* const* Vr, double* const* Vi, int* status);
+
+/* exp(A_b) for every matrix (skewexp!, exp.jl:3-35): E[b] n x n real, leading dimension n. */
+SKEW_API int skew_batch_exp_d(skew_batch_plan_t plan, const double* const* A, double* const* E, int* status);
+
+/* cis(A_b) = exp(i A_b) for every matrix (skewcis!, exp.jl:99-110): C[b] n x n ComplexF64
+ * interleaved, leading dimension n (complex elements). */
+SKEW_API int skew_batch_cis_d(skew_batch_plan_t plan, const double* const* A, double* const* C, int* status);
+
+/* Adjoint of exp (no reference counterpart): G[b] = d<Cbar_b, exp(A_b)>/dA_b, by
+ * Daleckii-Krein divided differences on the eigendecomposition.  Cbar[b], G[b] n x n real. */
+SKEW_API int skew_batch_exp_vjp_d(skew_batch_plan_t plan, const double* const* A, const double* const* Cbar,
+                                  double* const* G, int* status);
+
+/* Single-matrix adjoint of exp (no reference counterpart): G = d<Cbar, exp(A)>/dA.
+ * A is destroyed; lda, ldg must equal n (n <= 1024). */
+SKEW_API int skew_exp_vjp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* Cbar, double* G,
+                            int64_t ldg, int* info);
 
 /* Diagnostics: measured FP64 DFMA throughput of the current device in TFLOP/s
  * (runs a short microbenchmark on the handle's stream and synchronizes). */

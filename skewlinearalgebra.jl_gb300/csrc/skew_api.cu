@@ -22,6 +22,8 @@ struct skew_handle_st {
   int sms = 0;
   void* ws = nullptr;  // grow-only workspace, stream ordered
   size_t ws_bytes = 0;
+  struct skew_batch_plan_st* plan1 = nullptr;  // batch-of-one plan for single-matrix eigen/exp/cis
+  int64_t plan1_n = 0;
 };
 
 struct Bucket {
@@ -43,6 +45,29 @@ struct skew_batch_plan_st {
   double* d_gws = nullptr;
   int64_t ev_total = 0;
   size_t gws_total = 0;
+  // eigen / exp workspace, allocated on first use
+  bool eig_ready = false;
+  int nmax = 0;
+  double* e_refl = nullptr;   // sum n^2
+  double* e_tau = nullptr;    // ev_total (ev offsets)
+  double* e_evb = nullptr;
+  double* e_G = nullptr;
+  double* e_log = nullptr;
+  double* e_work = nullptr;   // 4 sum n^2
+  double* e_vr = nullptr;     // internal eigenvectors (exp, cis, vjp)
+  double* e_vi = nullptr;
+  double* e_vals = nullptr;   // internal eigenvalues (ev offsets)
+  int64_t* e_off_log = nullptr;
+  int64_t* e_cap_log = nullptr;
+  int64_t* e_log_len = nullptr;
+  int64_t* e_off_w = nullptr;
+  double** e_p_refl = nullptr;  // device pointer arrays
+  double** e_p_vr = nullptr;
+  double** e_p_vi = nullptr;
+  double** e_p_vals = nullptr;
+  double** e_p_scratch = nullptr;  // 8 x count: single-call pointer arrays
+  int* e_status = nullptr;
+  unsigned* e_counter = nullptr;
 };
 
 #define CK(x)                                  \
@@ -96,6 +121,7 @@ int skew_create(skew_handle_t* handle) {
 
 int skew_destroy(skew_handle_t h) {
   if (!h) return SKEW_BAD_ARG;
+  if (h->plan1) skew_batch_plan_destroy(h->plan1);
   if (h->ws) {
     cudaFreeAsync(h->ws, h->stream);
     cudaStreamSynchronize(h->stream);
@@ -231,11 +257,6 @@ int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* v
   return SKEW_OK;
 }
 
-int skew_eigen_d(skew_handle_t, double*, int64_t, int64_t, double*, double*, double*, int64_t, int*) {
-  return SKEW_UNSUPPORTED;
-}
-int skew_exp_d(skew_handle_t, double*, int64_t, int64_t, double*, int64_t, int*) { return SKEW_UNSUPPORTED; }
-int skew_cis_d(skew_handle_t, double*, int64_t, int64_t, double*, int64_t, int*) { return SKEW_UNSUPPORTED; }
 
 // ---------------------------------------------------------------------------
 // Batched plans
@@ -337,13 +358,19 @@ int skew_batch_plan_destroy(skew_batch_plan_t P) {
   if (P->d_counters) cudaFreeAsync(P->d_counters, st);
   if (P->d_ev) cudaFreeAsync(P->d_ev, st);
   if (P->d_gws) cudaFreeAsync(P->d_gws, st);
+  void* eig[] = {P->e_refl, P->e_tau, P->e_evb, P->e_G, P->e_log, P->e_work, P->e_vr, P->e_vi, P->e_vals,
+                 P->e_off_log, P->e_cap_log, P->e_log_len, P->e_off_w, P->e_p_refl, P->e_p_vr, P->e_p_vi,
+                 P->e_p_vals, P->e_p_scratch, P->e_status, P->e_counter};
+  for (void* q : eig)
+    if (q) cudaFreeAsync(q, st);
   cudaStreamSynchronize(st);
   delete P;
   return SKEW_OK;
 }
 
 static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logpf, double* sign,
-                       double* const* grad, int* status, bool tridiag_only) {
+                       double* const* grad, int* status, bool tridiag_only, double* tau_out = nullptr,
+                       double* const* refl_out = nullptr) {
   cudaStream_t st = P->h->stream;
   CK(cudaMemsetAsync(P->d_counters, 0, sizeof(unsigned) * std::max<size_t>(P->buckets.size(), 1), st));
   for (size_t i = 0; i < P->buckets.size(); i++) {
@@ -365,6 +392,8 @@ static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logp
     bp.grad = grad;
     bp.ev_out = tridiag_only ? P->d_ev : nullptr;
     bp.ev_off = P->d_ev_off;
+    bp.tau_out = tau_out;
+    bp.refl_out = refl_out;
     bp.status = status;
     CK(launch_batch_pf(bp, B.grid, st, tridiag_only));
   }
@@ -394,6 +423,245 @@ int skew_batch_eigvals_d(skew_batch_plan_t P, const double* const* A, double* co
   tp.status = status;
   CK(launch_batch_trieig(tp, P->h->stream));
   return SKEW_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Eigenvectors / exp / cis / exp adjoint (skew_eigen.cu)
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void fill_ptrs_kernel(double** dst, double* base, const int64_t* off, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < count) dst[i] = base + off[i];
+}
+__global__ void set8_kernel(double** dst, double* a, double* b, double* c, double* d, double* e, double* f,
+                            double* g, double* h) {
+  dst[0] = a;
+  dst[1] = b;
+  dst[2] = c;
+  dst[3] = d;
+  dst[4] = e;
+  dst[5] = f;
+  dst[6] = g;
+  dst[7] = h;
+}
+__global__ void copy_status_kernel(const int* src, int* dst) { *dst = *src; }
+}  // namespace
+
+static int eigen_ws(skew_batch_plan_t P) {
+  if (P->eig_ready) return SKEW_OK;
+  cudaStream_t st = P->h->stream;
+  const int64_t count = P->count;
+  std::vector<int64_t> off_sq(count), off_log(count), cap_log(count), off_w(count);
+  int64_t sq = 0, lg = 0, w = 0;
+  int nmax = 1;
+  for (int64_t b = 0; b < count; b++) {
+    const int64_t n = std::max<int32_t>(P->n_host[b], 1);
+    nmax = std::max<int>(nmax, (int)n);
+    off_sq[b] = sq;
+    sq += n * n;
+    off_log[b] = lg;
+    cap_log[b] = 3 * n * n + 64;
+    lg += cap_log[b];
+    off_w[b] = w;
+    w += 4 * n * n;
+  }
+  P->nmax = nmax;
+  bool ok = true;
+  auto alloc = [&](void** p, size_t bytes) { ok &= cudaMallocAsync(p, std::max<size_t>(bytes, 8), st) == cudaSuccess; };
+  alloc((void**)&P->e_refl, sizeof(double) * sq);
+  alloc((void**)&P->e_tau, sizeof(double) * P->ev_total);
+  alloc((void**)&P->e_evb, sizeof(double) * P->ev_total);
+  alloc((void**)&P->e_G, sizeof(double) * P->ev_total);
+  alloc((void**)&P->e_vals, sizeof(double) * P->ev_total);
+  alloc((void**)&P->e_log, sizeof(double) * lg);
+  alloc((void**)&P->e_work, sizeof(double) * w);
+  alloc((void**)&P->e_vr, sizeof(double) * sq);
+  alloc((void**)&P->e_vi, sizeof(double) * sq);
+  alloc((void**)&P->e_off_log, sizeof(int64_t) * count);
+  alloc((void**)&P->e_cap_log, sizeof(int64_t) * count);
+  alloc((void**)&P->e_log_len, sizeof(int64_t) * count);
+  alloc((void**)&P->e_off_w, sizeof(int64_t) * count);
+  alloc((void**)&P->e_p_refl, sizeof(double*) * count);
+  alloc((void**)&P->e_p_vr, sizeof(double*) * count);
+  alloc((void**)&P->e_p_vi, sizeof(double*) * count);
+  alloc((void**)&P->e_p_vals, sizeof(double*) * count);
+  alloc((void**)&P->e_p_scratch, sizeof(double*) * 8);
+  alloc((void**)&P->e_status, sizeof(int) * count);
+  alloc((void**)&P->e_counter, sizeof(unsigned));
+  if (!ok) return SKEW_NO_MEMORY;
+  int64_t* d_off_sq = nullptr;
+  ok &= cudaMallocAsync(&d_off_sq, sizeof(int64_t) * count, st) == cudaSuccess;
+  ok &= cudaMemcpyAsync(d_off_sq, off_sq.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, st) == cudaSuccess;
+  ok &= cudaMemcpyAsync(P->e_off_log, off_log.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, st) ==
+        cudaSuccess;
+  ok &= cudaMemcpyAsync(P->e_cap_log, cap_log.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, st) ==
+        cudaSuccess;
+  ok &= cudaMemcpyAsync(P->e_off_w, off_w.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, st) ==
+        cudaSuccess;
+  if (!ok) return SKEW_CUDA_ERROR;
+  const int g = (int)((count + 255) / 256);
+  fill_ptrs_kernel<<<g, 256, 0, st>>>(P->e_p_refl, P->e_refl, d_off_sq, (int)count);
+  fill_ptrs_kernel<<<g, 256, 0, st>>>(P->e_p_vr, P->e_vr, d_off_sq, (int)count);
+  fill_ptrs_kernel<<<g, 256, 0, st>>>(P->e_p_vi, P->e_vi, d_off_sq, (int)count);
+  fill_ptrs_kernel<<<g, 256, 0, st>>>(P->e_p_vals, P->e_vals, P->d_ev_off, (int)count);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));  // host vectors go out of scope
+  cudaFree(d_off_sq);
+  P->eig_ready = true;
+  return SKEW_OK;
+}
+
+// Reduction, QR with logged rotations, vectors, back-transformation.
+static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const* vals, double* const* Vr,
+                     double* const* Vi, EigenBatch* Eout) {
+  int s = eigen_ws(P);
+  if (s) return s;
+  cudaStream_t st = P->h->stream;
+  s = run_buckets(P, A, nullptr, nullptr, nullptr, nullptr, true, P->e_tau, P->e_p_refl);
+  if (s) return s;
+  EigenBatch E;
+  E.count = (int32_t)P->count;
+  E.nmax = P->nmax;
+  E.order = P->d_order;
+  E.n = P->d_n;
+  E.off_n = P->d_ev_off;
+  E.ev = P->d_ev;
+  E.evb = P->e_evb;
+  E.tau = P->e_tau;
+  E.G = P->e_G;
+  E.vals = vals ? vals : P->e_p_vals;
+  E.log = P->e_log;
+  E.off_log = P->e_off_log;
+  E.cap_log = P->e_cap_log;
+  E.log_len = P->e_log_len;
+  E.status = P->e_status;
+  E.counter = P->e_counter;
+  E.Vr = Vr ? Vr : P->e_p_vr;
+  E.Vi = Vi ? Vi : P->e_p_vi;
+  E.refl = P->e_p_refl;
+  E.work = P->e_work;
+  E.off_w = P->e_off_w;
+  E.out = nullptr;
+  E.cot = nullptr;
+  const int grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
+  CK(launch_eigen_chain(E, st));
+  CK(launch_eigen_vectors(E, grid, st));
+  CK(launch_eigen_back(E, grid, P->nmax, st));
+  *Eout = E;
+  return SKEW_OK;
+}
+
+static int finish_status(skew_batch_plan_t P, int* status) {
+  if (status)
+    CK(cudaMemcpyAsync(status, P->e_status, sizeof(int) * P->count, cudaMemcpyDeviceToDevice, P->h->stream));
+  return SKEW_OK;
+}
+
+int skew_batch_eigen_d(skew_batch_plan_t P, const double* const* A, double* const* vals_im, double* const* Vr,
+                       double* const* Vi, int* status) {
+  if (!P || (P->count > 0 && (!A || !vals_im || !Vr || !Vi))) return SKEW_BAD_ARG;
+  if (P->count == 0) return SKEW_OK;
+  EigenBatch E;
+  int s = eigen_run(P, A, vals_im, Vr, Vi, &E);
+  if (s) return s;
+  return finish_status(P, status);
+}
+
+static int func_run(skew_batch_plan_t P, const double* const* A, double* const* out, const double* const* cot,
+                    int mode, int* status) {
+  EigenBatch E;
+  int s = eigen_run(P, A, nullptr, nullptr, nullptr, &E);
+  if (s) return s;
+  E.out = out;
+  E.cot = cot;
+  const int grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
+  CK(launch_eigen_func(E, grid, mode, P->h->stream));
+  return finish_status(P, status);
+}
+
+int skew_batch_exp_d(skew_batch_plan_t P, const double* const* A, double* const* E, int* status) {
+  if (!P || (P->count > 0 && (!A || !E))) return SKEW_BAD_ARG;
+  if (P->count == 0) return SKEW_OK;
+  return func_run(P, A, E, nullptr, 0, status);
+}
+
+int skew_batch_cis_d(skew_batch_plan_t P, const double* const* A, double* const* C, int* status) {
+  if (!P || (P->count > 0 && (!A || !C))) return SKEW_BAD_ARG;
+  if (P->count == 0) return SKEW_OK;
+  return func_run(P, A, C, nullptr, 1, status);
+}
+
+int skew_batch_exp_vjp_d(skew_batch_plan_t P, const double* const* A, const double* const* Cbar, double* const* G,
+                         int* status) {
+  if (!P || (P->count > 0 && (!A || !Cbar || !G))) return SKEW_BAD_ARG;
+  if (P->count == 0) return SKEW_OK;
+  return func_run(P, A, G, Cbar, 2, status);
+}
+
+// Single matrices run as a batch of one through a plan cached on the handle.
+static int single_plan(skew_handle_t h, int64_t n, skew_batch_plan_t* out) {
+  if (h->plan1 && h->plan1_n == n) {
+    *out = h->plan1;
+    return SKEW_OK;
+  }
+  if (h->plan1) skew_batch_plan_destroy(h->plan1);
+  h->plan1 = nullptr;
+  skew_batch_plan_t p = nullptr;
+  int s = skew_batch_plan_create(h, &n, 1, &p);
+  if (s) return s;
+  s = eigen_ws(p);
+  if (s) {
+    skew_batch_plan_destroy(p);
+    return s;
+  }
+  h->plan1 = p;
+  h->plan1_n = n;
+  *out = p;
+  return SKEW_OK;
+}
+
+static int single_func(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,
+                       int64_t ldv, double* out, int64_t ldo, const double* cot, int mode, int* info) {
+  if (!h || n < 1 || !A || lda != n || (ldv && ldv != n) || (ldo && ldo != n)) return n < 1 ? SKEW_BAD_ARG
+                                                                                            : SKEW_UNSUPPORTED;
+  if (n > kSingleMax) return SKEW_UNSUPPORTED;
+  skew_batch_plan_t P = nullptr;
+  int s = single_plan(h, n, &P);
+  if (s) return s;
+  double** arr = P->e_p_scratch;  // [0] A, [1] vals, [2] Vr, [3] Vi, [4] out, [5] cot
+  set8_kernel<<<1, 1, 0, h->stream>>>(arr, A, vals_im, Vr, Vi, out, (double*)cot, nullptr, nullptr);
+  CK(cudaGetLastError());
+  if (mode < 0) {
+    EigenBatch E;
+    s = eigen_run(P, (const double* const*)arr, arr + 1, arr + 2, arr + 3, &E);
+  } else {
+    s = func_run(P, (const double* const*)arr, arr + 4, (const double* const*)(arr + 5), mode, nullptr);
+  }
+  if (s) return s;
+  if (info) {
+    copy_status_kernel<<<1, 1, 0, h->stream>>>(P->e_status, info);
+    CK(cudaGetLastError());
+  }
+  return SKEW_OK;
+}
+
+int skew_eigen_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,
+                 int64_t ldv, int* info) {
+  if (!vals_im || !Vr || !Vi) return SKEW_BAD_ARG;
+  return single_func(h, A, n, lda, vals_im, Vr, Vi, ldv, nullptr, 0, nullptr, -1, info);
+}
+int skew_exp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, int64_t lde, int* info) {
+  if (!E) return SKEW_BAD_ARG;
+  return single_func(h, A, n, lda, nullptr, nullptr, nullptr, 0, E, lde, nullptr, 0, info);
+}
+int skew_cis_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* C, int64_t ldc, int* info) {
+  if (!C) return SKEW_BAD_ARG;
+  return single_func(h, A, n, lda, nullptr, nullptr, nullptr, 0, C, ldc, nullptr, 1, info);
+}
+int skew_exp_vjp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* Cbar, double* G, int64_t ldg,
+                   int* info) {
+  if (!Cbar || !G) return SKEW_BAD_ARG;
+  return single_func(h, A, n, lda, nullptr, nullptr, nullptr, 0, G, ldg, Cbar, 2, info);
 }
 
 // ---------------------------------------------------------------------------

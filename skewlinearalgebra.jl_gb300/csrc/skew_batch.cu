@@ -112,23 +112,6 @@ __device__ double block_maxabs(double x, double* red) {
   return s;
 }
 
-// Sum over the 32 lanes of 32 per-lane values at once (butterfly transpose):
-// on return lane L holds sum_lanes v[L].  31 adds instead of 32 x 5.
-__device__ __forceinline__ double warp_transpose_sum32(double (&v)[32]) {
-  const int lane = threadIdx.x & 31;
-#pragma unroll
-  for (int s = 16; s >= 1; s >>= 1) {
-    const bool up = lane & s;
-#pragma unroll
-    for (int i = 0; i < s; i++) {
-      const double send = up ? v[i] : v[i + s];
-      const double keep = up ? v[i + s] : v[i];
-      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, s);
-    }
-  }
-  return v[0];
-}
-
 // ---------------------------------------------------------------------------
 // Copy-in with the exact skew check (isskewhermitian, skewhermitian.jl:84-94)
 // ---------------------------------------------------------------------------
@@ -402,27 +385,6 @@ __device__ void tinv_init(const GMat& G, int n, const Smem& s) {
   __syncthreads();
 }
 
-// Reduce per-thread partial values part[0..npair) (npair <= 32) over the block
-// into out[0..npair); scratch holds NW*32 doubles.
-template <int NT>
-__device__ void block_reduce_pairs(double (&part)[32], int npair, double* scratch, double* out) {
-  constexpr int NW = NT / 32;
-  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const double mine = warp_transpose_sum32(part);  // lane L holds the warp's sum for slot L
-  scratch[w * 32 + lane] = mine;
-  __syncthreads();
-  if ((int)threadIdx.x < npair) {
-    double acc = 0.0;
-#pragma unroll
-    for (int q = 0; q < NW; q++) acc += scratch[q * 32 + threadIdx.x];
-    out[threadIdx.x] = acc;
-  }
-  __syncthreads();
-}
-
-// Pair (l1 < l2) -> slot; for GNB = 8 there are 28 slots.
-__device__ __forceinline__ int pair_slot(int l1, int l2) { return l1 * GNB - (l1 * (l1 + 1)) / 2 + (l2 - l1 - 1); }
-
 // G <- Q G Q^T, G holding -1/2 T^{-1} on entry; reflectors from W's lower part.
 template <int NT, class MW>
 __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
@@ -653,8 +615,9 @@ struct Job {
   int64_t ldg;
   double* logpf;
   double* sign;
-  double* ev_out;   // optional (n-1)
-  double* tau_out;  // optional (n-1)
+  double* ev_out;    // optional (n-1)
+  double* tau_out;   // optional (n-1)
+  double* refl_out;  // optional n x n: the reduced matrix (reflectors below the subdiagonal)
   int* status;
   bool check;
   bool want_pf;
@@ -687,6 +650,13 @@ __device__ void run_job(const Job& J, const MW& W, bool inplace, const Smem& s) 
     if (!J.ev_out) return;
   }
   forward<NT>(W, n, s);
+  if (J.refl_out) {
+    const int64_t total = (int64_t)n * n;
+    for (int64_t e = threadIdx.x; e < total; e += NT) {
+      const int j = (int)(e / n), i = (int)(e - (int64_t)j * n);
+      J.refl_out[e] = W.at(i, j);
+    }
+  }
   if (J.ev_out || J.tau_out)
     for (int a = threadIdx.x; a < n - 1; a += NT) {
       if (J.ev_out) J.ev_out[a] = s.ev[a];
@@ -745,7 +715,8 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchParams P, int tridiag_on
     J.logpf = tridiag_only ? nullptr : P.logpf + b;
     J.sign = tridiag_only ? nullptr : P.sign + b;
     J.ev_out = P.ev_out ? P.ev_out + P.ev_off[b] : nullptr;
-    J.tau_out = nullptr;
+    J.tau_out = P.tau_out ? P.tau_out + P.ev_off[b] : nullptr;
+    J.refl_out = P.refl_out ? P.refl_out[b] : nullptr;
     J.status = tridiag_only ? nullptr : P.status + b;
     J.check = P.check != 0;
     J.want_pf = !tridiag_only;
@@ -773,6 +744,7 @@ __global__ void __launch_bounds__(NT) single_kernel(SingleParams P) {
   J.sign = P.sign;
   J.ev_out = P.ev;
   J.tau_out = P.tau;
+  J.refl_out = nullptr;
   J.status = P.info;
   J.check = P.check != 0;
   J.want_pf = P.want_pf != 0;

@@ -82,6 +82,44 @@ __device__ __forceinline__ Reflector make_reflector(double alpha, double ss, dou
   return R;
 }
 
+// Sum over the 32 lanes of 32 per-lane values at once (butterfly transpose):
+// on return lane L holds sum_lanes v[L].  31 adds instead of 32 x 5.
+__device__ __forceinline__ double warp_transpose_sum32(double (&v)[32]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 16; s >= 1; s >>= 1) {
+    const bool up = lane & s;
+#pragma unroll
+    for (int i = 0; i < s; i++) {
+      const double send = up ? v[i] : v[i + s];
+      const double keep = up ? v[i + s] : v[i];
+      v[i] = keep + __shfl_xor_sync(0xffffffffu, send, s);
+    }
+  }
+  return v[0];
+}
+
+// Reduce per-thread partial values part[0..npair) (npair <= 32) over the block
+// into out[0..npair); scratch holds NW*32 doubles.
+template <int NT>
+__device__ void block_reduce_pairs(double (&part)[32], int npair, double* scratch, double* out) {
+  constexpr int NW = NT / 32;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double mine = warp_transpose_sum32(part);  // lane L holds the warp's sum for slot L
+  scratch[w * 32 + lane] = mine;
+  __syncthreads();
+  if ((int)threadIdx.x < npair) {
+    double acc = 0.0;
+#pragma unroll
+    for (int q = 0; q < NW; q++) acc += scratch[q * 32 + threadIdx.x];
+    out[threadIdx.x] = acc;
+  }
+  __syncthreads();
+}
+
+// Pair (l1 < l2) of 8 columns -> slot; 28 slots.
+__device__ __forceinline__ int pair_slot(int l1, int l2) { return l1 * 8 - (l1 * (l1 + 1)) / 2 + (l2 - l1 - 1); }
+
 // Bounded spin on a device flag: returns false if `limit` polls pass first.
 __device__ __forceinline__ bool spin_until_geq(const volatile unsigned* flag, unsigned target, long long limit) {
   for (long long it = 0; it < limit; it++) {

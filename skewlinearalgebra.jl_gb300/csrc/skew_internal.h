@@ -21,7 +21,9 @@ struct BatchParams {
   double* sign;            // [count] or null
   double* const* grad;     // [count] device pointers or null
   double* ev_out;          // packed ev (n-1 per matrix) or null
-  const int64_t* ev_off;   // offsets into ev_out
+  const int64_t* ev_off;   // offsets into ev_out (and tau_out)
+  double* tau_out;         // packed tau, same offsets, or null
+  double* const* refl_out; // [count] n x n buffers receiving the reduced matrix (reflectors) or null
   int* status;             // [count] or null
 };
 
@@ -62,6 +64,38 @@ cudaError_t launch_batch_trieig(const TrieigParams& P, cudaStream_t st);
 // Eigenvalues of one skew tridiagonal by bisection on the equivalent zero-diagonal
 // symmetric tridiagonal; vals_im sorted descending.
 cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, double* scratch2, cudaStream_t st);
+
+// Eigenvectors / exp / cis / exp adjoint for batches of real skew matrices (skew_eigen.cu).
+// Leading dimensions of every per-matrix n x n buffer are n.
+struct EigenBatch {
+  int32_t count;
+  int32_t nmax;
+  const int32_t* order;      // processing order (largest first)
+  const int32_t* n;          // sizes
+  const int64_t* off_n;      // packed offsets (>= max(n,1) apart) of ev, evb, tau, G
+  double* ev;                // subdiagonals from the reduction (consumed by the QR)
+  double* evb;               // copy kept for the stagnation fallback
+  double* tau;               // reflector scalars
+  double* G;                 // reducetozero rotations (odd n)
+  double* const* vals;       // [count] -> n (imaginary parts of the eigenvalues)
+  double* log;               // rotation logs
+  const int64_t* off_log;    // per-matrix log offsets
+  const int64_t* cap_log;    // per-matrix log capacity (doubles)
+  int64_t* log_len;          // per-matrix log length
+  int* status;               // per-matrix skew_status_t
+  unsigned* counter;         // work counter of the per-matrix kernels
+  double* const* Vr;         // [count] n x n real parts of the eigenvectors
+  double* const* Vi;         // [count] n x n imaginary parts
+  double* const* refl;       // [count] n x n reduced matrices (reflectors)
+  double* work;              // 4 n^2 per matrix
+  const int64_t* off_w;
+  double* const* out;        // [count] exp (real) / cis (complex interleaved) / adjoint (real)
+  const double* const* cot;  // [count] cotangents for the adjoint
+};
+cudaError_t launch_eigen_chain(const EigenBatch& E, cudaStream_t st);
+cudaError_t launch_eigen_vectors(const EigenBatch& E, int grid, cudaStream_t st);
+cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStream_t st);
+cudaError_t launch_eigen_func(const EigenBatch& E, int grid, int mode, cudaStream_t st);
 
 // Multi-CTA blocked reduction of one large matrix (skew_blocked.cu).
 size_t blocked_ws_doubles(int n);

@@ -20,23 +20,20 @@
 
 namespace skew {
 
-// getgivens (skeweigen.jl:3-7): c = a/hypot(a,b), s = b/hypot(a,b); (1, 0) if both
-// vanish.  One reciprocal square root in the common exponent range.
+// getgivens (skeweigen.jl:3-7): nm = hypot(a, b); (1, 0) if nm == 0, else
+// (a/nm, b/nm).  The QR steps below round every product and sum separately (no
+// fused multiply-add), as the reference's Float64 code does: the iteration's
+// deflation decisions depend on the last bits of ev, so matching the reference's
+// rounding keeps the GPU on the reference's trajectory.
 __device__ __forceinline__ void givens(double a, double b, double& c, double& s) {
-  const int ea = (__double2hiint(a) >> 20) & 0x7ff, eb = (__double2hiint(b) >> 20) & 0x7ff;
-  const int em = max(ea, eb);
-  if (em >= 600 && em <= 1500) {
-    const double r = rsqrt(fma(a, a, b * b));
-    c = a * r;
-    s = b * r;
-  } else if (a == 0.0 && b == 0.0) {
+  const double nm = hypot(a, b);
+  if (nm == 0.0) {
     c = 1.0;
     s = 0.0;
-  } else {
-    const double nm = hypot(a, b);
-    c = a / nm;
-    s = b / nm;
+    return;
   }
+  c = __ddiv_rn(a, nm);
+  s = __ddiv_rn(b, nm);
 }
 
 // reducetozero (skeweigen.jl:11-47) for odd sizes; n = N-1 (even), G unused for values.
@@ -46,29 +43,29 @@ __device__ void reducetozero_dev(double* ev, int n) {
   if (n > 2) {
     const double a = ev[n - 3], b = ev[n - 2], g = ev[n - 1];
     givens(-b, g, c, s);
-    ev[n - 3] *= c;
-    ev[n - 2] = c * b - s * g;
+    ev[n - 3] = __dmul_rn(ev[n - 3], c);
+    ev[n - 2] = __dsub_rn(__dmul_rn(c, b), __dmul_rn(s, g));
     ev[n - 1] = 0.0;
-    bulge = -s * a;
+    bulge = __dmul_rn(neg(s), a);
     for (int i = n - 2; i >= 4; i -= 2) {
       const double a2 = ev[i - 3], b2 = ev[i - 2];
       givens(-b2, bulge, c, s);
-      ev[i - 3] *= c;
-      ev[i - 2] = c * b2 - s * bulge;
-      bulge = -s * a2;
+      ev[i - 3] = __dmul_rn(ev[i - 3], c);
+      ev[i - 2] = __dsub_rn(__dmul_rn(c, b2), __dmul_rn(s, bulge));
+      bulge = __dmul_rn(neg(s), a2);
     }
   }
   const double b = (n == 2 ? ev[1] : bulge);
   const double a = ev[0];
   givens(-a, b, c, s);
-  ev[0] = c * a - s * b;
-  if (n == 2) ev[1] = s * a + b * c;
+  ev[0] = __dsub_rn(__dmul_rn(c, a), __dmul_rn(s, b));
+  if (n == 2) ev[1] = __dadd_rn(__dmul_rn(s, a), __dmul_rn(b, c));
 }
 
 // implicitstep_novec (skeweigen.jl:73-103); n = active size - 1, start 1-based.
 __device__ int implicitstep_dev(double* ev, int n, int start) {
   double bulge = 0.0;
-  const double shift = ev[n - 1] * ev[n - 1];
+  const double shift = __dmul_rn(ev[n - 1], ev[n - 1]);
   const double tol = 2.220446049250313e-16;  // eps(Float64)
   for (int i = start; i <= n - 1; i++) {
     const double a = (i > start ? ev[i - 2] : 0.0);
@@ -78,17 +75,17 @@ __device__ int implicitstep_dev(double* ev, int n, int start) {
     if (i > start) {
       givens(a, bulge, c, s);
     } else {
-      const double x1 = fma(-a, a, fma(-b, b, shift));
-      const double x2 = fma(-a, bulge, b * g);
+      const double x1 = __dadd_rn(__dsub_rn(neg(__dmul_rn(a, a)), __dmul_rn(b, b)), shift);
+      const double x2 = __dadd_rn(neg(__dmul_rn(a, bulge)), __dmul_rn(b, g));
       givens(x1, x2, c, s);
     }
-    if (i > 1) ev[i - 2] = fma(c, a, s * bulge);
-    ev[i - 1] = fma(c, b, -(s * g));
-    ev[i] = fma(s, b, c * g);
+    if (i > 1) ev[i - 2] = __dadd_rn(__dmul_rn(c, a), __dmul_rn(s, bulge));
+    ev[i - 1] = __dsub_rn(__dmul_rn(c, b), __dmul_rn(s, g));
+    ev[i] = __dadd_rn(__dmul_rn(s, b), __dmul_rn(c, g));
     if (i < n - 1) {
       const double z = ev[i + 1];
-      ev[i + 1] = z * c;
-      bulge = s * z;
+      ev[i + 1] = __dmul_rn(z, c);
+      bulge = __dmul_rn(s, z);
       if (fabs(bulge) < tol && fabs(ev[i - 1]) < tol) return i + 1;
     }
   }

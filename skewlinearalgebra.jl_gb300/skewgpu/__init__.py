@@ -38,7 +38,7 @@ from ._lib import SkewError, check
 __all__ = [
     "SkewHermitian", "Hessenberg", "BatchPlan", "SkewError", "to_device", "from_device", "hessenberg",
     "logabspfaffian", "logabspfaffian_", "pfaffian", "eigvals", "logabspfaffian_rrule", "handle",
-    "measure_fp64_peak",
+    "measure_fp64_peak", "eigen", "exp", "cis", "exp_rrule",
 ]
 
 _lib.load()  # fail loudly at import if the CUDA library is missing
@@ -219,6 +219,72 @@ def eigvals(A) -> np.ndarray:
     return 1j * vals.cpu().numpy()
 
 
+def _info_ok(info: torch.Tensor, where: str) -> int:
+    st = int(info.item())
+    if st == _lib.SKEW_NO_CONVERGENCE:
+        raise RuntimeError("Maximum number of iterations reached, the algorithm didn't converge")
+    return st
+
+
+def eigen(A):
+    """eigen(A::SkewHermitian{Float64}) (eigen.jl:338-360): (values, vectors) as numpy
+    complex arrays; values in the reference's order, vectors = Vr + i Vi."""
+    S = _as_skew(A).copy()
+    n = S.n
+    vals = torch.zeros(n, dtype=torch.float64, device="cuda")
+    Vr = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    Vi = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_eigen_d(h, _ptr(S.data), n, n, _ptr(vals), _ptr(Vr), _ptr(Vi), n, _ptr(info)), "eigen")
+    _info_ok(info, "eigen")
+    return 1j * vals.cpu().numpy(), from_device(Vr) + 1j * from_device(Vi)
+
+
+def exp(A) -> np.ndarray:
+    """exp(A::SkewHermitian{Float64}) (exp.jl:3-35, :48), real n x n."""
+    S = _as_skew(A).copy()
+    n = S.n
+    E = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_exp_d(h, _ptr(S.data), n, n, _ptr(E), n, _ptr(info)), "exp")
+    _info_ok(info, "exp")
+    return from_device(E)
+
+
+def cis(A) -> np.ndarray:
+    """cis(A::SkewHermitian{Float64}) = exp(iA) (exp.jl:99-110, :204), complex Hermitian."""
+    S = _as_skew(A).copy()
+    n = S.n
+    C = torch.zeros((n, n, 2), dtype=torch.float64, device="cuda")  # column-major complex: C[j, i, :]
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_cis_d(h, _ptr(S.data), n, n, _ptr(C), n, _ptr(info)), "cis")
+    _info_ok(info, "cis")
+    c = C.cpu().numpy()
+    return (c[..., 0] + 1j * c[..., 1]).T.copy()
+
+
+def exp_rrule(A):
+    """Forward exp(A) and a pullback Cbar -> d<Cbar, exp(A)>/dA (Daleckii-Krein)."""
+    Anp = _as_skew(A).numpy()
+    E = exp(Anp)
+
+    def pullback(Cbar) -> np.ndarray:
+        S = SkewHermitian(Anp)
+        n = S.n
+        Cd = to_device(np.asarray(Cbar, dtype=np.float64))
+        G = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        info = _info_tensor()
+        h = handle().bind()
+        check(_lib.load().skew_exp_vjp_d(h, _ptr(S.data), n, n, _ptr(Cd), _ptr(G), n, _ptr(info)), "exp_vjp")
+        _info_ok(info, "exp_vjp")
+        return from_device(G)
+
+    return E, pullback
+
+
 def measure_fp64_peak() -> float:
     t = ctypes.c_double()
     check(_lib.load().skew_measure_fp64_peak(handle().bind(), ctypes.byref(t)), "measure_fp64_peak")
@@ -268,6 +334,32 @@ class BatchPlan:
         check(_lib.load().skew_batch_logabspf_d(self.plan, _ptr(A_ptrs), _ptr(logpf), _ptr(sign), _ptr(grad_ptrs),
                                                 _ptr(status)), "skew_batch_logabspf_d")
         return logpf, sign, status
+
+    def eigen(self, A_ptrs, val_ptrs, vr_ptrs, vi_ptrs, status=None):
+        status = torch.empty(self.count, dtype=torch.int32, device="cuda") if status is None else status
+        self._h.bind()
+        check(_lib.load().skew_batch_eigen_d(self.plan, _ptr(A_ptrs), _ptr(val_ptrs), _ptr(vr_ptrs), _ptr(vi_ptrs),
+                                             _ptr(status)), "skew_batch_eigen_d")
+        return status
+
+    def exp(self, A_ptrs, out_ptrs, status=None):
+        status = torch.empty(self.count, dtype=torch.int32, device="cuda") if status is None else status
+        self._h.bind()
+        check(_lib.load().skew_batch_exp_d(self.plan, _ptr(A_ptrs), _ptr(out_ptrs), _ptr(status)), "skew_batch_exp_d")
+        return status
+
+    def cis(self, A_ptrs, out_ptrs, status=None):
+        status = torch.empty(self.count, dtype=torch.int32, device="cuda") if status is None else status
+        self._h.bind()
+        check(_lib.load().skew_batch_cis_d(self.plan, _ptr(A_ptrs), _ptr(out_ptrs), _ptr(status)), "skew_batch_cis_d")
+        return status
+
+    def exp_vjp(self, A_ptrs, cot_ptrs, out_ptrs, status=None):
+        status = torch.empty(self.count, dtype=torch.int32, device="cuda") if status is None else status
+        self._h.bind()
+        check(_lib.load().skew_batch_exp_vjp_d(self.plan, _ptr(A_ptrs), _ptr(cot_ptrs), _ptr(out_ptrs), _ptr(status)),
+              "skew_batch_exp_vjp_d")
+        return status
 
     def eigvals(self, A_ptrs: torch.Tensor, val_ptrs: torch.Tensor, status: Optional[torch.Tensor] = None):
         status = torch.empty(self.count, dtype=torch.int32, device="cuda") if status is None else status

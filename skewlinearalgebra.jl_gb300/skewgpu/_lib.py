@@ -45,6 +45,11 @@ SIGNATURES = {
     "skew_batch_plan_destroy": (_int, [_vp]),
     "skew_batch_logabspf_d": (_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "skew_batch_eigvals_d": (_int, [_vp, _vp, _vp, _vp]),
+    "skew_batch_eigen_d": (_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "skew_batch_exp_d": (_int, [_vp, _vp, _vp, _vp]),
+    "skew_batch_cis_d": (_int, [_vp, _vp, _vp, _vp]),
+    "skew_batch_exp_vjp_d": (_int, [_vp, _vp, _vp, _vp, _vp]),
+    "skew_exp_vjp_d": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _i64, _vp]),
     "skew_measure_fp64_peak": (_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
 }
 
