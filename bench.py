@@ -171,9 +171,29 @@ def main():
     ap.add_argument("--nmax", type=int, default=NMAX)
     ap.add_argument("--large-n", type=int, default=8192, help="single-matrix hessenberg leg (0 = skip)")
     ap.add_argument("--only-large", action="store_true", help="run only the single-matrix hessenberg leg")
+    ap.add_argument("--no-legs", action="store_true", help="skip the eigvals / n=512 / adjoint legs")
+    ap.add_argument("--only-legs", action="store_true", help="run only the eigvals / n=512 / adjoint legs")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.only_legs:
+        import torch
+
+        import skewgpu
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        peak = skewgpu.measure_fp64_peak()
+        sizes = workload_sizes(args.count, nmin=args.nmin, nmax=args.nmax)
+        buf, offs = packed_inputs(sizes)
+        d_in = torch.from_numpy(buf).to("cuda")
+        plan = skewgpu.BatchPlan(sizes)
+        out = {"eigvals_batched": leg_eigvals_batched(plan, d_in, offs, sizes, max(1, args.steps)),
+               "plain_n512": leg_plain_n512(peak, cpu=not args.no_cpu),
+               "pfaffian_adjoint_1024x128": leg_pfaffian_adjoint(peak, max(1, args.steps)),
+               "exp_adjoint_512_mixed": leg_exp_adjoint(peak, max(1, min(args.steps, 3)))}
+        plan.close()
+        print(json.dumps({"legs": out}), flush=True)
+        return 0
     if args.only_large:
         import torch
 
@@ -186,17 +206,11 @@ def main():
 
     import torch
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
     import skewgpu
+    from skewgpu import replicas
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    world, rank, local, dist = replicas.init_from_env("nccl")
 
     count = args.count
     sizes = workload_sizes(count, rank=rank, nmin=args.nmin, nmax=args.nmax)
@@ -240,12 +254,8 @@ def main():
     barrier()
     wall = time.perf_counter() - t0
     ms_dev = ev0.elapsed_time(ev1)
-    sec = ms_dev / 1e3
-    if dist is not None:
-        t = torch.tensor([sec], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        sec = float(t.item())
-    value = world * count * args.steps / sec
+    sec = replicas.max_over_ranks(ms_dev / 1e3, dist, "cuda")
+    value = replicas.weak_scaling_throughput(count, world, args.steps, sec)
 
     # e2e through the public API: pinned host in -> device, results -> pinned host
     h_lp = torch.empty(count, dtype=torch.float64).pin_memory()
@@ -264,12 +274,8 @@ def main():
     e1.record(stream)
     barrier()
     clk = clocks.stop()
-    e2e_sec = e0.elapsed_time(e1) / 1e3
-    if dist is not None:
-        t = torch.tensor([e2e_sec], device="cuda", dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_sec = float(t.item())
-    e2e_value = world * count * e2e_steps / e2e_sec
+    e2e_sec = replicas.max_over_ranks(e0.elapsed_time(e1) / 1e3, dist, "cuda")
+    e2e_value = replicas.weak_scaling_throughput(count, world, e2e_steps, e2e_sec)
 
     # roofline of the dominant kernel (batch_pf_kernel: every launch of a step)
     flops = float(flops_per_matrix(sizes).sum())
@@ -355,6 +361,12 @@ def main():
     large = None
     if rank == 0 and args.large_n > 0:
         large = bench_hessenberg_large(args.large_n, 2, fp64_peak)
+    legs = {}
+    if rank == 0 and not args.no_legs:
+        legs["eigvals_batched"] = leg_eigvals_batched(plan, d_in, offs, sizes, args.steps)
+        legs["plain_n512"] = leg_plain_n512(fp64_peak, cpu=not args.no_cpu)
+        legs["pfaffian_adjoint_1024x128"] = leg_pfaffian_adjoint(fp64_peak, args.steps)
+        legs["exp_adjoint_512_mixed"] = leg_exp_adjoint(fp64_peak, max(1, min(args.steps, 3)))
 
     if rank == 0:
         line = {
@@ -383,6 +395,8 @@ def main():
             line["plain_gpu"] = plain
         if large:
             line[f"hessenberg_n{args.large_n}"] = large
+        if legs:
+            line["legs"] = legs
         print(json.dumps(line), flush=True)
     plan.close()
     if dist is not None:
@@ -431,6 +445,219 @@ def bench_hessenberg_large(n, reps, fp64_peak):
     fro_rel = abs(np.sqrt(2.0 * np.sum(e * e)) - np.linalg.norm(A)) / np.linalg.norm(A)
     return {"n": n, "ms": sec * 1e3, "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
             "algorithmic_flops": flops, "reps": reps, "check_frobenius_rel": float(fro_rel)}
+
+
+def _time_events(fn, reps, stream):
+    """Median device time (s) of fn() over reps calls, each bracketed by CUDA events."""
+    import torch
+
+    times = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    return float(np.median(times))
+
+
+def leg_eigvals_batched(plan, d_in, offs, sizes, steps):
+    """The batched workload's eigvals (hessenberg + skewtrieigvals! per matrix,
+    reference order) through skew_batch_eigvals_d; the inputs stay unmodified."""
+    import torch
+
+    count = len(sizes)
+    base = d_in.data_ptr()
+    a_ptrs = torch.tensor((base + 8 * offs).tolist(), dtype=torch.int64, device="cuda")
+    voff = np.zeros(count, dtype=np.int64)
+    voff[1:] = np.cumsum(sizes[:-1])
+    vals = torch.empty(int(sizes.sum()), dtype=torch.float64, device="cuda")
+    v_ptrs = torch.tensor((vals.data_ptr() + 8 * voff).tolist(), dtype=torch.int64, device="cuda")
+    st = torch.empty(count, dtype=torch.int32, device="cuda")
+    for _ in range(3):
+        plan.eigvals(a_ptrs, v_ptrs, st)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        plan.eigvals(a_ptrs, v_ptrs, st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / steps
+    s = st.cpu().numpy()
+    return {"value": count / sec, "unit": "matrices/s", "ms_per_step": sec * 1e3, "steps": steps,
+            "status_ok": int((s == 0).sum()), "status_fallback": int((s == 8).sum())}
+
+
+def leg_plain_n512(fp64_peak, reps=5, cpu=True):
+    """One real n=512 matrix, A = (B - B^T)/2 with B iid N(0,1): hessenberg,
+    eigvals and logabspfaffian through the single-matrix C-ABI calls (median of
+    reps, input restored outside the timed region), next to the oracle's FP64
+    restatement of the reference on one host core."""
+    import ctypes
+
+    import torch
+
+    import skewgpu
+
+    n = 512
+    rng = np.random.default_rng(SEED + 512)
+    B = rng.standard_normal((n, n))
+    A = (B - B.T) / 2
+    pristine = skewgpu.to_device(A)
+    work = torch.empty_like(pristine)
+    tau = torch.empty(n - 1, dtype=torch.float64, device="cuda")
+    ev = torch.empty(n - 1, dtype=torch.float64, device="cuda")
+    vals = torch.empty(n, dtype=torch.float64, device="cuda")
+    out2 = torch.empty(2, dtype=torch.float64, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    L = skewgpu._lib.load()
+    h = skewgpu.handle().bind()
+    stream = torch.cuda.current_stream()
+    P = lambda t, off=0: ctypes.c_void_p(t.data_ptr() + off)  # noqa: E731
+    calls = {
+        "hessenberg": lambda: L.skew_hessenberg_d(h, P(work), n, n, P(tau), P(ev), P(info)),
+        "eigvals": lambda: L.skew_eigvals_d(h, P(work), n, n, P(vals), P(info)),
+        "logabspfaffian": lambda: L.skew_logabspf_d(h, P(work), n, n, P(out2), P(out2, 8), 0, P(info)),
+    }
+    res = {"n": n}
+    for name, fn in calls.items():
+        times = []
+        for r in range(reps + 1):
+            work.copy_(pristine)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            assert fn() == 0
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r:
+                times.append(e0.elapsed_time(e1))
+        res[f"{name}_ms"] = float(np.median(times))
+    res["hessenberg_gflops"] = 4.0 / 3.0 * n ** 3 / (res["hessenberg_ms"] / 1e3) / 1e9
+    if cpu:
+        from oracle import oracle as O
+
+        t0 = time.perf_counter()
+        O.hessenberg(A)
+        t1 = time.perf_counter()
+        cv, _ = O.eigvals(A)
+        t2 = time.perf_counter()
+        clp, csg = O.logabspfaffian(A)
+        t3 = time.perf_counter()
+        res["cpu_port_ms"] = {"hessenberg": (t1 - t0) * 1e3, "eigvals": (t2 - t1) * 1e3,
+                              "logabspfaffian": (t3 - t2) * 1e3, "cores": 1}
+        g = out2.cpu().numpy()
+        gv = vals.cpu().numpy()
+        res["check"] = {"logpf_rel_vs_cpu": float(abs(g[0] - clp) / abs(clp)), "sign_equal": bool(g[1] == csg),
+                        "eigvals_rel_vs_cpu": float(np.abs(np.sort(gv) - np.sort(cv)).max() / np.abs(cv).max())}
+    return res
+
+
+def leg_pfaffian_adjoint(fp64_peak, steps, count=1024, n=128):
+    """1024 real n=128 matrices (B - B^T)/2 + 0.5 J, B iid N(0,1/n); loss
+    sum_i w_i log|Pf(A_i)| with w ~ U(-1,1); forward + gradient per step through
+    skew_batch_logabspf_d, gradient scaled by w on the device."""
+    import torch
+
+    import skewgpu
+
+    rng = np.random.default_rng(SEED + 128)
+    J = np.kron(np.eye(n // 2), np.array([[0.0, 1.0], [-1.0, 0.0]]))
+    buf = np.empty(count * n * n)
+    for b in range(count):
+        B = rng.standard_normal((n, n)) / np.sqrt(n)
+        buf[b * n * n:(b + 1) * n * n] = ((B - B.T) / 2 + 0.5 * J).ravel(order="F")
+    w = torch.from_numpy(rng.uniform(-1.0, 1.0, count)).to("cuda")
+    d_in = torch.from_numpy(buf).to("cuda")
+    d_g = torch.empty_like(d_in)
+    offs = np.arange(count, dtype=np.int64) * n * n
+    a_ptrs = torch.tensor((d_in.data_ptr() + 8 * offs).tolist(), dtype=torch.int64, device="cuda")
+    g_ptrs = torch.tensor((d_g.data_ptr() + 8 * offs).tolist(), dtype=torch.int64, device="cuda")
+    plan = skewgpu.BatchPlan([n] * count)
+    lp = torch.empty(count, dtype=torch.float64, device="cuda")
+    sg = torch.empty_like(lp)
+    st = torch.empty(count, dtype=torch.int32, device="cuda")
+    gv = d_g.view(count, n * n)
+
+    def step():
+        plan.logabspfaffian(a_ptrs, g_ptrs, lp, sg, st)
+        gv.mul_(w[:, None])
+        return torch.dot(w, lp)
+
+    for _ in range(3):
+        step()
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        loss = step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / steps
+    flops = count * float(flops_per_matrix(n))
+    plan.close()
+    return {"value": count / sec, "unit": "matrices/s", "ms_per_step": sec * 1e3, "steps": steps,
+            "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak, "loss": float(loss.item()),
+            "status_ok": int((st.cpu().numpy() == 0).sum())}
+
+
+def exp_adjoint_flops(n):
+    """Algorithmic FP64 work of one exp adjoint as computed: Householder reduction
+    4/3 n^3, back-transformation of Vr and Vi 4 n^3, and the twelve real n x n
+    products of the Daleckii-Krein assembly 24 n^3 (the QR chain is O(n^2))."""
+    n = np.asarray(n, dtype=np.float64)
+    return (4.0 / 3.0 + 4.0 + 24.0) * n ** 3
+
+
+def leg_exp_adjoint(fp64_peak, steps, count=512):
+    """512 real matrices, n uniform in {32, 64, ..., 512}, each scaled to a spectral
+    radius ~ U(0.5, 8); cotangents C_i iid N(0,1); G_i = d<C_i, exp(A_i)>/dA_i
+    through skew_batch_exp_vjp_d."""
+    import torch
+
+    import skewgpu
+
+    rng = np.random.default_rng(SEED + 5)
+    sizes = (32 * rng.integers(1, 17, count)).astype(np.int64)
+    offs = np.zeros(count, dtype=np.int64)
+    offs[1:] = np.cumsum(sizes[:-1] ** 2)
+    total = int(offs[-1] + sizes[-1] ** 2)
+    buf = np.empty(total)
+    cot = rng.standard_normal(total)
+    for b, n in enumerate(sizes):
+        B = rng.standard_normal((n, n))
+        A = (B - B.T) / 2
+        rho = np.abs(np.linalg.eigvalsh(1j * A)).max()
+        A *= rng.uniform(0.5, 8.0) / rho
+        buf[offs[b]:offs[b] + n * n] = A.ravel(order="F")
+    d_in = torch.from_numpy(buf).to("cuda")
+    d_c = torch.from_numpy(cot).to("cuda")
+    d_g = torch.empty_like(d_in)
+    ptr = lambda t: torch.tensor((t.data_ptr() + 8 * offs).tolist(), dtype=torch.int64, device="cuda")  # noqa: E731
+    a_ptrs, c_ptrs, g_ptrs = ptr(d_in), ptr(d_c), ptr(d_g)
+    plan = skewgpu.BatchPlan(sizes)
+    st = torch.empty(count, dtype=torch.int32, device="cuda")
+    plan.exp_vjp(a_ptrs, c_ptrs, g_ptrs, st)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        plan.exp_vjp(a_ptrs, c_ptrs, g_ptrs, st)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / steps
+    flops = float(exp_adjoint_flops(sizes).sum())
+    s = st.cpu().numpy()
+    plan.close()
+    return {"value": count / sec, "unit": "matrices/s", "ms_per_step": sec * 1e3, "steps": steps,
+            "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
+            "status_ok": int((s == 0).sum()), "status_fallback": int((s == 8).sum()),
+            "complex_part": "the 64 ComplexF64 n=256 matrices of this workload are not built (complex eigen)"}
 
 
 def _bucket_ids(sizes):

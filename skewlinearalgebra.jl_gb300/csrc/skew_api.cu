@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -68,6 +69,16 @@ struct skew_batch_plan_st {
   double** e_p_scratch = nullptr;  // 8 x count: single-call pointer arrays
   int* e_status = nullptr;
   unsigned* e_counter = nullptr;
+  // one instantiated CUDA graph per batched operation, keyed on its arguments
+  struct GraphSlot {
+    bool valid = false;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t stream = nullptr;
+    std::array<const void*, 6> key{};
+  };
+  GraphSlot graphs[6];
+  bool graphs_off = false;              // capture failed once (or disabled): launch directly
+  cudaStream_t capture_stream = nullptr;  // graphs are recorded here, launched on the caller's stream
 };
 
 #define CK(x)                                  \
@@ -351,6 +362,9 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
 
 int skew_batch_plan_destroy(skew_batch_plan_t P) {
   if (!P) return SKEW_BAD_ARG;
+  for (auto& g : P->graphs)
+    if (g.valid) cudaGraphExecDestroy(g.exec);
+  if (P->capture_stream) cudaStreamDestroy(P->capture_stream);
   cudaStream_t st = P->h ? P->h->stream : nullptr;
   if (P->d_n) cudaFreeAsync(P->d_n, st);
   if (P->d_order) cudaFreeAsync(P->d_order, st);
@@ -400,29 +414,107 @@ static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logp
   return SKEW_OK;
 }
 
+}  // extern "C"
+
+// Batched operations run as CUDA graphs: the first call with a given set of
+// argument pointers records the plan's launch sequence on a plan-owned stream
+// (the legacy default stream cannot be captured) and instantiates it; every
+// call then launches the graph on the handle's stream.  Kernels read the
+// per-matrix pointer arrays at run time, so new contents behind the same arrays
+// need no re-capture.  A stream that the caller is already capturing,
+// SKEW_BATCH_GRAPH=0, or a capture that fails falls back to plain launches of
+// the same kernels on the handle's stream.
+enum GraphOp { G_LOGPF = 0, G_EIGVALS, G_EIGEN, G_EXP, G_CIS, G_EXPVJP };
+
+static bool graphs_enabled() {
+  static const bool on = [] {
+    const char* e = std::getenv("SKEW_BATCH_GRAPH");
+    return !(e && e[0] == '0');
+  }();
+  return on;
+}
+
+template <class Issue>
+static int graph_issue(skew_batch_plan_t P, GraphOp op, const std::array<const void*, 6>& key, Issue&& issue) {
+  cudaStream_t user = P->h->stream;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (P->graphs_off || !graphs_enabled() || cudaStreamIsCapturing(user, &cs) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusNone) {
+    (void)cudaGetLastError();
+    return issue();
+  }
+  auto& g = P->graphs[op];
+  if (g.valid && g.key == key) {
+    CK(cudaGraphLaunch(g.exec, user));
+    return SKEW_OK;
+  }
+  if (g.valid) {
+    cudaGraphExecDestroy(g.exec);
+    g.valid = false;
+    g.exec = nullptr;
+  }
+  if (!P->capture_stream && cudaStreamCreateWithFlags(&P->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    (void)cudaGetLastError();
+    P->capture_stream = nullptr;
+    P->graphs_off = true;
+    return issue();
+  }
+  if (cudaStreamBeginCapture(P->capture_stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    (void)cudaGetLastError();
+    P->graphs_off = true;
+    return issue();
+  }
+  P->h->stream = P->capture_stream;  // issue() launches on the handle's stream
+  const int s = issue();
+  P->h->stream = user;
+  cudaGraph_t graph = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(P->capture_stream, &graph);
+  cudaGraphExec_t exec = nullptr;
+  const bool ok = s == SKEW_OK && ec == cudaSuccess && graph &&
+                  cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess;
+  if (graph) cudaGraphDestroy(graph);
+  if (!ok) {
+    (void)cudaGetLastError();
+    if (exec) cudaGraphExecDestroy(exec);
+    P->graphs_off = true;
+    return issue();
+  }
+  g.valid = true;
+  g.exec = exec;
+  g.stream = user;
+  g.key = key;
+  CK(cudaGraphLaunch(exec, user));
+  return SKEW_OK;
+}
+
+extern "C" {
+
 int skew_batch_logabspf_d(skew_batch_plan_t P, const double* const* A, double* logpf, double* sign,
                           double* const* grad, int* status) {
   if (!P || (P->count > 0 && (!A || !logpf || !sign || !status))) return SKEW_BAD_ARG;
   if (P->count == 0) return SKEW_OK;
-  return run_buckets(P, A, logpf, sign, grad, status, false);
+  return graph_issue(P, G_LOGPF, {A, logpf, sign, grad, status, nullptr},
+                     [&] { return run_buckets(P, A, logpf, sign, grad, status, false); });
 }
 
 int skew_batch_eigvals_d(skew_batch_plan_t P, const double* const* A, double* const* vals_im, int* status) {
   if (!P || (P->count > 0 && (!A || !vals_im))) return SKEW_BAD_ARG;
   if (P->count == 0) return SKEW_OK;
-  int s = run_buckets(P, A, nullptr, nullptr, nullptr, nullptr, true);
-  if (s) return s;
-  TrieigParams tp;
-  tp.ev_all = P->d_ev;
-  tp.ev_off = P->d_ev_off;
-  tp.n = P->d_n;
-  tp.order = P->d_order;
-  tp.count = (int32_t)P->count;
-  tp.evwork = P->d_ev;
-  tp.vals = vals_im;
-  tp.status = status;
-  CK(launch_batch_trieig(tp, P->h->stream));
-  return SKEW_OK;
+  return graph_issue(P, G_EIGVALS, {A, vals_im, status, nullptr, nullptr, nullptr}, [&]() -> int {
+    int s = run_buckets(P, A, nullptr, nullptr, nullptr, nullptr, true);
+    if (s) return s;
+    TrieigParams tp;
+    tp.ev_all = P->d_ev;
+    tp.ev_off = P->d_ev_off;
+    tp.n = P->d_n;
+    tp.order = P->d_order;
+    tp.count = (int32_t)P->count;
+    tp.evwork = P->d_ev;
+    tp.vals = vals_im;
+    tp.status = status;
+    CK(launch_batch_trieig(tp, P->h->stream));
+    return SKEW_OK;
+  });
 }
 
 // ---------------------------------------------------------------------------
@@ -561,14 +653,36 @@ int skew_batch_eigen_d(skew_batch_plan_t P, const double* const* A, double* cons
                        double* const* Vi, int* status) {
   if (!P || (P->count > 0 && (!A || !vals_im || !Vr || !Vi))) return SKEW_BAD_ARG;
   if (P->count == 0) return SKEW_OK;
-  EigenBatch E;
-  int s = eigen_run(P, A, vals_im, Vr, Vi, &E);
+  int s = eigen_ws(P);
   if (s) return s;
-  return finish_status(P, status);
+  return graph_issue(P, G_EIGEN, {A, vals_im, Vr, Vi, status, nullptr}, [&]() -> int {
+    EigenBatch E;
+    int s2 = eigen_run(P, A, vals_im, Vr, Vi, &E);
+    if (s2) return s2;
+    return finish_status(P, status);
+  });
+}
+
+static int func_issue(skew_batch_plan_t P, const double* const* A, double* const* out, const double* const* cot,
+                      int mode, int* status);
+
+// exp / cis / exp adjoint as one graph per mode (batched entry points).
+static int func_run_graph(skew_batch_plan_t P, const double* const* A, double* const* out,
+                          const double* const* cot, int mode, int* status) {
+  int s = eigen_ws(P);
+  if (s) return s;
+  const GraphOp op = mode == 0 ? G_EXP : (mode == 1 ? G_CIS : G_EXPVJP);
+  return graph_issue(P, op, {A, out, cot, status, nullptr, nullptr},
+                     [&] { return func_issue(P, A, out, cot, mode, status); });
 }
 
 static int func_run(skew_batch_plan_t P, const double* const* A, double* const* out, const double* const* cot,
                     int mode, int* status) {
+  return func_issue(P, A, out, cot, mode, status);
+}
+
+static int func_issue(skew_batch_plan_t P, const double* const* A, double* const* out, const double* const* cot,
+                      int mode, int* status) {
   EigenBatch E;
   int s = eigen_run(P, A, nullptr, nullptr, nullptr, &E);
   if (s) return s;
@@ -582,20 +696,20 @@ static int func_run(skew_batch_plan_t P, const double* const* A, double* const* 
 int skew_batch_exp_d(skew_batch_plan_t P, const double* const* A, double* const* E, int* status) {
   if (!P || (P->count > 0 && (!A || !E))) return SKEW_BAD_ARG;
   if (P->count == 0) return SKEW_OK;
-  return func_run(P, A, E, nullptr, 0, status);
+  return func_run_graph(P, A, E, nullptr, 0, status);
 }
 
 int skew_batch_cis_d(skew_batch_plan_t P, const double* const* A, double* const* C, int* status) {
   if (!P || (P->count > 0 && (!A || !C))) return SKEW_BAD_ARG;
   if (P->count == 0) return SKEW_OK;
-  return func_run(P, A, C, nullptr, 1, status);
+  return func_run_graph(P, A, C, nullptr, 1, status);
 }
 
 int skew_batch_exp_vjp_d(skew_batch_plan_t P, const double* const* A, const double* const* Cbar, double* const* G,
                          int* status) {
   if (!P || (P->count > 0 && (!A || !Cbar || !G))) return SKEW_BAD_ARG;
   if (P->count == 0) return SKEW_OK;
-  return func_run(P, A, G, Cbar, 2, status);
+  return func_run_graph(P, A, G, Cbar, 2, status);
 }
 
 // Single matrices run as a batch of one through a plan cached on the handle.

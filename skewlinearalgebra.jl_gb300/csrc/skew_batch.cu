@@ -781,9 +781,14 @@ size_t batch_smem_bytes(int nmax, bool smem_matrix) {
   return b;
 }
 
+// Per-instantiation record of the devices on which the shared-memory limit of
+// batch_kernel<NT, SM> has been raised (shared by the launch and the occupancy query).
+template <int NT, bool SM>
+std::atomic<uint64_t> g_smem_raised{0};
+
 template <int NT, bool SM>
 static cudaError_t launch_t(const BatchParams& P, int grid, size_t smem, cudaStream_t st, int tridiag_only) {
-  cudaError_t e = cudaFuncSetAttribute(batch_kernel<NT, SM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit_once((const void*)batch_kernel<NT, SM>, g_smem_raised<NT, SM>);
   if (e != cudaSuccess) return e;
   batch_kernel<NT, SM><<<grid, NT, smem, st>>>(P, tridiag_only);
   return cudaGetLastError();
@@ -814,7 +819,7 @@ int batch_threads() { return NT_LARGE; }
 template <int NT, bool SM>
 static int occ_t(size_t smem) {
   int occ = 0;
-  cudaError_t e = cudaFuncSetAttribute(batch_kernel<NT, SM>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = raise_smem_limit_once((const void*)batch_kernel<NT, SM>, g_smem_raised<NT, SM>);
   if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<NT, SM>, NT, smem);
   if (e != cudaSuccess || occ < 1) {
     cudaGetLastError();

@@ -794,7 +794,8 @@ cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStrea
   cudaError_t e = cudaMemsetAsync(E.counter, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
   const size_t smem = sizeof(double) * (size_t)EB * 3 * (size_t)nmax;
-  e = cudaFuncSetAttribute(eigen_back_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  static std::atomic<uint64_t> raised{0};
+  e = raise_smem_limit_once((const void*)eigen_back_kernel, raised);
   if (e != cudaSuccess) return e;
   eigen_back_kernel<<<grid, ENT, smem, st>>>(E);
   return cudaGetLastError();

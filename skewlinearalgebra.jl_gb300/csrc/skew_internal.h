@@ -3,7 +3,33 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 namespace skew {
+
+// Raises a kernel's dynamic shared-memory limit to the most the device allows
+// beside the kernel's static shared memory (opt-in maximum minus static bytes),
+// once per device (bit `device` of `done`), so that later launches, which may be
+// recorded into a CUDA graph, issue no attribute calls.
+inline cudaError_t raise_smem_limit_once(const void* kernel, std::atomic<uint64_t>& done) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const uint64_t bit = 1ull << (dev & 63);
+  if (done.load(std::memory_order_acquire) & bit) return cudaSuccess;
+  int optin = 0;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  cudaFuncAttributes fa;
+  e = cudaFuncGetAttributes(&fa, kernel);
+  if (e != cudaSuccess) return e;
+  const int dyn = optin - (int)fa.sharedSizeBytes;
+  if (dyn <= 0) return cudaErrorInvalidValue;
+  e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+  if (e != cudaSuccess) return e;
+  done.fetch_or(bit, std::memory_order_release);
+  return cudaSuccess;
+}
 
 // Batched one-CTA-per-matrix launches (skew_batch.cu).
 struct BatchParams {
