@@ -200,8 +200,11 @@ def main():
         import skewgpu
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps({"hessenberg": bench_hessenberg_large(args.large_n, max(1, args.steps),
-                                                               skewgpu.measure_fp64_peak())}), flush=True)
+        peak = skewgpu.measure_fp64_peak()
+        out = {"hessenberg": bench_hessenberg_large(args.large_n, max(1, args.steps), peak)}
+        if not args.no_legs:
+            out["eigen"] = leg_eigen_large(args.large_n, peak)
+        print(json.dumps(out), flush=True)
         return 0
 
     import torch
@@ -359,8 +362,10 @@ def main():
                  "max_rel_grad_vs_cpu": gerr, "matrices": k, "status_nonzero": int((st != 0).sum())}
 
     large = None
+    eig_large = None
     if rank == 0 and args.large_n > 0:
         large = bench_hessenberg_large(args.large_n, 2, fp64_peak)
+        eig_large = leg_eigen_large(args.large_n, fp64_peak)
     legs = {}
     if rank == 0 and not args.no_legs:
         legs["eigvals_batched"] = leg_eigvals_batched(plan, d_in, offs, sizes, args.steps)
@@ -395,6 +400,8 @@ def main():
             line["plain_gpu"] = plain
         if large:
             line[f"hessenberg_n{args.large_n}"] = large
+        if eig_large:
+            line[f"eigen_n{args.large_n}"] = eig_large
         if legs:
             line["legs"] = legs
         print(json.dumps(line), flush=True)
@@ -445,6 +452,59 @@ def bench_hessenberg_large(n, reps, fp64_peak):
     fro_rel = abs(np.sqrt(2.0 * np.sum(e * e)) - np.linalg.norm(A)) / np.linalg.norm(A)
     return {"n": n, "ms": sec * 1e3, "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
             "algorithmic_flops": flops, "reps": reps, "check_frobenius_rel": float(fro_rel)}
+
+
+def leg_eigen_large(n, fp64_peak, reps=1):
+    """eigen with vectors of one dense n x n skew matrix (A = (B - B^T)/2, B iid
+    N(0,1)) through skew_eigen_d: blocked reduction, bisection, twisted
+    eigenvectors, blocked back-transformation; input restored outside the timed
+    region.  Checked on 16 sampled eigenpairs: residual |A v - i lambda v| and
+    orthonormality of the sample (torch FP64 on the device, outside the timing)."""
+    import ctypes
+
+    import torch
+
+    import skewgpu
+
+    rng = np.random.default_rng(SEED + n)
+    B = rng.standard_normal((n, n))
+    A = (B - B.T) / 2
+    del B
+    pristine = skewgpu.to_device(A)
+    work = torch.empty_like(pristine)
+    vals = torch.empty(n, dtype=torch.float64, device="cuda")
+    Vr = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    Vi = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    L = skewgpu._lib.load()
+    h = skewgpu.handle().bind()
+    stream = torch.cuda.current_stream()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    times = []
+    for r in range(reps + 1):
+        work.copy_(pristine)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = L.skew_eigen_d(h, P(work), n, n, P(vals), P(Vr), P(Vi), n, P(info))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        assert st == 0, st
+        if r:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    sec = float(np.median(times))
+    # device buffers hold A^T (column-major A); V columns are Vr.T[:, k] in torch terms
+    At = pristine.T
+    idx = torch.tensor(np.sort(rng.choice(n, 16, replace=False)), device="cuda")
+    Vs = torch.complex(Vr.T[:, idx], Vi.T[:, idx])
+    lam = 1j * vals[idx]
+    Ac = torch.complex(At, torch.zeros_like(At))
+    res = (Ac @ Vs - Vs * lam).abs().max().item() / vals.abs().max().item()
+    orth = (Vs.conj().T @ Vs - torch.eye(16, dtype=Vs.dtype, device="cuda")).abs().max().item()
+    flops = (4.0 / 3.0 + 2.0) * n ** 3  # reduction + back-transformation of n real columns
+    return {"n": n, "ms": sec * 1e3, "algorithmic_flops": flops, "gflops": flops / sec / 1e9,
+            "frac_fp64": flops / sec / 1e12 / fp64_peak, "reps": reps,
+            "check_sample": {"pairs": 16, "max_residual_rel": res, "max_orthonormality_err": orth}}
 
 
 def _time_events(fn, reps, stream):

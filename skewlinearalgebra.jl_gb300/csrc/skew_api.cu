@@ -42,6 +42,7 @@ struct skew_batch_plan_st {
   int32_t* d_order = nullptr;
   int64_t* d_ev_off = nullptr;
   unsigned* d_counters = nullptr;
+  unsigned* d_fallback = nullptr;  // eigvals: stagnated matrices for the fallback kernel
   double* d_ev = nullptr;
   double* d_gws = nullptr;
   int64_t ev_total = 0;
@@ -342,6 +343,8 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
   ok &= cudaMallocAsync(&P->d_counters, sizeof(unsigned) * std::max<size_t>(P->buckets.size(), 1), st) ==
         cudaSuccess;
   ok &= cudaMallocAsync(&P->d_ev, sizeof(double) * std::max<int64_t>(P->ev_total, 1), st) == cudaSuccess;
+  ok &= cudaMallocAsync(&P->d_fallback, sizeof(unsigned) * (2 + 2 * (size_t)std::max<int64_t>(count, 1)), st) ==
+        cudaSuccess;
   if (gws_total) ok &= cudaMallocAsync(&P->d_gws, sizeof(double) * gws_total, st) == cudaSuccess;
   if (ok && count) {
     ok &= cudaMemcpyAsync(P->d_n, P->n_host.data(), sizeof(int32_t) * count, cudaMemcpyHostToDevice, st) ==
@@ -370,6 +373,7 @@ int skew_batch_plan_destroy(skew_batch_plan_t P) {
   if (P->d_order) cudaFreeAsync(P->d_order, st);
   if (P->d_ev_off) cudaFreeAsync(P->d_ev_off, st);
   if (P->d_counters) cudaFreeAsync(P->d_counters, st);
+  if (P->d_fallback) cudaFreeAsync(P->d_fallback, st);
   if (P->d_ev) cudaFreeAsync(P->d_ev, st);
   if (P->d_gws) cudaFreeAsync(P->d_gws, st);
   void* eig[] = {P->e_refl, P->e_tau, P->e_evb, P->e_G, P->e_log, P->e_work, P->e_vr, P->e_vi, P->e_vals,
@@ -512,6 +516,8 @@ int skew_batch_eigvals_d(skew_batch_plan_t P, const double* const* A, double* co
     tp.evwork = P->d_ev;
     tp.vals = vals_im;
     tp.status = status;
+    tp.fallback = P->d_fallback;
+    tp.grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
     CK(launch_batch_trieig(tp, P->h->stream));
     return SKEW_OK;
   });
@@ -759,9 +765,32 @@ static int single_func(skew_handle_t h, double* A, int64_t n, int64_t lda, doubl
   return SKEW_OK;
 }
 
+// Large single matrices (n > 1024): blocked reduction, bisection and the
+// twisted-factorisation eigenvectors of skew_tdvec.cu (the reference's fallback
+// formulation, values sorted descending).
+static int eigen_large(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,
+                       int64_t ldv, int* info) {
+  if (lda < n || ldv < n || n > (1LL << 15)) return n > (1LL << 15) ? SKEW_UNSUPPORTED : SKEW_BAD_ARG;
+  const size_t wsd = blocked_ws_doubles((int)n) + persist_ws_extra_doubles();
+  const size_t extra = 2 * (size_t)n + 8 + large_eigen_ws_doubles((int)n);
+  int st = ensure_ws(h, sizeof(double) * (wsd + extra));
+  if (st) return st;
+  double* base = (double*)h->ws + wsd;  // [ev (n)][tau (n)][bisection scratch (8)][eigenvector workspace]
+  double* ev = base;
+  double* tau = base + n;
+  double* bp = base + 2 * n;
+  double* lws = base + 2 * n + 8;
+  st = blocked(h, A, n, lda, tau, ev, info, extra, nullptr);
+  if (st) return st;
+  CK(launch_tridiag_bisect(ev, (int)n, vals_im, bp, h->stream));
+  CK(large_eigen_vectors(A, lda, (int)n, tau, ev, vals_im, bp, Vr, Vi, ldv, lws, h->stream));
+  return SKEW_OK;
+}
+
 int skew_eigen_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,
                  int64_t ldv, int* info) {
   if (!vals_im || !Vr || !Vi) return SKEW_BAD_ARG;
+  if (h && n > kSingleMax) return eigen_large(h, A, n, lda, vals_im, Vr, Vi, ldv, info);
   return single_func(h, A, n, lda, vals_im, Vr, Vi, ldv, nullptr, 0, nullptr, -1, info);
 }
 int skew_exp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, int64_t lde, int* info) {

@@ -84,12 +84,23 @@ struct TrieigParams {
   double* evwork;          // packed scratch, same layout as ev_all
   double* const* vals;     // [count] device pointers (n[b] each)
   int* status;             // [count] or null
+  unsigned* fallback;      // [2 + 2 count]: number of stagnated matrices, work counter,
+                           // then their indices and active sizes (solved by a second kernel)
+  int grid;                // CTAs of the fallback kernel
 };
 cudaError_t launch_batch_trieig(const TrieigParams& P, cudaStream_t st);
 
 // Eigenvalues of one skew tridiagonal by bisection on the equivalent zero-diagonal
 // symmetric tridiagonal; vals_im sorted descending.
 cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, double* scratch2, cudaStream_t st);
+
+// Eigenvectors of one large skew matrix after the blocked reduction (skew_tdvec.cu):
+// vals (descending, from launch_tridiag_bisect) and its scratch bp (bound, pivmin);
+// A holds the reflectors, tau their scalars, ev the subdiagonal.  Vr, Vi (n x n, ldv).
+size_t large_eigen_ws_doubles(int n);
+cudaError_t large_eigen_vectors(const double* A, int64_t lda, int n, const double* tau, const double* ev,
+                                const double* vals, const double* bp, double* Vr, double* Vi, int64_t ldv, double* ws,
+                                cudaStream_t st);
 
 // Eigenvectors / exp / cis / exp adjoint for batches of real skew matrices (skew_eigen.cu).
 // Leading dimensions of every per-matrix n x n buffer are n.

@@ -5,7 +5,10 @@
 // stagnation rule, one matrix per thread.  The iteration is a serial chain of
 // Givens rotations; since the FP64 pipe charges a warp instruction the same
 // whether one lane or 32 are active, 32 matrices share each warp (matrices are
-// sorted by size, so warp-mates run similar trip counts).
+// sorted by size, so warp-mates run similar trip counts).  A matrix whose
+// shifts stagnate is handed to a second kernel that solves the reference's
+// fallback, the eigenvalues of SymTridiagonal(0, ev) (skeweigen.jl:134-137,
+// 463-468), with one CTA per matrix and one eigenvalue per thread.
 //
 // Single large matrix: bisection with Sturm counts on the equivalent
 // zero-diagonal symmetric tridiagonal SymTridiagonal(0, ev), one eigenvalue per
@@ -109,33 +112,11 @@ __device__ int sturm_count(const double* e, int n, double x, double pivmin) {
   return c;
 }
 
-// Descending eigenvalues of SymTridiagonal(0, e) by serial bisection (fallback
-// path inside the batched QR; rare).
-__device__ void bisect_serial(const double* e, int n, double* out) {
-  double bound = 0.0, emax2 = 0.0;
-  for (int i = 0; i < n; i++) {
-    const double l = (i > 0 ? fabs(e[i - 1]) : 0.0), r = (i + 1 < n ? fabs(e[i]) : 0.0);
-    bound = fmax(bound, l + r);
-    if (i + 1 < n) emax2 = fmax(emax2, e[i] * e[i]);
-  }
-  const double pivmin = 2.2250738585072014e-308 * fmax(1.0, emax2);
-  bound = bound * (1.0 + 1e-14) + 1e-300;
-  for (int k = 0; k < n; k++) {  // k-th largest = (n-1-k)-th smallest
-    double lo = -bound, hi = bound;
-    for (int it = 0; it < 120 && hi - lo > 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300; it++) {
-      const double mid = 0.5 * (lo + hi);
-      if (sturm_count(e, n, mid, pivmin) <= n - 1 - k)
-        lo = mid;
-      else
-        hi = mid;
-    }
-    out[k] = 0.5 * (lo + hi);
-  }
-}
-
 // skewtrieigvals! (skeweigen.jl:105-156).  ev (N-1 entries) is destroyed;
-// vals[N] receives the imaginary parts in the reference's order.
-__device__ int skewtrieigvals_dev(double* ev, int N, double* vals) {
+// vals[N] receives the imaginary parts in the reference's order.  On stagnation
+// the active size n is returned in *fb_n (vals[0..n) and ev[0..n-1) are then
+// left to the fallback kernel).
+__device__ int skewtrieigvals_dev(double* ev, int N, double* vals, int* fb_n) {
   int n = N;
   for (int i = 0; i < N; i++) vals[i] = 0.0;
   if (n & 1) {
@@ -161,7 +142,7 @@ __device__ int skewtrieigvals_dev(double* ev, int N, double* vals) {
     if (n > 1 && fabs(mem - ev[n - 2]) < 0.0001 * fabs(ev[n - 2])) {
       count_static += 1;
       if (count_static > 4) {  // stagnation: symmetric tridiagonal fallback (:134-137)
-        bisect_serial(ev, n, vals);
+        *fb_n = n;
         return SKEW_FALLBACK_USED;
       }
     } else {
@@ -190,14 +171,83 @@ __global__ void batch_trieig_kernel(TrieigParams P) {
   double* ev = P.evwork + P.ev_off[b];
   if (P.evwork != P.ev_all)
     for (int i = 0; i + 1 < N; i++) ev[i] = P.ev_all[P.ev_off[b] + i];
-  const int st = (N >= 1) ? skewtrieigvals_dev(ev, N, P.vals[b]) : SKEW_OK;
+  int fb_n = 0;
+  const int st = (N >= 1) ? skewtrieigvals_dev(ev, N, P.vals[b], &fb_n) : SKEW_OK;
+  if (st == SKEW_FALLBACK_USED) {
+    const unsigned k = atomicAdd(P.fallback, 1u);
+    P.fallback[2 + k] = (unsigned)b;
+    P.fallback[2 + P.count + k] = (unsigned)fb_n;
+  }
   if (P.status) P.status[b] = st;
+}
+
+constexpr int FB_NT = 256;
+
+// The reference's fallback for matrices whose shifts stagnated: values[1:n] =
+// -eigvals(SymTridiagonal(0, ev[1:n-1])) (skeweigen.jl:134-137, 463-468), i.e.
+// the eigenvalues in descending order.  One CTA per matrix (taken from a work
+// counter), one eigenvalue per thread by Sturm-count bisection.
+__global__ void __launch_bounds__(FB_NT) batch_fallback_kernel(TrieigParams P) {
+  __shared__ int s_item;
+  __shared__ double red[2][FB_NT / 32];
+  const unsigned nfb = *(volatile unsigned*)P.fallback;
+  for (;;) {
+    if (threadIdx.x == 0) s_item = (int)atomicAdd(P.fallback + 1, 1u);
+    __syncthreads();
+    const int item = s_item;
+    __syncthreads();
+    if (item >= (int)nfb) break;
+    const int b = (int)P.fallback[2 + item];
+    const int n = (int)P.fallback[2 + P.count + item];
+    const double* e = P.evwork + P.ev_off[b];
+    double* vals = P.vals[b];
+    double bound = 0.0, emax2 = 0.0;
+    for (int i = threadIdx.x; i < n; i += FB_NT) {
+      const double l = (i > 0 ? fabs(e[i - 1]) : 0.0), r = (i + 1 < n ? fabs(e[i]) : 0.0);
+      bound = fmax(bound, l + r);
+      if (i + 1 < n) emax2 = fmax(emax2, e[i] * e[i]);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      bound = fmax(bound, __shfl_xor_sync(0xffffffffu, bound, o));
+      emax2 = fmax(emax2, __shfl_xor_sync(0xffffffffu, emax2, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+      red[0][threadIdx.x >> 5] = bound;
+      red[1][threadIdx.x >> 5] = emax2;
+    }
+    __syncthreads();
+    bound = 0.0;
+    emax2 = 0.0;
+    for (int w = 0; w < FB_NT / 32; w++) {
+      bound = fmax(bound, red[0][w]);
+      emax2 = fmax(emax2, red[1][w]);
+    }
+    __syncthreads();
+    const double pivmin = 2.2250738585072014e-308 * fmax(1.0, emax2);
+    bound = bound * (1.0 + 1e-14) + 1e-300;
+    for (int k = threadIdx.x; k < n; k += FB_NT) {  // k-th largest = (n-1-k)-th smallest
+      double lo = -bound, hi = bound;
+      for (int it = 0; it < 120 && hi - lo > 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300; it++) {
+        const double mid = 0.5 * (lo + hi);
+        if (sturm_count(e, n, mid, pivmin) <= n - 1 - k)
+          lo = mid;
+        else
+          hi = mid;
+      }
+      vals[k] = 0.5 * (lo + hi);
+    }
+  }
 }
 
 cudaError_t launch_batch_trieig(const TrieigParams& P, cudaStream_t st) {
   if (P.count <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(P.fallback, 0, 2 * sizeof(unsigned), st);
+  if (e != cudaSuccess) return e;
   const int bs = 32;
   batch_trieig_kernel<<<(P.count + bs - 1) / bs, bs, 0, st>>>(P);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  batch_fallback_kernel<<<P.grid > 0 ? P.grid : 1, FB_NT, 0, st>>>(P);
   return cudaGetLastError();
 }
 

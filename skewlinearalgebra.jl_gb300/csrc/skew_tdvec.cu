@@ -1,0 +1,624 @@
+// Eigenvectors of one large real skew matrix (n > 1024) on the whole GPU.
+//
+// The reference solves the tridiagonal eigenproblem by implicit QR with the
+// rotations accumulated into Qodd / Qeven (skewtrieigen_divided!, skeweigen.jl:
+// 322-457) and, when the shifts stagnate, through the symmetric tridiagonal
+// SymTridiagonal(0, ev) (skewtrieigen_backup!, skeweigen.jl:470-489).  The QR
+// chain is serial (about 2n^2 dependent rotations), which one GPU thread cannot
+// run at n = 8192 in reasonable time.  This file computes the same
+// decomposition the way the fallback formulates it:
+//   1. eigenvalues sigma_k > 0 of SymTridiagonal(0, ev) by bisection (skew_qr.cu),
+//      sorted descending (the reference's fallback order: vals = -eigvals(H));
+//   2. one eigenvector w_k of SymTridiagonal(0, ev) per sigma_k, one thread
+//      each, from the twisted factorisation of T - sigma I: the stationary
+//      L D L^T (top-down) and progressive U D U^T (bottom-up) pivots, the twist
+//      index r = argmin |gamma_r|, and the vector by the two recurrences out of
+//      r (the twisted-factorisation eigenvector of Dhillon and Parlett's MRRR,
+//      here without the relatively robust representations);
+//   3. the even-row and odd-row parts of the w_k are the left and right singular
+//      vectors of the bidiagonal coupling; each set is made orthonormal by one
+//      symmetric (Lowdin) correction restricted to a band of LW neighbours in
+//      the sorted spectrum, which keeps residuals at the eps level;
+//   4. the skew eigenvectors in the tridiagonal basis follow the fallback's
+//      pattern (real on odd 1-based rows, imaginary on even rows, sign flipped
+//      every pair); the vector of -sigma_k is the conjugate of that of sigma_k;
+//   5. back-transformation X <- Q X with the stored reflectors, panel by panel in
+//      compact WY form (Q_b = I - V T V^T, dlarft-style T), each CTA owning a
+//      strip of 32 columns (no inter-CTA dependence);
+//   6. the +sigma columns are mirrored from the -sigma columns (Vr equal, Vi
+//      negated).
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include <algorithm>
+
+#include "skew_common.cuh"
+#include "skew_internal.h"
+
+namespace skew {
+
+constexpr int TW_NT = 64;  // threads per CTA of the twisted kernel (one vector each)
+constexpr int TW_PF = 8;   // rows prefetched per chunk
+constexpr int LW = 16;     // half-width of the Lowdin band
+constexpr int WB = 64;     // reflectors per compact-WY panel
+constexpr int SW = 32;     // columns per back-transformation strip
+constexpr int RC = 32;     // rows per staged chunk
+
+struct TdvecLayout {
+  int n, h, K, KP;  // n, positive eigenvalues, vectors (h + n odd), padded to 32
+  int npan;         // WY panels
+  double* dp;       // n x KP
+  double* dm;       // n x KP
+  double* z;        // n x KP
+  double* nrm2;     // KP
+  double* bandU;    // KP x (LW + 1) raw dots over even rows
+  double* bandV;    // KP x (LW + 1) raw dots over odd rows
+  double* T;        // npan x WB x WB
+};
+
+static TdvecLayout layout(int n, double* ws) {
+  TdvecLayout L;
+  L.n = n;
+  L.h = n / 2;
+  L.K = L.h + (n & 1);
+  L.KP = (L.K + 31) / 32 * 32;
+  L.npan = (n - 2 + WB - 1) / WB;
+  const size_t big = (size_t)n * L.KP;
+  L.dp = ws;
+  L.dm = L.dp + big;
+  L.z = L.dm + big;
+  L.nrm2 = L.z + big;
+  L.bandU = L.nrm2 + L.KP;
+  L.bandV = L.bandU + (size_t)L.KP * (LW + 1);
+  L.T = L.bandV + (size_t)L.KP * (LW + 1);
+  return L;
+}
+
+size_t large_eigen_ws_doubles(int n) {
+  const int h = n / 2, K = h + (n & 1), KP = (K + 31) / 32 * 32;
+  const int npan = (n - 2 + WB - 1) / WB;
+  return 3 * (size_t)n * KP + KP + 2 * (size_t)KP * (LW + 1) + (size_t)std::max(npan, 1) * WB * WB + 64;
+}
+
+// ---------------------------------------------------------------------------
+// 2. twisted factorisation eigenvectors, one thread per sigma
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(TW_NT) twisted_kernel(const double* __restrict__ e, const double* __restrict__ vals,
+                                                        const double* __restrict__ bp, TdvecLayout L) {
+  const int k = blockIdx.x * TW_NT + threadIdx.x;
+  if (k >= L.KP) return;  // KP is a multiple of 32: whole warps leave together
+  const int n = L.n;
+  const int64_t KP = L.KP;
+  const double sig = (k < L.h) ? vals[k] : 0.0;  // padded lanes solve a dummy sigma = 0 vector
+  const double nsig = neg(sig);
+  const double pivmin = bp[1];
+  double* __restrict__ dp = L.dp;
+  double* __restrict__ dm = L.dm;
+  double* __restrict__ z = L.z;
+
+  // pass 1: T - sigma I = L+ D+ L+^T, D+ stored
+  double d = nsig;
+  for (int i = 0; i < n; i++) {
+    if (fabs(d) <= pivmin) d = neg(pivmin);
+    dp[(int64_t)i * KP + k] = d;
+    if (i + 1 < n) {
+      const double ei = e[i];
+      d = nsig - (ei * ei) / d;
+    }
+  }
+  // pass 2: T - sigma I = U- D- U-^T (bottom-up), D- stored; twist r = argmin |gamma|
+  double best = INFINITY;
+  int r = n - 1;
+  d = nsig;
+  {
+    double cur[TW_PF], nxt[TW_PF];
+#pragma unroll
+    for (int j = 0; j < TW_PF; j++) cur[j] = (n - 1 - j >= 0) ? dp[(int64_t)(n - 1 - j) * KP + k] : 0.0;
+    for (int i0 = n - 1; i0 >= 0; i0 -= TW_PF) {
+#pragma unroll
+      for (int j = 0; j < TW_PF; j++) {
+        const int i = i0 - TW_PF - j;
+        nxt[j] = (i >= 0) ? dp[(int64_t)i * KP + k] : 0.0;
+      }
+#pragma unroll
+      for (int j = 0; j < TW_PF; j++) {
+        const int i = i0 - j;
+        if (i >= 0) {
+          if (fabs(d) <= pivmin) d = neg(pivmin);
+          dm[(int64_t)i * KP + k] = d;
+          const double g = fabs(cur[j] + d + sig);  // gamma_i = D+_i + D-_i - (T_ii - sigma), T_ii = 0
+          if (g < best) {
+            best = g;
+            r = i;
+          }
+          if (i > 0) {
+            const double ei = e[i - 1];
+            d = nsig - (ei * ei) / d;
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < TW_PF; j++) cur[j] = nxt[j];
+    }
+  }
+  // pass 3: z_r = 1; z_i = -(e_i / D+_i) z_{i+1} above r, z_{i+1} = -(e_i / D-_{i+1}) z_i below.
+  // A zero neighbour falls back on the three-term relation of the row between.
+  z[(int64_t)r * KP + k] = 1.0;
+  double nrm = 1.0;
+  int rmax = r, rmin = r;
+  for (int o = 16; o > 0; o >>= 1) {
+    rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    rmin = min(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
+  }
+  {  // top part, rows rmax-1 .. 0 in lockstep (coalesced), lanes active below their r
+    double z1 = 1.0, z2 = 0.0;
+    double cur[TW_PF], nxt[TW_PF];
+#pragma unroll
+    for (int j = 0; j < TW_PF; j++) cur[j] = (rmax - 1 - j >= 0) ? dp[(int64_t)(rmax - 1 - j) * KP + k] : 1.0;
+    for (int i0 = rmax - 1; i0 >= 0; i0 -= TW_PF) {
+#pragma unroll
+      for (int j = 0; j < TW_PF; j++) {
+        const int i = i0 - TW_PF - j;
+        nxt[j] = (i >= 0) ? dp[(int64_t)i * KP + k] : 1.0;
+      }
+#pragma unroll
+      for (int j = 0; j < TW_PF; j++) {
+        const int i = i0 - j;
+        if (i >= 0 && i < r) {
+          const double ei = e[i];
+          double zi;
+          if (z1 != 0.0)
+            zi = neg(ei / cur[j]) * z1;
+          else
+            zi = (ei != 0.0) ? neg(e[i + 1] / ei) * z2 : 0.0;
+          z[(int64_t)i * KP + k] = zi;
+          nrm = fma(zi, zi, nrm);
+          z2 = z1;
+          z1 = zi;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < TW_PF; j++) cur[j] = nxt[j];
+    }
+  }
+  {  // bottom part, rows rmin+1 .. n-1, lanes active above their r
+    double z1 = 1.0, z0 = 0.0;  // z_i, z_{i-1}
+    double cur[TW_PF], nxt[TW_PF];
+#pragma unroll
+    for (int j = 0; j < TW_PF; j++) cur[j] = (rmin + 1 + j < n) ? dm[(int64_t)(rmin + 1 + j) * KP + k] : 1.0;
+    for (int i0 = rmin; i0 <= n - 2; i0 += TW_PF) {
+#pragma unroll
+      for (int j = 0; j < TW_PF; j++) {
+        const int i = i0 + TW_PF + j;
+        nxt[j] = (i + 1 < n) ? dm[(int64_t)(i + 1) * KP + k] : 1.0;
+      }
+#pragma unroll
+      for (int j = 0; j < TW_PF; j++) {
+        const int i = i0 + j;
+        if (i <= n - 2 && i >= r) {
+          const double ei = e[i];
+          double zn;
+          if (z1 != 0.0)
+            zn = neg(ei / cur[j]) * z1;
+          else
+            zn = (ei != 0.0 && i > 0) ? neg(e[i - 1] / ei) * z0 : 0.0;
+          z[(int64_t)(i + 1) * KP + k] = zn;
+          nrm = fma(zn, zn, nrm);
+          z0 = z1;
+          z1 = zn;
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < TW_PF; j++) cur[j] = nxt[j];
+    }
+  }
+  L.nrm2[k] = nrm;
+}
+
+// ---------------------------------------------------------------------------
+// 3. banded Gram entries: raw dots of vector k with k + d (d = 0..LW), over the
+//    even rows (U) and the odd rows (V) separately
+// ---------------------------------------------------------------------------
+constexpr int BD_NT = 256;
+constexpr int BD_COLS = 32 + LW;
+constexpr int BD_PAIRS = 32 * (LW + 1);
+constexpr int BD_PER = (BD_PAIRS + BD_NT - 1) / BD_NT;
+
+__global__ void __launch_bounds__(BD_NT) band_dots_kernel(TdvecLayout L) {
+  __shared__ double zs[RC][BD_COLS + 1];
+  const int k0 = blockIdx.x * 32;
+  const int n = L.n;
+  const int64_t KP = L.KP;
+  double accU[BD_PER], accV[BD_PER];
+#pragma unroll
+  for (int q = 0; q < BD_PER; q++) accU[q] = accV[q] = 0.0;
+  for (int i0 = 0; i0 < n; i0 += RC) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < RC * BD_COLS; idx += BD_NT) {
+      const int rr = idx / BD_COLS, cc = idx - rr * BD_COLS;
+      const int i = i0 + rr, k = k0 + cc;
+      zs[rr][cc] = (i < n && k < L.K) ? L.z[(int64_t)i * KP + k] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int q = 0; q < BD_PER; q++) {
+      const int pr = threadIdx.x + q * BD_NT;
+      if (pr < BD_PAIRS) {
+        const int kk = pr % 32, dd = pr / 32;
+        double su = 0.0, sv = 0.0;
+        for (int rr = 0; rr < RC; rr += 2) {  // i0 is even, so rr even <-> even row
+          su = fma(zs[rr][kk], zs[rr][kk + dd], su);
+          sv = fma(zs[rr + 1][kk], zs[rr + 1][kk + dd], sv);
+        }
+        accU[q] += su;
+        accV[q] += sv;
+      }
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < BD_PER; q++) {
+    const int pr = threadIdx.x + q * BD_NT;
+    if (pr < BD_PAIRS) {
+      const int kk = pr % 32, dd = pr / 32;
+      const int k = k0 + kk;
+      L.bandU[(int64_t)k * (LW + 1) + dd] = accU[q];
+      L.bandV[(int64_t)k * (LW + 1) + dd] = accV[q];
+    }
+  }
+}
+
+// scale s_k that makes the even-row (or odd-row) part of vector k a unit vector:
+// sqrt(2)/|z_k| for sigma_k > 0, 1/|z_k| for the zero-eigenvalue vector (no odd part)
+__device__ __forceinline__ double part_scale(const TdvecLayout& L, int k) {
+  if (k >= L.K) return 0.0;
+  const double inv = rsqrt(L.nrm2[k]);
+  return (k < L.h) ? 1.4142135623730951 * inv : inv;
+}
+
+// ---------------------------------------------------------------------------
+// 3-4. Lowdin-corrected vectors, written in the tridiagonal basis into the
+//      columns of Vr / Vi that hold the -sigma eigenvectors
+// ---------------------------------------------------------------------------
+constexpr int LA_NT = 256;
+constexpr int LA_COLS = 32 + 2 * LW;
+
+__global__ void __launch_bounds__(LA_NT) lowdin_apply_kernel(TdvecLayout L, double* __restrict__ Vr,
+                                                             double* __restrict__ Vi, int64_t ldv) {
+  __shared__ double zs[RC][LA_COLS + 1];
+  __shared__ double sc[LA_COLS];
+  __shared__ double eU[32][2 * LW + 1], eV[32][2 * LW + 1];
+  __shared__ double out[RC][33];
+  const int k0 = blockIdx.x * 32, i0 = blockIdx.y * RC;
+  const int n = L.n;
+  const int64_t KP = L.KP;
+  for (int c = threadIdx.x; c < LA_COLS; c += LA_NT) sc[c] = (k0 - LW + c >= 0) ? part_scale(L, k0 - LW + c) : 0.0;
+  for (int idx = threadIdx.x; idx < RC * LA_COLS; idx += LA_NT) {
+    const int rr = idx / LA_COLS, cc = idx - rr * LA_COLS;
+    const int i = i0 + rr, k = k0 - LW + cc;
+    zs[rr][cc] = (i < n && k >= 0 && k < L.K) ? L.z[(int64_t)i * KP + k] : 0.0;
+  }
+  __syncthreads();
+  // normalised band E(k, k+d) = s_k s_{k+d} dot - delta, d in [-LW, LW]
+  for (int idx = threadIdx.x; idx < 32 * (2 * LW + 1); idx += LA_NT) {
+    const int kk = idx / (2 * LW + 1), dd = idx - kk * (2 * LW + 1) - LW;
+    const int k = k0 + kk, j = k + dd;
+    double u = 0.0, v = 0.0;
+    if (k < L.K && j >= 0 && j < L.K) {
+      const int lo = min(k, j), off = abs(dd);
+      const double s = sc[kk + LW] * sc[kk + LW + dd];
+      u = s * L.bandU[(int64_t)lo * (LW + 1) + off] - (dd == 0 ? 1.0 : 0.0);
+      const bool zk = (k >= L.h), zj = (j >= L.h);  // the zero-eigenvalue vector has no odd part
+      v = (zk || zj) ? 0.0 : s * L.bandV[(int64_t)lo * (LW + 1) + off] - (dd == 0 ? 1.0 : 0.0);
+    }
+    eU[kk][dd + LW] = u;
+    eV[kk][dd + LW] = v;
+  }
+  __syncthreads();
+  // out(i, k) = s_k z(i,k) - 1/2 sum_d E(k,k+d) s_{k+d} z(i,k+d), then back to |w| = 1 scale
+  for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
+    const int kk = idx / RC, rr = idx - kk * RC;  // consecutive threads: consecutive rows
+    const int i = i0 + rr, k = k0 + kk;
+    double o = 0.0;
+    if (i < n && k < L.K) {
+      const double(*E)[2 * LW + 1] = (i & 1) ? eV : eU;
+      double acc = sc[kk + LW] * zs[rr][kk + LW];
+#pragma unroll 11
+      for (int dd = -LW; dd <= LW; dd++) acc = fma(-0.5 * E[kk][dd + LW], sc[kk + LW + dd] * zs[rr][kk + LW + dd], acc);
+      o = (k < L.h) ? acc * 0.7071067811865476 : acc;
+      if ((i >> 1) & 1) o = neg(o);  // fallback pattern: sign flips every (odd, even) pair
+    }
+    out[rr][kk] = o;
+  }
+  __syncthreads();
+  // column of the -sigma_k eigenvector: n-1-k; the zero-eigenvalue vector: column h
+  for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
+    const int kk = idx / RC, rr = idx - kk * RC;
+    const int i = i0 + rr, k = k0 + kk;
+    if (i >= n || k >= L.K) continue;
+    const int col = (k < L.h) ? n - 1 - k : L.h;
+    const double o = out[rr][kk];
+    if ((i & 1) == 0) {
+      Vr[i + (int64_t)col * ldv] = o;
+      if (k < L.h) Vi[i + (int64_t)col * ldv] = 0.0;
+    } else {
+      Vr[i + (int64_t)col * ldv] = 0.0;
+      if (k < L.h) Vi[i + (int64_t)col * ldv] = o;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 5. compact WY factors T_b (dlarft, forward, columnwise) of each panel
+// ---------------------------------------------------------------------------
+// Reflector c (0 <= c <= n-3) lives in column c of A below the diagonal: v_c = 0
+// above row c+1, v_c[c+1] = 1, v_c[c+2:] = A[c+2:, c]; tau_c = 0 means H_c = I.
+__device__ __forceinline__ double refl_at(const double* A, int64_t lda, const double* tau, int row, int c) {
+  if (row < c + 1 || tau[c] == 0.0) return 0.0;
+  return (row == c + 1) ? 1.0 : A[row + (int64_t)c * lda];
+}
+
+constexpr int WT_NT = 256;
+constexpr int WT_RC = 16;  // rows per staged chunk of the factor kernel
+
+// One array holds both: the lower triangle of M is the Gram matrix G = V^T V
+// (symmetric, so G(l, i) is read as M(i, l)), the upper triangle and diagonal
+// receive T as the recurrence produces it (a diagonal G entry is never needed).
+__global__ void __launch_bounds__(WT_NT) wy_factor_kernel(const double* __restrict__ A, int64_t lda,
+                                                          const double* __restrict__ tau, TdvecLayout L) {
+  __shared__ double Vs[WT_RC][WB + 1];
+  __shared__ double M[WB][WB + 1];
+  const int b = blockIdx.x;
+  const int n = L.n;
+  const int c0 = b * WB, c1 = min(c0 + WB, n - 2), nb = c1 - c0;
+  const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) acc[a][q] = 0.0;
+  for (int r0 = c0 + 1; r0 < n; r0 += WT_RC) {
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < WT_RC * WB; idx += WT_NT) {
+      const int cc = idx / WT_RC, rr = idx - cc * WT_RC;
+      const int row = r0 + rr, c = c0 + cc;
+      Vs[rr][cc] = (row < n && cc < nb) ? refl_at(A, lda, tau, row, c) : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < WT_RC; rr++) {
+      double va[4], vb[4];
+#pragma unroll
+      for (int a = 0; a < 4; a++) {
+        va[a] = Vs[rr][ty + 16 * a];
+        vb[a] = Vs[rr][tx + 16 * a];
+      }
+#pragma unroll
+      for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int q = 0; q < 4; q++) acc[a][q] = fma(va[a], vb[q], acc[a][q]);
+    }
+  }
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int i = ty + 16 * a, j = tx + 16 * q;
+      M[i][j] = (i > j) ? acc[a][q] : 0.0;  // G below the diagonal, T (zero so far) on and above
+    }
+  __syncthreads();
+  // T(i,i) = tau_i; T(0:i, i) = -tau_i T(0:i, 0:i) G(0:i, i)
+  for (int i = 0; i < nb; i++) {
+    const double ti = tau[c0 + i];
+    if (threadIdx.x < i) {
+      const int j = threadIdx.x;
+      double s = 0.0;
+      for (int l = j; l < i; l++) s = fma(M[j][l], M[i][l], s);
+      M[j][i] = neg(ti) * s;
+    }
+    if (threadIdx.x == 0) M[i][i] = ti;
+    __syncthreads();
+  }
+  double* Tg = L.T + (size_t)b * WB * WB;
+  for (int idx = threadIdx.x; idx < WB * WB; idx += WT_NT) {
+    const int i = idx / WB, j = idx % WB;
+    Tg[idx] = (j >= i) ? M[i][j] : 0.0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 5. X <- Q X, one CTA per strip of SW columns, panels last to first:
+//    W = V^T X, W <- T W, X <- X - V W
+// ---------------------------------------------------------------------------
+constexpr int BT_NT = 256;
+
+struct StripParams {
+  const double* A;
+  int64_t lda;
+  const double* tau;
+  TdvecLayout L;
+  double* Xr;  // columns [cr0, n) of Vr
+  double* Xi;  // columns [ci0, n) of Vi
+  int64_t ldv;
+  int cr0, ci0, nstr_r;  // strips over Vr first
+};
+
+__global__ void __launch_bounds__(BT_NT) back_strip_kernel(StripParams P) {
+  extern __shared__ __align__(16) double bsm[];
+  double(*Ts)[WB + 1] = reinterpret_cast<double(*)[WB + 1]>(bsm);                   // WB x (WB+1)
+  double(*Ws)[SW + 1] = reinterpret_cast<double(*)[SW + 1]>(bsm + WB * (WB + 1));  // WB x (SW+1)
+  double(*Vs)[WB + 1] = reinterpret_cast<double(*)[WB + 1]>(bsm + WB * (WB + 1) + WB * (SW + 1));  // RC x (WB+1)
+  double(*Xs)[SW + 1] =
+      reinterpret_cast<double(*)[SW + 1]>(bsm + WB * (WB + 1) + WB * (SW + 1) + RC * (WB + 1));  // RC x (SW+1)
+  const int n = P.L.n;
+  const int s = blockIdx.x;
+  double* X;
+  int col0, ncol;
+  if (s < P.nstr_r) {
+    X = P.Xr;
+    col0 = P.cr0 + s * SW;
+  } else {
+    X = P.Xi;
+    col0 = P.ci0 + (s - P.nstr_r) * SW;
+  }
+  ncol = min(SW, n - col0);
+  X += (int64_t)col0 * P.ldv;
+  const int64_t ldx = P.ldv;
+  // thread tiles: W (WB x SW = 64 x 32): 4 x 2 per thread; X chunk (RC x SW = 32 x 32): 2 x 2 per thread
+  const int wr = (threadIdx.x >> 4) * 4, wc = (threadIdx.x & 15) * 2;
+  const int xr = (threadIdx.x >> 4) * 2, xc = (threadIdx.x & 15) * 2;
+  for (int b = P.L.npan - 1; b >= 0; b--) {
+    const int c0 = b * WB, c1 = min(c0 + WB, n - 2), nb = c1 - c0;
+    __syncthreads();
+    for (int idx = threadIdx.x; idx < WB * WB; idx += BT_NT)
+      Ts[idx / WB][idx % WB] = P.L.T[(size_t)b * WB * WB + idx];
+    // W = V^T X over rows c0+1 .. n-1
+    double w[4][2];
+#pragma unroll
+    for (int a = 0; a < 4; a++) w[a][0] = w[a][1] = 0.0;
+    for (int r0 = c0 + 1; r0 < n; r0 += RC) {
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < RC * WB; idx += BT_NT) {
+        const int cc = idx / RC, rr = idx - cc * RC;
+        const int row = r0 + rr;
+        Vs[rr][cc] = (row < n && cc < nb) ? refl_at(P.A, P.lda, P.tau, row, c0 + cc) : 0.0;
+      }
+      for (int idx = threadIdx.x; idx < RC * SW; idx += BT_NT) {
+        const int cc = idx / RC, rr = idx - cc * RC;
+        const int row = r0 + rr;
+        Xs[rr][cc] = (row < n && cc < ncol) ? X[row + (int64_t)cc * ldx] : 0.0;
+      }
+      __syncthreads();
+#pragma unroll 8
+      for (int rr = 0; rr < RC; rr++) {
+        const double x0 = Xs[rr][wc], x1 = Xs[rr][wc + 1];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+          const double v = Vs[rr][wr + a];
+          w[a][0] = fma(v, x0, w[a][0]);
+          w[a][1] = fma(v, x1, w[a][1]);
+        }
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      Ws[wr + a][wc] = w[a][0];
+      Ws[wr + a][wc + 1] = w[a][1];
+    }
+    __syncthreads();
+    // W <- T W (T upper triangular)
+    double tw[4][2];
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      tw[a][0] = tw[a][1] = 0.0;
+      const int i = wr + a;
+      for (int l = i; l < WB; l++) {
+        const double t = Ts[i][l];
+        tw[a][0] = fma(t, Ws[l][wc], tw[a][0]);
+        tw[a][1] = fma(t, Ws[l][wc + 1], tw[a][1]);
+      }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int a = 0; a < 4; a++) {
+      Ws[wr + a][wc] = tw[a][0];
+      Ws[wr + a][wc + 1] = tw[a][1];
+    }
+    // X <- X - V W over rows c0+1 .. n-1 (X chunk staged: coalesced column reads and writes)
+    for (int r0 = c0 + 1; r0 < n; r0 += RC) {
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < RC * WB; idx += BT_NT) {
+        const int cc = idx / RC, rr = idx - cc * RC;
+        const int row = r0 + rr;
+        Vs[rr][cc] = (row < n && cc < nb) ? refl_at(P.A, P.lda, P.tau, row, c0 + cc) : 0.0;
+      }
+      for (int idx = threadIdx.x; idx < RC * SW; idx += BT_NT) {
+        const int cc = idx / RC, rr = idx - cc * RC;
+        const int row = r0 + rr;
+        Xs[rr][cc] = (row < n && cc < ncol) ? X[row + (int64_t)cc * ldx] : 0.0;
+      }
+      __syncthreads();
+      double acc[2][2] = {{0.0, 0.0}, {0.0, 0.0}};
+#pragma unroll 8
+      for (int l = 0; l < WB; l++) {
+        const double w0 = Ws[l][xc], w1 = Ws[l][xc + 1];
+        const double v0 = Vs[xr][l], v1 = Vs[xr + 1][l];
+        acc[0][0] = fma(v0, w0, acc[0][0]);
+        acc[0][1] = fma(v0, w1, acc[0][1]);
+        acc[1][0] = fma(v1, w0, acc[1][0]);
+        acc[1][1] = fma(v1, w1, acc[1][1]);
+      }
+#pragma unroll
+      for (int a = 0; a < 2; a++)
+#pragma unroll
+        for (int q = 0; q < 2; q++) Xs[xr + a][xc + q] -= acc[a][q];
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < RC * SW; idx += BT_NT) {
+        const int cc = idx / RC, rr = idx - cc * RC;
+        const int row = r0 + rr;
+        if (row < n && cc < ncol) X[row + (int64_t)cc * ldx] = Xs[rr][cc];
+      }
+    }
+  }
+}
+
+// 6. +sigma columns: Vr[:, k] = Vr[:, n-1-k], Vi[:, k] = -Vi[:, n-1-k]; odd n: Vi[:, h] = 0
+__global__ void mirror_kernel(double* __restrict__ Vr, double* __restrict__ Vi, int64_t ldv, int n) {
+  const int h = n / 2;
+  const int k = blockIdx.y;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (k < h) {
+      const int64_t src = i + (int64_t)(n - 1 - k) * ldv, dst = i + (int64_t)k * ldv;
+      Vr[dst] = Vr[src];
+      Vi[dst] = neg(Vi[src]);
+    } else {
+      Vi[i + (int64_t)h * ldv] = 0.0;  // k == h only launched for odd n
+    }
+  }
+}
+
+static size_t strip_smem_bytes() {
+  return sizeof(double) * ((size_t)WB * (WB + 1) + (size_t)WB * (SW + 1) + (size_t)RC * (WB + 1) + (size_t)RC * (SW + 1));
+}
+
+cudaError_t large_eigen_vectors(const double* A, int64_t lda, int n, const double* tau, const double* ev,
+                                const double* vals, const double* bp, double* Vr, double* Vi, int64_t ldv, double* ws,
+                                cudaStream_t st) {
+  if (n < 3) return cudaErrorInvalidValue;
+  const TdvecLayout L = layout(n, ws);
+  twisted_kernel<<<L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), TW_NT, 0, st>>>(ev, vals, bp, L);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  band_dots_kernel<<<L.KP / 32, BD_NT, 0, st>>>(L);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  lowdin_apply_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC), LA_NT, 0, st>>>(L, Vr, Vi, ldv);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  wy_factor_kernel<<<L.npan, WT_NT, 0, st>>>(A, lda, tau, L);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  StripParams P;
+  P.A = A;
+  P.lda = lda;
+  P.tau = tau;
+  P.L = L;
+  P.Xr = Vr;
+  P.Xi = Vi;
+  P.ldv = ldv;
+  P.cr0 = L.h;                // -sigma columns and the zero vector
+  P.ci0 = L.h + (n & 1);      // -sigma columns
+  P.nstr_r = (n - P.cr0 + SW - 1) / SW;
+  const int nstr_i = (n - P.ci0 + SW - 1) / SW;
+  static std::atomic<uint64_t> raised{0};
+  e = raise_smem_limit_once((const void*)back_strip_kernel, raised);
+  if (e != cudaSuccess) return e;
+  back_strip_kernel<<<P.nstr_r + nstr_i, BT_NT, strip_smem_bytes(), st>>>(P);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  mirror_kernel<<<dim3((n + 255) / 256, L.h + (n & 1)), 256, 0, st>>>(Vr, Vi, ldv, n);
+  return cudaGetLastError();
+}
+
+}  // namespace skew

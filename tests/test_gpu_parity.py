@@ -242,3 +242,35 @@ def test_batch_eigvals_tridiagonal_cases(skewgpu, oracle):
         ref = np.sort(np.linalg.eigvals(A).imag)
         np.testing.assert_allclose(np.sort(v), ref, atol=1e-12)
     plan.close()
+
+
+def test_batch_eigvals_stagnation_fallback(skewgpu, oracle):
+    """Matrix 274 (n = 200) of the seeded 4096-matrix workload makes the Wilkinson
+    shifts stagnate in the reference algorithm (the oracle's FP64 restatement
+    takes the fallback there too).  The batched eigvals must report
+    SKEW_FALLBACK_USED and return the fallback's descending values."""
+    import torch
+
+    import bench
+
+    sizes = bench.workload_sizes()[:275]
+    buf, offs = bench.packed_inputs(sizes)
+    pick = [274, 0, 1, 273]
+    mats = [buf[offs[b]:offs[b] + sizes[b] ** 2].reshape(sizes[b], sizes[b], order="F") for b in pick]
+    assert oracle.eigvals(mats[0])[1] != 0  # the oracle stagnates on it as well
+    ns = [m.shape[0] for m in mats]
+    plan = skewgpu.BatchPlan(ns)
+    devs = [skewgpu.to_device(A) for A in mats]
+    vals = [torch.zeros(n, dtype=torch.float64, device="cuda") for n in ns]
+    st = plan.eigvals(plan.pointer_array(devs), plan.pointer_array(vals))
+    torch.cuda.synchronize()
+    st = st.cpu().numpy()
+    assert st[0] == 8 and (st[1:] == 0).all()
+    for b, A in enumerate(mats):
+        v = vals[b].cpu().numpy()
+        vq, _ = oracle.eigvals(A, quad=True)
+        vd, _ = oracle.eigvals(A)
+        scale = np.abs(vq).max()
+        np.testing.assert_allclose(np.sort(v), np.sort(vq), atol=RTOL * scale)
+        np.testing.assert_allclose(v, vd, atol=1e-11 * scale)  # same order as the reference
+    plan.close()
