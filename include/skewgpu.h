@@ -149,6 +149,40 @@ SKEW_API int skew_batch_exp_vjp_d(skew_batch_plan_t plan, const double* const* A
 SKEW_API int skew_exp_vjp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* Cbar, double* G,
                             int64_t ldg, int* info);
 
+/* ---------------------------------------------------------------------------
+ * ComplexF64 skew-Hermitian matrices (A^H = -A).  Complex arrays are ComplexF64
+ * interleaved (re, im), column-major, leading dimensions in complex elements.
+ * ------------------------------------------------------------------------- */
+
+/* LA.hessenberg!(A::SkewHermitian{ComplexF64})  hessenberg.jl:5-13 with the complex
+ * branches of householder! :26-44, skewlatrd! :92-131 and skewblockedhess! :144-173.
+ * In place: reflectors below the subdiagonal (v[1] = 1 on the subdiagonal), tau[n-1]
+ * complex, ev[n-1] the real subdiagonal and dvim[n] = imag(diag) of
+ * H = SkewHermTridiagonal(ev, dvim).  dvim may be NULL. */
+SKEW_API int skew_hessenberg_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev,
+                               double* dvim, int* info);
+
+/* LA.eigvals!(A::SkewHermitian{ComplexF64})  eigen.jl:18-27: vals_im[n] = imaginary parts,
+ * descending (the reference returns -eigvals(Hermitian(i A)), eigenvalues ascending).
+ * A is destroyed. */
+SKEW_API int skew_eigvals_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info);
+
+/* LA.eigen!(A::SkewHermitian{ComplexF64})  eigen.jl:101-106: vals_im[n] (descending) and
+ * the eigenvectors V (n x n ComplexF64, ldv).  Eigenvectors are defined up to a
+ * phase per column (LAPACK's choice in the reference).  A is destroyed. */
+SKEW_API int skew_eigen_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* V,
+                          int64_t ldv, int* info);
+
+/* Base.exp(A::SkewHermitian{ComplexF64})  exp.jl:37-46: E = V diag(exp(lambda)) V^H
+ * (ComplexF64, lde).  A is destroyed. */
+SKEW_API int skew_exp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, int64_t lde, int* info);
+
+/* Adjoint of exp for ComplexF64 (no reference counterpart): G = V (conj(Phi) o (V^H Cbar V)) V^H
+ * with Phi the divided differences of exp on the spectrum, i.e. dL = Re tr(G^H dA) for
+ * L = Re tr(Cbar^H exp(A)).  Cbar (n x n, leading dimension n), G (ldg) ComplexF64. */
+SKEW_API int skew_exp_vjp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* Cbar, double* G,
+                            int64_t ldg, int* info);
+
 /* Diagnostics: measured FP64 DFMA throughput of the current device in TFLOP/s
  * (runs a short microbenchmark on the handle's stream and synchronizes). */
 SKEW_API int skew_measure_fp64_peak(skew_handle_t h, double* tflops);

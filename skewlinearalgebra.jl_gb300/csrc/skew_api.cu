@@ -808,6 +808,146 @@ int skew_exp_vjp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, const dou
 }
 
 // ---------------------------------------------------------------------------
+// ComplexF64 skew-Hermitian matrices (skew_complex.cu)
+// ---------------------------------------------------------------------------
+// Workspace of the complex calls: [reduction ws][ev (n)][tau (2n)][dvim (n)]
+// [vals (n)][V (2 n^2, eigen/exp)][eigen ws][function ws].
+struct ZLayout {
+  double *zws, *ev, *tau, *dvim, *vals, *V, *ews, *fws;
+};
+
+static int zlayout(skew_handle_t h, int64_t n, bool vecs, bool func, ZLayout* L) {
+  // every segment a multiple of 32 doubles: complex arrays stay 16-byte aligned
+  auto seg = [](size_t d) { return (d + 31) & ~(size_t)31; };
+  const size_t zr = seg(zhess_large_ws_doubles((int)n));
+  const size_t ze = seg(zeigen_ws_doubles((int)n));
+  const size_t zf = func ? seg(zfunc_ws_doubles((int)n)) : 0;
+  const size_t nv = vecs ? seg(2 * (size_t)n * n) : 0;
+  const size_t sn = seg(n), s2n = seg(2 * (size_t)n), sv = seg(n + 8);
+  const size_t total = zr + sn + s2n + sn + sv + nv + ze + zf + 64;
+  int st = ensure_ws(h, sizeof(double) * total);
+  if (st) return st;
+  double* p = (double*)h->ws;
+  L->zws = p;
+  p += zr;
+  L->ev = p;
+  p += sn;
+  L->tau = p;
+  p += s2n;
+  L->dvim = p;
+  p += sn;
+  L->vals = p;
+  p += sv;
+  L->V = vecs ? p : nullptr;
+  p += nv;
+  L->ews = p;
+  p += ze;
+  L->fws = func ? p : nullptr;
+  return SKEW_OK;
+}
+
+// complex reduction in place: one CTA for small n, per-column multi-CTA kernels above
+static int zreduce(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev, double* dvim,
+                   double* zws) {
+  if (n <= 128) {
+    ZHessParams P;
+    P.W = nullptr;
+    P.W1 = A;
+    P.n1 = (int)n;
+    P.ld1 = lda;
+    P.n = nullptr;
+    P.order = nullptr;
+    P.off = nullptr;
+    P.count = 1;
+    P.nmax = (int)n;
+    P.counter = nullptr;
+    P.tau = tau;
+    P.ev = ev;
+    P.dvim = dvim;
+    CK(launch_zhess_cta(P, 1, h->stream));
+    return SKEW_OK;
+  }
+  CK(zhess_large(A, lda, (int)n, tau, ev, dvim, zws, h->stream));
+  return SKEW_OK;
+}
+
+static int zcheck(skew_handle_t h, const double* A, int64_t n, int64_t lda) {
+  if (!h || n < 0 || (n > 0 && (!A || lda < n))) return SKEW_BAD_ARG;
+  if (n > (1LL << 15)) return SKEW_UNSUPPORTED;
+  return SKEW_OK;
+}
+
+int skew_hessenberg_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev, double* dvim,
+                      int* info) {
+  int st = zcheck(h, A, n, lda);
+  if (st) return st;
+  if (n > 1 && (!tau || !ev)) return SKEW_BAD_ARG;
+  if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+  if (n == 0) return SKEW_OK;
+  ZLayout L;
+  st = zlayout(h, n, false, false, &L);
+  if (st) return st;
+  return zreduce(h, A, n, lda, n > 1 ? tau : L.tau, n > 1 ? ev : L.ev, dvim ? dvim : L.dvim, L.zws);
+}
+
+int skew_eigvals_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info) {
+  int st = zcheck(h, A, n, lda);
+  if (st) return st;
+  if (n > 0 && !vals_im) return SKEW_BAD_ARG;
+  if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+  if (n == 0) return SKEW_OK;
+  ZLayout L;
+  st = zlayout(h, n, false, false, &L);
+  if (st) return st;
+  st = zreduce(h, A, n, lda, L.tau, L.ev, L.dvim, L.zws);
+  if (st) return st;
+  CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, vals_im, nullptr, 0, L.ews, h->stream));
+  return SKEW_OK;
+}
+
+int skew_eigen_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* V, int64_t ldv,
+                 int* info) {
+  int st = zcheck(h, A, n, lda);
+  if (st) return st;
+  if (n > 0 && (!vals_im || !V || ldv < n)) return SKEW_BAD_ARG;
+  if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+  if (n == 0) return SKEW_OK;
+  ZLayout L;
+  st = zlayout(h, n, false, false, &L);
+  if (st) return st;
+  st = zreduce(h, A, n, lda, L.tau, L.ev, L.dvim, L.zws);
+  if (st) return st;
+  CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, vals_im, V, ldv, L.ews, h->stream));
+  return SKEW_OK;
+}
+
+static int zfunc(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* C, double* O, int64_t ldo,
+                 int mode, int* info) {
+  int st = zcheck(h, A, n, lda);
+  if (st) return st;
+  if (n > 0 && (!O || ldo < n || (mode == 1 && !C))) return SKEW_BAD_ARG;
+  if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+  if (n == 0) return SKEW_OK;
+  ZLayout L;
+  st = zlayout(h, n, true, true, &L);
+  if (st) return st;
+  st = zreduce(h, A, n, lda, L.tau, L.ev, L.dvim, L.zws);
+  if (st) return st;
+  CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, L.vals, L.V, n, L.ews, h->stream));
+  CK(zfunc_from_eigen(mode, (int)n, L.vals, L.V, n, C, n, O, ldo, L.fws, h->stream));
+  return SKEW_OK;
+}
+
+int skew_exp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, int64_t lde, int* info) {
+  return zfunc(h, A, n, lda, nullptr, E, lde, 0, info);
+}
+
+int skew_exp_vjp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* Cbar, double* G, int64_t ldg,
+                   int* info) {
+  return zfunc(h, A, n, lda, Cbar, G, ldg, 1, info);
+}
+
+// ---------------------------------------------------------------------------
 // FP64 peak probe
 // ---------------------------------------------------------------------------
 int skew_measure_fp64_peak(skew_handle_t h, double* tflops) {

@@ -94,10 +94,46 @@ cudaError_t launch_batch_trieig(const TrieigParams& P, cudaStream_t st);
 // symmetric tridiagonal; vals_im sorted descending.
 cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, double* scratch2, cudaStream_t st);
 
+// ComplexF64 Householder tridiagonalisation (skew_complex.cu).  Complex values are
+// interleaved (re, im).  Batched: W[b] (in place, ld n[b]), tau/ev/dvim at off[b];
+// single: W == nullptr and W1/n1/ld1 (off 0).  counter == nullptr: CTA b takes
+// matrix b (grid = count), else matrices come from the counter (largest first via order).
+struct ZHessParams {
+  double* const* W;
+  double* W1;
+  int n1;
+  int64_t ld1;
+  const int32_t* n;
+  const int32_t* order;
+  const int64_t* off;
+  int32_t count;
+  int nmax;
+  unsigned* counter;
+  double* tau;   // complex
+  double* ev;    // real subdiagonal
+  double* dvim;  // imag(diag) after the reduction, or null
+};
+size_t zhess_cta_smem_bytes(int nmax);
+cudaError_t launch_zhess_cta(const ZHessParams& P, int grid, cudaStream_t st);
+size_t zhess_large_ws_doubles(int n);
+cudaError_t zhess_large(double* A, int64_t lda, int n, double* tau, double* ev, double* dvim, double* ws,
+                        cudaStream_t st);
+// complex eigen from the reduced matrix; values descending (-mu, mu ascending), vectors Q D Y
+size_t zeigen_ws_doubles(int n);
+cudaError_t zeigen_from_tridiag(const double* A, int64_t lda, int n, const double* tau, const double* ev,
+                                const double* dvim, double* vals_im, double* V, int64_t ldv, double* ws,
+                                cudaStream_t st);
+// exp (mode 0: O = V e^{i mu} V^H) or its adjoint (mode 1: O = V (conj(Phi) o (V^H C V)) V^H)
+size_t zfunc_ws_doubles(int n);
+cudaError_t zfunc_from_eigen(int mode, int n, const double* vals_im, const double* V, int64_t ldv, const double* C,
+                             int64_t ldc, double* O, int64_t ldo, double* ws, cudaStream_t st);
+
 // Eigenvectors of one large skew matrix after the blocked reduction (skew_tdvec.cu):
 // vals (descending, from launch_tridiag_bisect) and its scratch bp (bound, pivmin);
 // A holds the reflectors, tau their scalars, ev the subdiagonal.  Vr, Vi (n x n, ldv).
 size_t large_eigen_ws_doubles(int n);
+cudaError_t symtri_vectors(const double* dg, const double* e, int n, const double* mu, const double* bp, double* Y,
+                           double* ws, cudaStream_t st);
 cudaError_t large_eigen_vectors(const double* A, int64_t lda, int n, const double* tau, const double* ev,
                                 const double* vals, const double* bp, double* Vr, double* Vi, int64_t ldv, double* ws,
                                 cudaStream_t st);

@@ -48,6 +48,8 @@ constexpr int RC = 32;     // rows per staged chunk
 struct TdvecLayout {
   int n, h, K, KP;  // n, positive eigenvalues, vectors (h + n odd), padded to 32
   int npan;         // WY panels
+  int full;         // 1: general symmetric tridiagonal (diagonal dg), one vector per eigenvalue (K = n)
+  const double* dg; // diagonal (full mode) or null (zero diagonal)
   double* dp;       // n x KP
   double* dm;       // n x KP
   double* z;        // n x KP
@@ -57,11 +59,13 @@ struct TdvecLayout {
   double* T;        // npan x WB x WB
 };
 
-static TdvecLayout layout(int n, double* ws) {
+static TdvecLayout layout(int n, double* ws, bool full = false, const double* dg = nullptr) {
   TdvecLayout L;
   L.n = n;
   L.h = n / 2;
-  L.K = L.h + (n & 1);
+  L.K = full ? n : L.h + (n & 1);
+  L.full = full ? 1 : 0;
+  L.dg = dg;
   L.KP = (L.K + 31) / 32 * 32;
   L.npan = (n - 2 + WB - 1) / WB;
   const size_t big = (size_t)n * L.KP;
@@ -76,7 +80,7 @@ static TdvecLayout layout(int n, double* ws) {
 }
 
 size_t large_eigen_ws_doubles(int n) {
-  const int h = n / 2, K = h + (n & 1), KP = (K + 31) / 32 * 32;
+  const int KP = (n + 31) / 32 * 32;  // covers both modes (K <= n)
   const int npan = (n - 2 + WB - 1) / WB;
   return 3 * (size_t)n * KP + KP + 2 * (size_t)KP * (LW + 1) + (size_t)std::max(npan, 1) * WB * WB + 64;
 }
@@ -90,27 +94,31 @@ __global__ void __launch_bounds__(TW_NT) twisted_kernel(const double* __restrict
   if (k >= L.KP) return;  // KP is a multiple of 32: whole warps leave together
   const int n = L.n;
   const int64_t KP = L.KP;
-  const double sig = (k < L.h) ? vals[k] : 0.0;  // padded lanes solve a dummy sigma = 0 vector
+  // sigma: the k-th eigenvalue (full mode: ascending list; skew mode: descending
+  // positive values, then 0 for odd n); padded lanes solve a dummy vector
+  const double sig = L.full ? (k < L.K ? vals[k] : vals[L.K - 1]) : ((k < L.h) ? vals[k] : 0.0);
   const double nsig = neg(sig);
   const double pivmin = bp[1];
+  const double* __restrict__ dg = L.dg;
+#define TW_DIAG(i) (dg ? dg[i] - sig : nsig)
   double* __restrict__ dp = L.dp;
   double* __restrict__ dm = L.dm;
   double* __restrict__ z = L.z;
 
   // pass 1: T - sigma I = L+ D+ L+^T, D+ stored
-  double d = nsig;
+  double d = TW_DIAG(0);
   for (int i = 0; i < n; i++) {
     if (fabs(d) <= pivmin) d = neg(pivmin);
     dp[(int64_t)i * KP + k] = d;
     if (i + 1 < n) {
       const double ei = e[i];
-      d = nsig - (ei * ei) / d;
+      d = TW_DIAG(i + 1) - (ei * ei) / d;
     }
   }
   // pass 2: T - sigma I = U- D- U-^T (bottom-up), D- stored; twist r = argmin |gamma|
   double best = INFINITY;
   int r = n - 1;
-  d = nsig;
+  d = TW_DIAG(n - 1);
   {
     double cur[TW_PF], nxt[TW_PF];
 #pragma unroll
@@ -127,14 +135,14 @@ __global__ void __launch_bounds__(TW_NT) twisted_kernel(const double* __restrict
         if (i >= 0) {
           if (fabs(d) <= pivmin) d = neg(pivmin);
           dm[(int64_t)i * KP + k] = d;
-          const double g = fabs(cur[j] + d + sig);  // gamma_i = D+_i + D-_i - (T_ii - sigma), T_ii = 0
+          const double g = fabs(cur[j] + d - TW_DIAG(i));  // gamma_i = D+_i + D-_i - (T_ii - sigma)
           if (g < best) {
             best = g;
             r = i;
           }
           if (i > 0) {
             const double ei = e[i - 1];
-            d = nsig - (ei * ei) / d;
+            d = TW_DIAG(i - 1) - (ei * ei) / d;
           }
         }
       }
@@ -214,6 +222,7 @@ __global__ void __launch_bounds__(TW_NT) twisted_kernel(const double* __restrict
     }
   }
   L.nrm2[k] = nrm;
+#undef TW_DIAG
 }
 
 // ---------------------------------------------------------------------------
@@ -346,6 +355,73 @@ __global__ void __launch_bounds__(LA_NT) lowdin_apply_kernel(TdvecLayout L, doub
       if (k < L.h) Vi[i + (int64_t)col * ldv] = o;
     }
   }
+}
+
+// Full mode: Y(:, k) = s_k z_k - 1/2 sum_d E(k, k+d) s_{k+d} z_{k+d}, with
+// s_k = 1/|z_k| and E the normalised Gram band over all rows.  Y is n x n, ld n.
+__global__ void __launch_bounds__(LA_NT) lowdin_full_kernel(TdvecLayout L, double* __restrict__ Y) {
+  __shared__ double zs[RC][LA_COLS + 1];
+  __shared__ double sc[LA_COLS];
+  __shared__ double eA[32][2 * LW + 1];
+  __shared__ double out[RC][33];
+  const int k0 = blockIdx.x * 32, i0 = blockIdx.y * RC;
+  const int n = L.n;
+  const int64_t KP = L.KP;
+  for (int c = threadIdx.x; c < LA_COLS; c += LA_NT) {
+    const int k = k0 - LW + c;
+    sc[c] = (k >= 0 && k < L.K) ? rsqrt(L.nrm2[k]) : 0.0;
+  }
+  for (int idx = threadIdx.x; idx < RC * LA_COLS; idx += LA_NT) {
+    const int rr = idx / LA_COLS, cc = idx - rr * LA_COLS;
+    const int i = i0 + rr, k = k0 - LW + cc;
+    zs[rr][cc] = (i < n && k >= 0 && k < L.K) ? L.z[(int64_t)i * KP + k] : 0.0;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < 32 * (2 * LW + 1); idx += LA_NT) {
+    const int kk = idx / (2 * LW + 1), dd = idx - kk * (2 * LW + 1) - LW;
+    const int k = k0 + kk, j = k + dd;
+    double u = 0.0;
+    if (k < L.K && j >= 0 && j < L.K) {
+      const int lo = min(k, j), off = abs(dd);
+      const double g = L.bandU[(int64_t)lo * (LW + 1) + off] + L.bandV[(int64_t)lo * (LW + 1) + off];
+      u = sc[kk + LW] * sc[kk + LW + dd] * g - (dd == 0 ? 1.0 : 0.0);
+    }
+    eA[kk][dd + LW] = u;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
+    const int kk = idx / RC, rr = idx - kk * RC;
+    const int i = i0 + rr, k = k0 + kk;
+    double o = 0.0;
+    if (i < n && k < L.K) {
+      double acc = sc[kk + LW] * zs[rr][kk + LW];
+#pragma unroll 11
+      for (int dd = -LW; dd <= LW; dd++) acc = fma(-0.5 * eA[kk][dd + LW], sc[kk + LW + dd] * zs[rr][kk + LW + dd], acc);
+      o = acc;
+    }
+    out[rr][kk] = o;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
+    const int kk = idx / RC, rr = idx - kk * RC;
+    const int i = i0 + rr, k = k0 + kk;
+    if (i < n && k < L.K) Y[i + (int64_t)k * n] = out[rr][kk];
+  }
+}
+
+// Eigenvectors of the symmetric tridiagonal with diagonal dg and off-diagonal e
+// for the ascending eigenvalues mu (bp: bound, pivmin), into Y (n x n, ld n).
+cudaError_t symtri_vectors(const double* dg, const double* e, int n, const double* mu, const double* bp, double* Y,
+                           double* ws, cudaStream_t st) {
+  const TdvecLayout L = layout(n, ws, true, dg);
+  twisted_kernel<<<L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), TW_NT, 0, st>>>(e, mu, bp, L);
+  cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  band_dots_kernel<<<L.KP / 32, BD_NT, 0, st>>>(L);
+  err = cudaGetLastError();
+  if (err != cudaSuccess) return err;
+  lowdin_full_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC), LA_NT, 0, st>>>(L, Y);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

@@ -285,6 +285,120 @@ def exp_rrule(A):
     return E, pullback
 
 
+# ---------------------------------------------------------------------------
+# ComplexF64 skew-Hermitian matrices
+# ---------------------------------------------------------------------------
+def to_device_complex(A, device="cuda") -> torch.Tensor:
+    """Host complex matrix -> device complex128 tensor holding it column-major."""
+    A = np.asarray(A, dtype=np.complex128)
+    return torch.from_numpy(np.ascontiguousarray(A.T)).to(device)
+
+
+def from_device_complex(T: torch.Tensor) -> np.ndarray:
+    return T.detach().cpu().numpy().T.copy()
+
+
+def _skew_hermitian_complex(A) -> torch.Tensor:
+    """A copy of A on the device after the reference constructor's check
+    A == -A^H (skewhermitian.jl:23-26)."""
+    if isinstance(A, torch.Tensor):
+        T = A.to(torch.complex128).cuda().clone()
+        if not bool(torch.equal(T, -T.conj().T)):
+            raise ValueError("Matrix is not skew-hermitian")
+        return T
+    A = np.asarray(A, dtype=np.complex128)
+    if A.ndim != 2 or A.shape[0] != A.shape[1] or not np.array_equal(A, -A.conj().T):
+        raise ValueError("Matrix is not skew-hermitian")
+    return to_device_complex(A)
+
+
+@dataclass
+class HessenbergComplex:
+    """hessenberg(A::SkewHermitian{ComplexF64}): factors (reflectors, column major,
+    complex128), tau (complex), the real subdiagonal ev and dvim = imag(diag(H))."""
+
+    factors: torch.Tensor
+    tau: torch.Tensor
+    ev: torch.Tensor
+    dvim: torch.Tensor
+
+    def H(self) -> np.ndarray:
+        e = self.ev.cpu().numpy()
+        d = self.dvim.cpu().numpy()
+        n = len(d)
+        T = np.diag(1j * d).astype(np.complex128)
+        T[np.arange(1, n), np.arange(n - 1)] = e
+        T[np.arange(n - 1), np.arange(1, n)] = -e
+        return T
+
+
+def hessenberg_complex(A) -> HessenbergComplex:
+    """LA.hessenberg(A::SkewHermitian{ComplexF64}) on the GPU (copy, reduce in place)."""
+    W = _skew_hermitian_complex(A)
+    n = W.shape[0]
+    tau = torch.zeros(max(n - 1, 0), dtype=torch.complex128, device="cuda")
+    ev = torch.zeros(max(n - 1, 0), dtype=torch.float64, device="cuda")
+    dvim = torch.zeros(n, dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_hessenberg_z(h, _ptr(W), n, n, _ptr(tau), _ptr(ev), _ptr(dvim), _ptr(info)),
+          "hessenberg_complex")
+    return HessenbergComplex(W, tau, ev, dvim)
+
+
+def eigvals_complex(A) -> np.ndarray:
+    """eigvals(A::SkewHermitian{ComplexF64}) (eigen.jl:18-27): 0 + i*vals, vals descending."""
+    W = _skew_hermitian_complex(A)
+    n = W.shape[0]
+    vals = torch.zeros(n, dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_eigvals_z(h, _ptr(W), n, n, _ptr(vals), _ptr(info)), "eigvals_complex")
+    return 1j * vals.cpu().numpy()
+
+
+def eigen_complex(A):
+    """eigen(A::SkewHermitian{ComplexF64}) (eigen.jl:101-106): (values, vectors)."""
+    W = _skew_hermitian_complex(A)
+    n = W.shape[0]
+    vals = torch.zeros(n, dtype=torch.float64, device="cuda")
+    V = torch.zeros((n, n), dtype=torch.complex128, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_eigen_z(h, _ptr(W), n, n, _ptr(vals), _ptr(V), n, _ptr(info)), "eigen_complex")
+    return 1j * vals.cpu().numpy(), from_device_complex(V)
+
+
+def exp_complex(A) -> np.ndarray:
+    """exp(A::SkewHermitian{ComplexF64}) (exp.jl:37-46)."""
+    W = _skew_hermitian_complex(A)
+    n = W.shape[0]
+    E = torch.zeros((n, n), dtype=torch.complex128, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_exp_z(h, _ptr(W), n, n, _ptr(E), n, _ptr(info)), "exp_complex")
+    return from_device_complex(E)
+
+
+def exp_complex_rrule(A):
+    """Forward exp(A) and a pullback Cbar -> G with dL = Re tr(G^H dA) for
+    L = Re tr(Cbar^H exp(A)) (Daleckii-Krein divided differences)."""
+    E = exp_complex(A)
+    Ah = np.asarray(A, dtype=np.complex128)
+
+    def pullback(Cbar) -> np.ndarray:
+        W = _skew_hermitian_complex(Ah)
+        n = W.shape[0]
+        Cd = to_device_complex(Cbar)
+        G = torch.zeros((n, n), dtype=torch.complex128, device="cuda")
+        info = _info_tensor()
+        h = handle().bind()
+        check(_lib.load().skew_exp_vjp_z(h, _ptr(W), n, n, _ptr(Cd), _ptr(G), n, _ptr(info)), "exp_vjp_complex")
+        return from_device_complex(G)
+
+    return E, pullback
+
+
 def measure_fp64_peak() -> float:
     t = ctypes.c_double()
     check(_lib.load().skew_measure_fp64_peak(handle().bind(), ctypes.byref(t)), "measure_fp64_peak")

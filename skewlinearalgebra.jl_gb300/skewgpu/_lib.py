@@ -50,6 +50,11 @@ SIGNATURES = {
     "skew_batch_cis_d": (_int, [_vp, _vp, _vp, _vp]),
     "skew_batch_exp_vjp_d": (_int, [_vp, _vp, _vp, _vp, _vp]),
     "skew_exp_vjp_d": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _i64, _vp]),
+    "skew_hessenberg_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp]),
+    "skew_eigvals_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp]),
+    "skew_eigen_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _i64, _vp]),
+    "skew_exp_z": (_int, [_vp, _vp, _i64, _i64, _vp, _i64, _vp]),
+    "skew_exp_vjp_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _i64, _vp]),
     "skew_measure_fp64_peak": (_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
 }
 
