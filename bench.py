@@ -190,7 +190,9 @@ def main():
         out = {"eigvals_batched": leg_eigvals_batched(plan, d_in, offs, sizes, max(1, args.steps)),
                "plain_n512": leg_plain_n512(peak, cpu=not args.no_cpu),
                "pfaffian_adjoint_1024x128": leg_pfaffian_adjoint(peak, max(1, args.steps)),
-               "exp_adjoint_512_mixed": leg_exp_adjoint(peak, max(1, min(args.steps, 3)))}
+               "exp_adjoint_512_mixed": leg_exp_adjoint(peak, max(1, min(args.steps, 3))),
+               "exp_adjoint_complex_64x256": leg_complex_exp_adjoint(peak),
+               "complex_n4096": leg_complex_large(4096, peak)}
         plan.close()
         print(json.dumps({"legs": out}), flush=True)
         return 0
@@ -372,6 +374,8 @@ def main():
         legs["plain_n512"] = leg_plain_n512(fp64_peak, cpu=not args.no_cpu)
         legs["pfaffian_adjoint_1024x128"] = leg_pfaffian_adjoint(fp64_peak, args.steps)
         legs["exp_adjoint_512_mixed"] = leg_exp_adjoint(fp64_peak, max(1, min(args.steps, 3)))
+        legs["exp_adjoint_complex_64x256"] = leg_complex_exp_adjoint(fp64_peak)
+        legs["complex_n4096"] = leg_complex_large(4096, fp64_peak)
 
     if rank == 0:
         line = {
@@ -505,6 +509,111 @@ def leg_eigen_large(n, fp64_peak, reps=1):
     return {"n": n, "ms": sec * 1e3, "algorithmic_flops": flops, "gflops": flops / sec / 1e9,
             "frac_fp64": flops / sec / 1e12 / fp64_peak, "reps": reps,
             "check_sample": {"pairs": 16, "max_residual_rel": res, "max_orthonormality_err": orth}}
+
+
+def leg_complex_large(n, fp64_peak, reps=1):
+    """One ComplexF64 skew-Hermitian n x n matrix, A = (C - C^H)/2 with re/im of C
+    iid N(0,1): hessenberg (skew_hessenberg_z) and eigen with vectors
+    (skew_eigen_z), each timed with CUDA events, input restored outside the timed
+    region; eigen checked on 16 sampled pairs."""
+    import ctypes
+
+    import torch
+
+    import skewgpu
+
+    rng = np.random.default_rng(SEED + 3 * n)
+    C = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    A = (C - C.conj().T) / 2
+    del C
+    pristine = skewgpu.to_device_complex(A)
+    work = torch.empty_like(pristine)
+    tau = torch.empty(n - 1, dtype=torch.complex128, device="cuda")
+    ev = torch.empty(n - 1, dtype=torch.float64, device="cuda")
+    dvim = torch.empty(n, dtype=torch.float64, device="cuda")
+    vals = torch.empty(n, dtype=torch.float64, device="cuda")
+    V = torch.empty((n, n), dtype=torch.complex128, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    L = skewgpu._lib.load()
+    h = skewgpu.handle().bind()
+    stream = torch.cuda.current_stream()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+    calls = {
+        "hessenberg": lambda: L.skew_hessenberg_z(h, P(work), n, n, P(tau), P(ev), P(dvim), P(info)),
+        "eigen": lambda: L.skew_eigen_z(h, P(work), n, n, P(vals), P(V), n, P(info)),
+    }
+    res = {"n": n}
+    for name, fn in calls.items():
+        times = []
+        for r in range(reps + 1):
+            work.copy_(pristine)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            assert fn() == 0
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r:
+                times.append(e0.elapsed_time(e1))
+        res[f"{name}_ms"] = float(np.median(times))
+    flops_h = 16.0 / 3.0 * n ** 3  # complex reduction in real flops
+    res["hessenberg_gflops"] = flops_h / (res["hessenberg_ms"] / 1e3) / 1e9
+    res["hessenberg_frac_fp64"] = res["hessenberg_gflops"] / 1e3 / fp64_peak
+    At = pristine.T  # device buffer holds A^T (column-major A)
+    idx = torch.tensor(np.sort(rng.choice(n, 16, replace=False)), device="cuda")
+    Vs = V.T[:, idx]
+    lam = 1j * vals[idx]
+    r = (At @ Vs - Vs * lam).abs().max().item() / vals.abs().max().item()
+    o = (Vs.conj().T @ Vs - torch.eye(16, dtype=Vs.dtype, device="cuda")).abs().max().item()
+    res["check_sample"] = {"pairs": 16, "max_residual_rel": r, "max_orthonormality_err": o}
+    return res
+
+
+def leg_complex_exp_adjoint(fp64_peak, count=64, n=256):
+    """The exp-adjoint workload's complex part: 64 ComplexF64 skew-Hermitian
+    matrices, n = 256, scaled to a spectral radius ~ U(0.5, 8), cotangents iid
+    complex N(0,1); G_i through skew_exp_vjp_z, one call per matrix on one stream
+    (no batched complex entry point)."""
+    import ctypes
+
+    import torch
+
+    import skewgpu
+
+    rng = np.random.default_rng(SEED + 64)
+    mats, cots = [], []
+    for _ in range(count):
+        C = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        A = (C - C.conj().T) / 2
+        A *= rng.uniform(0.5, 8.0) / np.abs(np.linalg.eigvalsh(1j * A)).max()
+        mats.append(skewgpu.to_device_complex(A))
+        cots.append(skewgpu.to_device_complex(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))))
+    work = [torch.empty_like(m) for m in mats]
+    outs = [torch.empty_like(m) for m in mats]
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    L = skewgpu._lib.load()
+    h = skewgpu.handle().bind()
+    stream = torch.cuda.current_stream()
+    P = lambda t, off=0: ctypes.c_void_p(t.data_ptr() + off)  # noqa: E731
+
+    def run():
+        for k in range(count):
+            work[k].copy_(mats[k])
+            assert L.skew_exp_vjp_z(h, P(work[k]), n, n, P(cots[k]), P(outs[k]), n, P(info, 4 * k)) == 0
+
+    run()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    run()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3
+    # reduction 16/3 n^3 + back-transformation 8 n^3 + four complex products 32 n^3 (real flops)
+    flops = count * (16.0 / 3.0 + 8.0 + 32.0) * n ** 3
+    return {"value": count / sec, "unit": "matrices/s", "ms_per_step": sec * 1e3, "count": count, "n": n,
+            "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
+            "note": "looped single-matrix calls (input copy inside the timed region)"}
 
 
 def _time_events(fn, reps, stream):
@@ -717,7 +826,7 @@ def leg_exp_adjoint(fp64_peak, steps, count=512):
     return {"value": count / sec, "unit": "matrices/s", "ms_per_step": sec * 1e3, "steps": steps,
             "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
             "status_ok": int((s == 0).sum()), "status_fallback": int((s == 8).sum()),
-            "complex_part": "the 64 ComplexF64 n=256 matrices of this workload are not built (complex eigen)"}
+            "complex_part": "reported separately as exp_adjoint_complex_64x256"}
 
 
 def _bucket_ids(sizes):

@@ -130,3 +130,51 @@ __device__ __forceinline__ bool spin_until_geq(const volatile unsigned* flag, un
 }
 
 }  // namespace skew
+
+namespace skew {
+
+// Multisection for the target-th smallest eigenvalue (0-based) of a symmetric
+// tridiagonal, given count(x) = number of eigenvalues smaller than x (Sturm).
+// Groups of p lanes (p a power of two, p <= 32) share one eigenvalue: each step
+// the p lanes count at p interior points of [lo, hi] and the group keeps the
+// sub-interval [x_{j-1}, x_j] where x_j is the first point whose count exceeds
+// the target, so the bracket count(lo) <= target < count(hi) holds by
+// construction.  The interval shrinks (p+1)-fold per step until it is below
+// max(2 eps max(|lo|, |hi|), abstol).  All 32 lanes of the warp must call this
+// (active = false for a group with nothing to find).  Returns the midpoint.
+template <class Count>
+__device__ double group_multisect(double lo, double hi, int target, double abstol, int p, bool active, Count count) {
+  const int lane = threadIdx.x & 31;
+  const int g = lane / p, gl = lane - g * p;
+  const unsigned gmask = (p == 32) ? 0xffffffffu : (((1u << p) - 1u) << (g * p));
+  const double inv = 1.0 / (double)(p + 1);
+  bool run = active;
+  for (int it = 0; it < 256; it++) {
+    const double w = hi - lo;
+    if (run && !(w > fmax(2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)), abstol))) run = false;
+    if (!__any_sync(0xffffffffu, run)) break;
+    const double x = lo + w * ((double)(gl + 1) * inv);
+    const bool below = run ? (count(x) <= target) : true;
+    const unsigned bits = __ballot_sync(0xffffffffu, below) & gmask;
+    if (run) {
+      const unsigned above = ~bits & gmask;  // points whose count exceeds the target
+      const int j = above ? (__ffs(above) - 1 - g * p) : p;  // first such point (p: none)
+      const double nlo = (j == 0) ? lo : lo + w * ((double)j * inv);
+      const double nhi = (j == p) ? hi : lo + w * ((double)(j + 1) * inv);
+      lo = nlo;
+      hi = nhi;
+    }
+  }
+  return 0.5 * (lo + hi);
+}
+
+// lanes per eigenvalue for m eigenvalues on a GPU with `sms` SMs: enough groups
+// to give every SM sub-partition a warp, at most a warp per eigenvalue
+__host__ __device__ inline int multisect_lanes(int m, int sms) {
+  const long long want = (long long)sms * 4 * 32 / (m > 0 ? m : 1);
+  int p = 1;
+  while (p < 32 && 2LL * p <= want) p *= 2;
+  return p;
+}
+
+}  // namespace skew

@@ -473,23 +473,21 @@ __device__ int zsturm(const double* dg, const double* off, int n, double x, doub
   return c;
 }
 
-// mu_k = k-th smallest eigenvalue of S (one thread each); vals_im[k] = -mu_k
+// mu_k = k-th smallest eigenvalue of S by a group of p lanes (multisection,
+// absolute tolerance eps * max|Gershgorin bound|); vals_im[k] = -mu_k
 __global__ void zbisect_kernel(const double* __restrict__ dg, const double* __restrict__ off, int n,
-                               const double* __restrict__ bp, double* __restrict__ mu, double* __restrict__ vals_im) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= n) return;
-  double lo = bp[0], hi = bp[2];
-  const double pivmin = bp[1];
-  for (int it = 0; it < 200 && hi - lo > 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)) + 1e-300; it++) {
-    const double mid = 0.5 * (lo + hi);
-    if (zsturm(dg, off, n, mid, pivmin) <= k)
-      lo = mid;
-    else
-      hi = mid;
+                               const double* __restrict__ bp, double* __restrict__ mu, double* __restrict__ vals_im,
+                               int p) {
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) / p;
+  const int gl = (threadIdx.x & 31) % p;
+  const double lo = bp[0], hi = bp[2], pivmin = bp[1];
+  const bool active = k < n;
+  const double x = group_multisect(lo, hi, active ? k : 0, 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)), p,
+                                   active, [&](double y) { return zsturm(dg, off, n, y, pivmin); });
+  if (active && gl == 0) {
+    if (mu) mu[k] = x;
+    vals_im[k] = neg(x);
   }
-  const double m = 0.5 * (lo + hi);
-  if (mu) mu[k] = m;
-  vals_im[k] = neg(m);
 }
 
 // V(:, k) = D Y(:, k)
@@ -667,7 +665,11 @@ cudaError_t zeigen_from_tridiag(const double* Ad, int64_t lda, int n, const doub
   zc* Tg = reinterpret_cast<zc*>(Y + seg((size_t)n * n));
   double* tws = Y + seg((size_t)n * n) + seg(2 * (size_t)std::max(npan, 1) * ZWB * ZWB);
   zprep_kernel<<<1, 1024, 0, st>>>(ev, dvim, n, dg, off, ph, bp);
-  zbisect_kernel<<<(n + 127) / 128, 128, 0, st>>>(dg, off, n, bp, mu, vals_im);
+  int dev = 0, sms = 148;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int p = multisect_lanes(n, sms);
+  const long long threads = ((long long)n * p + 31) / 32 * 32;
+  zbisect_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(dg, off, n, bp, mu, vals_im, p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || !Vd) return e;
   e = symtri_vectors(dg, off, n, mu, bp, Y, tws, st);

@@ -18,6 +18,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "skew_common.cuh"
 #include "skew_internal.h"
 
@@ -280,35 +282,35 @@ __global__ void bisect_prep_kernel(const double* __restrict__ e, int n, double* 
   }
 }
 
-// One positive eigenvalue per thread: the k-th largest of SymTridiagonal(0, e).
+// The positive eigenvalues of SymTridiagonal(0, e): the k-th largest (k < n/2) by
+// a group of p lanes (multisection, absolute tolerance eps * bound); vals[k] and
+// vals[n-1-k] = -vals[k] written together; odd n: vals[n/2] = 0.
 __global__ void bisect_kernel_dev(const double* __restrict__ e, int n, const double* __restrict__ bp,
-                                  double* __restrict__ vals) {
+                                  double* __restrict__ vals, int p) {
   const int h = n / 2;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= h) {
-    if (k == h && (n & 1)) vals[h] = 0.0;
-    return;
-  }
+  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / p;  // eigenvalue index of the lane's group
+  const int gl = (threadIdx.x & 31) % p;
+  if ((n & 1) && gid == 0 && gl == 0 && blockIdx.x == 0) vals[h] = 0.0;
   const double bound = bp[0], pivmin = bp[1];
-  double lo = 0.0, hi = bound;
-  for (int it = 0; it < 120 && hi - lo > 2.220446049250313e-16 * hi + 1e-300; it++) {
-    const double mid = 0.5 * (lo + hi);
-    if (sturm_count(e, n, mid, pivmin) <= n - 1 - k)
-      lo = mid;
-    else
-      hi = mid;
+  const bool active = gid < h;
+  const double x = group_multisect(0.0, bound, n - 1 - (active ? gid : 0), 2.220446049250313e-16 * bound, p,
+                                   active, [&](double y) { return sturm_count(e, n, y, pivmin); });
+  if (active && gl == 0) {
+    vals[gid] = x;
+    vals[n - 1 - gid] = neg(x);
   }
-  const double x = 0.5 * (lo + hi);
-  vals[k] = x;
-  vals[n - 1 - k] = neg(x);
 }
 
 cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, double* scratch2, cudaStream_t st) {
   if (n <= 0) return cudaSuccess;
   bisect_prep_kernel<<<1, 256, 0, st>>>(ev, n, scratch2);
-  const int h = n / 2 + 1;
+  int dev = 0, sms = 148;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int h = n / 2;
+  const int p = multisect_lanes(h, sms);
+  const long long threads = ((long long)std::max(h, 1) * p + 31) / 32 * 32;
   const int bs = 128;
-  bisect_kernel_dev<<<(h + bs - 1) / bs, bs, 0, st>>>(ev, n, scratch2, vals_im);
+  bisect_kernel_dev<<<(unsigned)((threads + bs - 1) / bs), bs, 0, st>>>(ev, n, scratch2, vals_im, p);
   return cudaGetLastError();
 }
 
