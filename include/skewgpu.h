@@ -183,6 +183,19 @@ SKEW_API int skew_exp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, doub
 SKEW_API int skew_exp_vjp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* Cbar, double* G,
                             int64_t ldg, int* info);
 
+/* Batched ComplexF64 of one size: `count` skew-Hermitian n x n matrices stored back to
+ * back (matrix b at A + 2 n^2 b doubles, column-major, leading dimension n), read only;
+ * outputs laid out the same way.  n <= 1024 (else SKEW_UNSUPPORTED).  status[count]
+ * (may be NULL) receives SKEW_OK per matrix.
+ * eigen: vals_im (count x n, descending per matrix) and V (count x n x n). */
+SKEW_API int skew_batch_eigen_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* vals_im,
+                                double* V, int* status);
+/* exp for every matrix (exp.jl:37-46): E (count x n x n ComplexF64). */
+SKEW_API int skew_batch_exp_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* E, int* status);
+/* Adjoint of exp for every matrix: G_b = V_b (conj(Phi_b) o (V_b^H Cbar_b V_b)) V_b^H. */
+SKEW_API int skew_batch_exp_vjp_z(skew_handle_t h, const double* A, int64_t n, int64_t count, const double* Cbar,
+                                  double* G, int* status);
+
 /* Diagnostics: measured FP64 DFMA throughput of the current device in TFLOP/s
  * (runs a short microbenchmark on the handle's stream and synchronizes). */
 SKEW_API int skew_measure_fp64_peak(skew_handle_t h, double* tflops);

@@ -810,26 +810,30 @@ int skew_exp_vjp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, const dou
 // ---------------------------------------------------------------------------
 // ComplexF64 skew-Hermitian matrices (skew_complex.cu)
 // ---------------------------------------------------------------------------
-// Workspace of the complex calls: [reduction ws][ev (n)][tau (2n)][dvim (n)]
-// [vals (n)][V (2 n^2, eigen/exp)][eigen ws][function ws].
+// Workspace of the complex calls (B matrices of size n): [reduction ws][working
+// copy (batched: 2 B n^2)][ev (B n)][tau (2 B n)][dvim (B n)][vals (B n + 8)]
+// [V (2 B n^2, exp / adjoint)][eigen ws][function ws].
 struct ZLayout {
-  double *zws, *ev, *tau, *dvim, *vals, *V, *ews, *fws;
+  double *zws, *W, *ev, *tau, *dvim, *vals, *V, *ews, *fws;
 };
 
-static int zlayout(skew_handle_t h, int64_t n, bool vecs, bool func, ZLayout* L) {
+static int zlayout(skew_handle_t h, int64_t n, int64_t B, bool copy, bool vecs, bool func, ZLayout* L) {
   // every segment a multiple of 32 doubles: complex arrays stay 16-byte aligned
   auto seg = [](size_t d) { return (d + 31) & ~(size_t)31; };
-  const size_t zr = seg(zhess_large_ws_doubles((int)n));
-  const size_t ze = seg(zeigen_ws_doubles((int)n));
-  const size_t zf = func ? seg(zfunc_ws_doubles((int)n)) : 0;
-  const size_t nv = vecs ? seg(2 * (size_t)n * n) : 0;
-  const size_t sn = seg(n), s2n = seg(2 * (size_t)n), sv = seg(n + 8);
-  const size_t total = zr + sn + s2n + sn + sv + nv + ze + zf + 64;
+  const size_t zr = B == 1 ? seg(zhess_large_ws_doubles((int)n)) : 0;
+  const size_t zw = copy ? seg(2 * (size_t)B * n * n) : 0;
+  const size_t ze = seg(zeigen_ws_doubles((int)n, (int)B));
+  const size_t zf = func ? seg(zfunc_ws_doubles((int)n, (int)B)) : 0;
+  const size_t nv = vecs ? seg(2 * (size_t)B * n * n) : 0;
+  const size_t sn = seg((size_t)B * n), s2n = seg(2 * (size_t)B * n), sv = seg((size_t)B * n + 8);
+  const size_t total = zr + zw + sn + s2n + sn + sv + nv + ze + zf + 64;
   int st = ensure_ws(h, sizeof(double) * total);
   if (st) return st;
   double* p = (double*)h->ws;
   L->zws = p;
   p += zr;
+  L->W = copy ? p : nullptr;
+  p += zw;
   L->ev = p;
   p += sn;
   L->tau = p;
@@ -846,25 +850,27 @@ static int zlayout(skew_handle_t h, int64_t n, bool vecs, bool func, ZLayout* L)
   return SKEW_OK;
 }
 
-// complex reduction in place: one CTA for small n, per-column multi-CTA kernels above
-static int zreduce(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev, double* dvim,
-                   double* zws) {
-  if (n <= 128) {
+// complex reduction in place.  One matrix: one CTA for n <= 128, per-column
+// multi-CTA kernels above.  B > 1 matrices of size n, n^2 apart: one CTA each.
+static int zreduce(skew_handle_t h, double* A, int64_t n, int64_t lda, int64_t B, double* tau, double* ev,
+                   double* dvim, double* zws) {
+  if (B > 1 || n <= 128) {
     ZHessParams P;
     P.W = nullptr;
     P.W1 = A;
     P.n1 = (int)n;
     P.ld1 = lda;
+    P.stride = lda * n;
     P.n = nullptr;
     P.order = nullptr;
     P.off = nullptr;
-    P.count = 1;
+    P.count = (int32_t)B;
     P.nmax = (int)n;
     P.counter = nullptr;
     P.tau = tau;
     P.ev = ev;
     P.dvim = dvim;
-    CK(launch_zhess_cta(P, 1, h->stream));
+    CK(launch_zhess_cta(P, (int)B, h->stream));
     return SKEW_OK;
   }
   CK(zhess_large(A, lda, (int)n, tau, ev, dvim, zws, h->stream));
@@ -885,9 +891,9 @@ int skew_hessenberg_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double
   if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
   if (n == 0) return SKEW_OK;
   ZLayout L;
-  st = zlayout(h, n, false, false, &L);
+  st = zlayout(h, n, 1, false, false, false, &L);
   if (st) return st;
-  return zreduce(h, A, n, lda, n > 1 ? tau : L.tau, n > 1 ? ev : L.ev, dvim ? dvim : L.dvim, L.zws);
+  return zreduce(h, A, n, lda, 1, n > 1 ? tau : L.tau, n > 1 ? ev : L.ev, dvim ? dvim : L.dvim, L.zws);
 }
 
 int skew_eigvals_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info) {
@@ -897,11 +903,11 @@ int skew_eigvals_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* v
   if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
   if (n == 0) return SKEW_OK;
   ZLayout L;
-  st = zlayout(h, n, false, false, &L);
+  st = zlayout(h, n, 1, false, false, false, &L);
   if (st) return st;
-  st = zreduce(h, A, n, lda, L.tau, L.ev, L.dvim, L.zws);
+  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws);
   if (st) return st;
-  CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, vals_im, nullptr, 0, L.ews, h->stream));
+  CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, vals_im, nullptr, 0, L.ews, 1, h->stream));
   return SKEW_OK;
 }
 
@@ -913,11 +919,11 @@ int skew_eigen_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* val
   if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
   if (n == 0) return SKEW_OK;
   ZLayout L;
-  st = zlayout(h, n, false, false, &L);
+  st = zlayout(h, n, 1, false, false, false, &L);
   if (st) return st;
-  st = zreduce(h, A, n, lda, L.tau, L.ev, L.dvim, L.zws);
+  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws);
   if (st) return st;
-  CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, vals_im, V, ldv, L.ews, h->stream));
+  CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, vals_im, V, ldv, L.ews, 1, h->stream));
   return SKEW_OK;
 }
 
@@ -929,12 +935,12 @@ static int zfunc(skew_handle_t h, double* A, int64_t n, int64_t lda, const doubl
   if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
   if (n == 0) return SKEW_OK;
   ZLayout L;
-  st = zlayout(h, n, true, true, &L);
+  st = zlayout(h, n, 1, false, true, true, &L);
   if (st) return st;
-  st = zreduce(h, A, n, lda, L.tau, L.ev, L.dvim, L.zws);
+  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws);
   if (st) return st;
-  CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, L.vals, L.V, n, L.ews, h->stream));
-  CK(zfunc_from_eigen(mode, (int)n, L.vals, L.V, n, C, n, O, ldo, L.fws, h->stream));
+  CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, L.vals, L.V, n, L.ews, 1, h->stream));
+  CK(zfunc_from_eigen(mode, (int)n, L.vals, L.V, n, C, n, O, ldo, L.fws, 1, h->stream));
   return SKEW_OK;
 }
 
@@ -945,6 +951,42 @@ int skew_exp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, in
 int skew_exp_vjp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* Cbar, double* G, int64_t ldg,
                    int* info) {
   return zfunc(h, A, n, lda, Cbar, G, ldg, 1, info);
+}
+
+// Batched ComplexF64 of one size: count matrices n^2 apart (inputs read only).
+static int zbatch(skew_handle_t h, const double* A, int64_t n, int64_t count, double* vals_im, double* V,
+                  const double* C, double* O, int mode, int* status) {
+  if (!h || n < 0 || count < 0 || (count > 0 && n > 0 && !A)) return SKEW_BAD_ARG;
+  if (n > 1024) return SKEW_UNSUPPORTED;
+  if (count == 0 || n == 0) return SKEW_OK;
+  if (mode < 0 && (!vals_im || !V)) return SKEW_BAD_ARG;
+  if (mode >= 0 && (!O || (mode == 1 && !C))) return SKEW_BAD_ARG;
+  if (status) CK(cudaMemsetAsync(status, 0, sizeof(int) * count, h->stream));
+  ZLayout L;
+  int st = zlayout(h, n, count, true, mode >= 0, mode >= 0, &L);
+  if (st) return st;
+  CK(cudaMemcpyAsync(L.W, A, sizeof(double) * 2 * (size_t)count * n * n, cudaMemcpyDeviceToDevice, h->stream));
+  st = zreduce(h, L.W, n, n, count, L.tau, L.ev, L.dvim, L.zws);
+  if (st) return st;
+  double* vv = mode < 0 ? vals_im : L.vals;
+  double* VV = mode < 0 ? V : L.V;
+  CK(zeigen_from_tridiag(L.W, n, (int)n, L.tau, L.ev, L.dvim, vv, VV, n, L.ews, (int)count, h->stream));
+  if (mode >= 0) CK(zfunc_from_eigen(mode, (int)n, vv, VV, n, C, n, O, n, L.fws, (int)count, h->stream));
+  return SKEW_OK;
+}
+
+int skew_batch_eigen_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* vals_im, double* V,
+                       int* status) {
+  return zbatch(h, A, n, count, vals_im, V, nullptr, nullptr, -1, status);
+}
+
+int skew_batch_exp_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* E, int* status) {
+  return zbatch(h, A, n, count, nullptr, nullptr, nullptr, E, 0, status);
+}
+
+int skew_batch_exp_vjp_z(skew_handle_t h, const double* A, int64_t n, int64_t count, const double* Cbar, double* G,
+                         int* status) {
+  return zbatch(h, A, n, count, nullptr, nullptr, Cbar, G, 1, status);
 }
 
 // ---------------------------------------------------------------------------

@@ -89,11 +89,11 @@ __global__ void __launch_bounds__(ZNT) zhess_cta_kernel(ZHessParams P) {
     __syncthreads();
     if (t >= P.count) break;
     const int b = P.order ? P.order[t] : t;
-    const bool one = (P.W == nullptr);  // single matrix given directly
+    const bool one = (P.W == nullptr);  // matrices given directly: W1 + b * stride
     const int n = one ? P.n1 : P.n[b];
     const int64_t ld = one ? P.ld1 : n;
-    const int64_t off = one ? 0 : P.off[b];
-    zc* W = reinterpret_cast<zc*>(one ? P.W1 : P.W[b]);
+    const int64_t off = one ? (int64_t)b * P.n1 : P.off[b];
+    zc* W = one ? reinterpret_cast<zc*>(P.W1) + (int64_t)b * P.stride : reinterpret_cast<zc*>(P.W[b]);
     zc* tau = reinterpret_cast<zc*>(P.tau) + off;
     double* ev = P.ev + off;
     for (int c = 0; c + 1 < n; c++) {
@@ -382,6 +382,7 @@ cudaError_t zhess_large(double* Ad, int64_t lda, int n, double* taud, double* ev
   P.W1 = reinterpret_cast<double*>(A + c0 + (int64_t)c0 * lda);
   P.n1 = n - c0;
   P.ld1 = lda;
+  P.stride = 0;
   P.n = nullptr;
   P.off = nullptr;
   P.order = nullptr;
@@ -413,6 +414,13 @@ cudaError_t zhess_large(double* Ad, int64_t lda, int n, double* taud, double* ev
 __global__ void __launch_bounds__(1024) zprep_kernel(const double* __restrict__ ev, const double* __restrict__ dvim,
                                                     int n, double* __restrict__ dg, double* __restrict__ off,
                                                     zc* __restrict__ ph, double* __restrict__ bp) {
+  const size_t mb = blockIdx.x;  // problem of a batch: arrays n (bp: 8) apart
+  ev += mb * n;
+  dvim += mb * n;
+  dg += mb * n;
+  off += mb * n;
+  ph += mb * n;
+  bp += mb * 8;
   __shared__ double red[3][32];
   double lo = INFINITY, hi = -INFINITY, e2 = 0.0;
   for (int i = threadIdx.x; i < n; i += blockDim.x) {
@@ -475,24 +483,33 @@ __device__ int zsturm(const double* dg, const double* off, int n, double x, doub
 
 // mu_k = k-th smallest eigenvalue of S by a group of p lanes (multisection,
 // absolute tolerance eps * max|Gershgorin bound|); vals_im[k] = -mu_k
-__global__ void zbisect_kernel(const double* __restrict__ dg, const double* __restrict__ off, int n,
+__global__ void zbisect_kernel(const double* __restrict__ dg, const double* __restrict__ off, int n, int batch,
                                const double* __restrict__ bp, double* __restrict__ mu, double* __restrict__ vals_im,
                                int p) {
-  const int k = (blockIdx.x * blockDim.x + threadIdx.x) / p;
+  const long long gid = ((long long)blockIdx.x * blockDim.x + threadIdx.x) / p;
   const int gl = (threadIdx.x & 31) % p;
+  const bool active = gid < (long long)n * batch;
+  const size_t mb = active ? (size_t)(gid / n) : 0;
+  const int k = active ? (int)(gid - (long long)mb * n) : 0;
+  dg += mb * n;
+  off += mb * n;
+  bp += mb * 8;
   const double lo = bp[0], hi = bp[2], pivmin = bp[1];
-  const bool active = k < n;
   const double x = group_multisect(lo, hi, active ? k : 0, 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)), p,
                                    active, [&](double y) { return zsturm(dg, off, n, y, pivmin); });
   if (active && gl == 0) {
-    if (mu) mu[k] = x;
-    vals_im[k] = neg(x);
+    if (mu) mu[mb * n + k] = x;
+    vals_im[mb * n + k] = neg(x);
   }
 }
 
 // V(:, k) = D Y(:, k)
 __global__ void zassemble_kernel(const double* __restrict__ Y, const zc* __restrict__ ph, int n, zc* __restrict__ V,
                                  int64_t ldv) {
+  const size_t mb = blockIdx.z;  // problem mb: Y, V n^2 (V: ldv n) apart, ph n apart
+  Y += mb * n * n;
+  ph += mb * n;
+  V += mb * (size_t)ldv * n;
   const int k = blockIdx.y;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const double y = Y[i + (int64_t)k * n];
@@ -517,6 +534,10 @@ __global__ void __launch_bounds__(256) zwy_factor_kernel(const zc* __restrict__ 
                                                          const zc* __restrict__ tau, int n, zc* __restrict__ Tg) {
   __shared__ zc Vs[16][ZWB + 1];
   __shared__ zc M[ZWB][ZWB + 1];  // lower: G = V^H V, upper + diagonal: T
+  const size_t mb = blockIdx.y;   // problem mb: A lda*n, tau n, T gridDim.x panels apart
+  A += mb * (size_t)lda * n;
+  tau += mb * n;
+  Tg += mb * gridDim.x * (size_t)ZWB * ZWB;
   const int b = blockIdx.x;
   const int c0 = b * ZWB, c1 = min(c0 + ZWB, n - 1), nb = c1 - c0;
   const int ty = threadIdx.x >> 4, tx = threadIdx.x & 15;  // G (32 x 32): 2 x 2 per thread
@@ -570,6 +591,11 @@ __global__ void __launch_bounds__(256) zback_strip_kernel(const zc* __restrict__
   __shared__ zc Ws[ZWB][ZSW + 1];
   __shared__ zc Vs[ZRC][ZWB + 1];
   __shared__ zc Xs[ZRC][ZSW + 1];
+  const size_t mb = blockIdx.y;  // problem mb: A lda*n, tau n, T npan panels, X ldx*ncols apart
+  A += mb * (size_t)lda * n;
+  tau += mb * n;
+  Tg += mb * (size_t)npan * ZWB * ZWB;
+  X += mb * (size_t)ldx * ncols;
   const int col0 = blockIdx.x * ZSW;
   const int ncol = min(ZSW, ncols - col0);
   X += (int64_t)col0 * ldx;
@@ -639,49 +665,51 @@ __global__ void __launch_bounds__(256) zback_strip_kernel(const zc* __restrict__
 // workspace segments are rounded to 32 doubles so that every complex array is 16-byte aligned
 static inline size_t seg(size_t d) { return (d + 31) & ~(size_t)31; }
 
-size_t zeigen_ws_doubles(int n) {
+size_t zeigen_ws_doubles(int n, int batch) {
   const int npan = (n - 1 + ZWB - 1) / ZWB;
-  return 3 * seg(n)                      // dg, off, mu
-         + seg(2 * (size_t)n)            // phases
-         + seg(8)                        // bp
-         + seg((size_t)n * n)            // Y
-         + seg(2 * (size_t)std::max(npan, 1) * ZWB * ZWB)  // T factors
-         + large_eigen_ws_doubles(n) + 64;
+  const size_t B = (size_t)(batch > 0 ? batch : 1);
+  return 3 * seg(B * n)                      // dg, off, mu
+         + seg(2 * B * n)                    // phases
+         + seg(8 * B)                        // bp
+         + seg(B * n * n)                    // Y
+         + seg(2 * B * std::max(npan, 1) * ZWB * ZWB)  // T factors
+         + B * large_eigen_ws_doubles(n) + 64;
 }
 
-// Eigen-decomposition of the reduced matrix (A holds the reflectors, tau, ev,
-// dvim from the reduction): vals_im (descending) and, if V != null, the
-// eigenvectors V (n x n complex, ldv).
+// Eigen-decomposition of `batch` reduced matrices of size n (A: the reflectors,
+// lda*n apart; tau, ev, dvim, vals_im n apart): vals_im (descending) and, if
+// V != null, the eigenvectors V (ldv*n apart).
 cudaError_t zeigen_from_tridiag(const double* Ad, int64_t lda, int n, const double* taud, const double* ev,
-                                const double* dvim, double* vals_im, double* Vd, int64_t ldv, double* ws,
+                                const double* dvim, double* vals_im, double* Vd, int64_t ldv, double* ws, int batch,
                                 cudaStream_t st) {
   const int npan = (n - 1 + ZWB - 1) / ZWB;
+  const size_t B = (size_t)batch;
   double* dg = ws;
-  double* off = dg + seg(n);
-  double* mu = off + seg(n);
-  zc* ph = reinterpret_cast<zc*>(mu + seg(n));
-  double* bp = mu + seg(n) + seg(2 * (size_t)n);
-  double* Y = bp + seg(8);
-  zc* Tg = reinterpret_cast<zc*>(Y + seg((size_t)n * n));
-  double* tws = Y + seg((size_t)n * n) + seg(2 * (size_t)std::max(npan, 1) * ZWB * ZWB);
-  zprep_kernel<<<1, 1024, 0, st>>>(ev, dvim, n, dg, off, ph, bp);
+  double* off = dg + seg(B * n);
+  double* mu = off + seg(B * n);
+  zc* ph = reinterpret_cast<zc*>(mu + seg(B * n));
+  double* bp = mu + seg(B * n) + seg(2 * B * n);
+  double* Y = bp + seg(8 * B);
+  zc* Tg = reinterpret_cast<zc*>(Y + seg(B * n * n));
+  double* tws = Y + seg(B * n * n) + seg(2 * B * std::max(npan, 1) * ZWB * ZWB);
+  zprep_kernel<<<batch, 1024, 0, st>>>(ev, dvim, n, dg, off, ph, bp);
   int dev = 0, sms = 148;
   if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  const int p = multisect_lanes(n, sms);
-  const long long threads = ((long long)n * p + 31) / 32 * 32;
-  zbisect_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(dg, off, n, bp, mu, vals_im, p);
+  const int p = multisect_lanes(n * batch, sms);
+  const long long threads = ((long long)n * batch * p + 31) / 32 * 32;
+  zbisect_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(dg, off, n, batch, bp, mu, vals_im, p);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess || !Vd) return e;
-  e = symtri_vectors(dg, off, n, mu, bp, Y, tws, st);
+  e = symtri_vectors(dg, off, n, mu, bp, Y, tws, batch, st);
   if (e != cudaSuccess) return e;
   zc* V = reinterpret_cast<zc*>(Vd);
-  zassemble_kernel<<<dim3((n + 255) / 256, n), 256, 0, st>>>(Y, ph, n, V, ldv);
+  zassemble_kernel<<<dim3((n + 255) / 256, n, batch), 256, 0, st>>>(Y, ph, n, V, ldv);
   e = cudaGetLastError();
   if (e != cudaSuccess || n < 2) return e;
   const zc* A = reinterpret_cast<const zc*>(Ad);
   const zc* tau = reinterpret_cast<const zc*>(taud);
-  zwy_factor_kernel<<<npan, 256, 0, st>>>(A, lda, tau, n, Tg);
-  zback_strip_kernel<<<(n + ZSW - 1) / ZSW, 256, 0, st>>>(A, lda, tau, n, Tg, npan, V, ldv, n);
+  zwy_factor_kernel<<<dim3(npan, batch), 256, 0, st>>>(A, lda, tau, n, Tg);
+  zback_strip_kernel<<<dim3((n + ZSW - 1) / ZSW, batch), 256, 0, st>>>(A, lda, tau, n, Tg, npan, V, ldv, n);
   return cudaGetLastError();
 }
 
@@ -694,6 +722,10 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int n, const zc* __restrict_
                                                     int64_t ldc) {
   __shared__ zc As[32][17];
   __shared__ zc Bs[16][33];
+  const size_t mb = blockIdx.z;  // problem mb: each operand ld*n apart
+  A += mb * (size_t)lda * n;
+  B += mb * (size_t)ldb * n;
+  C += mb * (size_t)ldc * n;
   const int i0 = blockIdx.x * 32, j0 = blockIdx.y * 32;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;  // rows i0 + tx + 16a, columns j0 + ty + 16q
   zc acc[2][2] = {{{0.0, 0.0}, {0.0, 0.0}}, {{0.0, 0.0}, {0.0, 0.0}}};
@@ -739,6 +771,10 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int n, const zc* __restrict_
 // mode 1: M(j, k) <- conj(Phi(j, k)) M(j, k), Phi(j,k) = e^{i(mu_j+mu_k)/2} sinc((mu_j-mu_k)/2)
 __global__ void zscale_kernel(int mode, int n, const double* __restrict__ mu, const zc* __restrict__ V, int64_t ldv,
                               zc* __restrict__ M, int64_t ldm) {
+  const size_t mb = blockIdx.z;  // problem mb: mu n, V ldv*n, M ldm*n apart
+  mu += mb * n;
+  V += mb * (size_t)ldv * n;
+  M += mb * (size_t)ldm * n;
   const int k = blockIdx.y;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
     if (mode == 0) {
@@ -757,13 +793,13 @@ __global__ void zscale_kernel(int mode, int n, const double* __restrict__ mu, co
 }
 
 cudaError_t zfunc_from_eigen(int mode, int n, const double* vals_im, const double* Vd, int64_t ldv, const double* Cd,
-                             int64_t ldc, double* Od, int64_t ldo, double* ws, cudaStream_t st) {
+                             int64_t ldc, double* Od, int64_t ldo, double* ws, int batch, cudaStream_t st) {
   const zc* V = reinterpret_cast<const zc*>(Vd);
   zc* O = reinterpret_cast<zc*>(Od);
   zc* T1 = reinterpret_cast<zc*>(ws);
-  zc* T2 = T1 + (size_t)n * n;
-  const dim3 g((n + 31) / 32, (n + 31) / 32);
-  const dim3 gs((n + 255) / 256, n);
+  zc* T2 = T1 + (size_t)batch * n * n;
+  const dim3 g((n + 31) / 32, (n + 31) / 32, batch);
+  const dim3 gs((n + 255) / 256, n, batch);
   if (mode == 0) {  // exp(A) = V diag(e^{i mu}) V^H
     zscale_kernel<<<gs, 256, 0, st>>>(0, n, vals_im, V, ldv, T1, n);
     zgemm_kernel<<<g, 256, 0, st>>>(n, T1, n, 0, V, ldv, 1, O, ldo);
@@ -778,6 +814,6 @@ cudaError_t zfunc_from_eigen(int mode, int n, const double* vals_im, const doubl
   return cudaGetLastError();
 }
 
-size_t zfunc_ws_doubles(int n) { return 4 * (size_t)n * n + 32; }
+size_t zfunc_ws_doubles(int n, int batch) { return 4 * (size_t)batch * n * n + 32; }
 
 }  // namespace skew

@@ -109,6 +109,7 @@ struct ZHessParams {
   int32_t count;
   int nmax;
   unsigned* counter;
+  int64_t stride;  // W == nullptr: matrix b at W1 + b * stride (complex elements)
   double* tau;   // complex
   double* ev;    // real subdiagonal
   double* dvim;  // imag(diag) after the reduction, or null
@@ -118,22 +119,24 @@ cudaError_t launch_zhess_cta(const ZHessParams& P, int grid, cudaStream_t st);
 size_t zhess_large_ws_doubles(int n);
 cudaError_t zhess_large(double* A, int64_t lda, int n, double* tau, double* ev, double* dvim, double* ws,
                         cudaStream_t st);
-// complex eigen from the reduced matrix; values descending (-mu, mu ascending), vectors Q D Y
-size_t zeigen_ws_doubles(int n);
+// complex eigen from `batch` reduced matrices of size n (arrays per matrix: A lda*n,
+// tau/ev/dvim/vals n, V ldv*n apart); values descending (-mu, mu ascending), vectors Q D Y
+size_t zeigen_ws_doubles(int n, int batch);
 cudaError_t zeigen_from_tridiag(const double* A, int64_t lda, int n, const double* tau, const double* ev,
-                                const double* dvim, double* vals_im, double* V, int64_t ldv, double* ws,
+                                const double* dvim, double* vals_im, double* V, int64_t ldv, double* ws, int batch,
                                 cudaStream_t st);
-// exp (mode 0: O = V e^{i mu} V^H) or its adjoint (mode 1: O = V (conj(Phi) o (V^H C V)) V^H)
-size_t zfunc_ws_doubles(int n);
+// exp (mode 0: O = V e^{i mu} V^H) or its adjoint (mode 1: O = V (conj(Phi) o (V^H C V)) V^H),
+// `batch` problems with operands ld*n apart
+size_t zfunc_ws_doubles(int n, int batch);
 cudaError_t zfunc_from_eigen(int mode, int n, const double* vals_im, const double* V, int64_t ldv, const double* C,
-                             int64_t ldc, double* O, int64_t ldo, double* ws, cudaStream_t st);
+                             int64_t ldc, double* O, int64_t ldo, double* ws, int batch, cudaStream_t st);
 
 // Eigenvectors of one large skew matrix after the blocked reduction (skew_tdvec.cu):
 // vals (descending, from launch_tridiag_bisect) and its scratch bp (bound, pivmin);
 // A holds the reflectors, tau their scalars, ev the subdiagonal.  Vr, Vi (n x n, ldv).
 size_t large_eigen_ws_doubles(int n);
 cudaError_t symtri_vectors(const double* dg, const double* e, int n, const double* mu, const double* bp, double* Y,
-                           double* ws, cudaStream_t st);
+                           double* ws, int batch, cudaStream_t st);
 cudaError_t large_eigen_vectors(const double* A, int64_t lda, int n, const double* tau, const double* ev,
                                 const double* vals, const double* bp, double* Vr, double* Vi, int64_t ldv, double* ws,
                                 cudaStream_t st);

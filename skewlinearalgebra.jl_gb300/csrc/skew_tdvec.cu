@@ -50,6 +50,9 @@ struct TdvecLayout {
   int npan;         // WY panels
   int full;         // 1: general symmetric tridiagonal (diagonal dg), one vector per eigenvalue (K = n)
   const double* dg; // diagonal (full mode) or null (zero diagonal)
+  // batches of equal-size problems (full mode): problem mb = blockIdx.z uses the
+  // workspace block mb (mstride doubles apart) and inputs mb * (n, n, 8) apart
+  size_t mstride;
   double* dp;       // n x KP
   double* dm;       // n x KP
   double* z;        // n x KP
@@ -59,6 +62,8 @@ struct TdvecLayout {
   double* T;        // npan x WB x WB
 };
 
+size_t large_eigen_ws_doubles(int n);
+
 static TdvecLayout layout(int n, double* ws, bool full = false, const double* dg = nullptr) {
   TdvecLayout L;
   L.n = n;
@@ -66,6 +71,7 @@ static TdvecLayout layout(int n, double* ws, bool full = false, const double* dg
   L.K = full ? n : L.h + (n & 1);
   L.full = full ? 1 : 0;
   L.dg = dg;
+  L.mstride = large_eigen_ws_doubles(n);
   L.KP = (L.K + 31) / 32 * 32;
   L.npan = (n - 2 + WB - 1) / WB;
   const size_t big = (size_t)n * L.KP;
@@ -85,11 +91,31 @@ size_t large_eigen_ws_doubles(int n) {
   return 3 * (size_t)n * KP + KP + 2 * (size_t)KP * (LW + 1) + (size_t)std::max(npan, 1) * WB * WB + 64;
 }
 
+// the layout of problem mb of a batch (mb = 0: unchanged)
+__device__ __forceinline__ TdvecLayout at_problem(TdvecLayout L, int mb) {
+  if (mb == 0) return L;
+  const size_t o = (size_t)mb * L.mstride;
+  L.dp += o;
+  L.dm += o;
+  L.z += o;
+  L.nrm2 += o;
+  L.bandU += o;
+  L.bandV += o;
+  L.T += o;
+  if (L.dg) L.dg += (size_t)mb * L.n;
+  return L;
+}
+
 // ---------------------------------------------------------------------------
 // 2. twisted factorisation eigenvectors, one thread per sigma
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(TW_NT) twisted_kernel(const double* __restrict__ e, const double* __restrict__ vals,
-                                                        const double* __restrict__ bp, TdvecLayout L) {
+                                                        const double* __restrict__ bp, TdvecLayout L0) {
+  const int mb = blockIdx.z;
+  const TdvecLayout L = at_problem(L0, mb);
+  e += (size_t)mb * L.n;
+  vals += (size_t)mb * L.n;
+  bp += (size_t)mb * 8;
   const int k = blockIdx.x * TW_NT + threadIdx.x;
   if (k >= L.KP) return;  // KP is a multiple of 32: whole warps leave together
   const int n = L.n;
@@ -234,7 +260,8 @@ constexpr int BD_COLS = 32 + LW;
 constexpr int BD_PAIRS = 32 * (LW + 1);
 constexpr int BD_PER = (BD_PAIRS + BD_NT - 1) / BD_NT;
 
-__global__ void __launch_bounds__(BD_NT) band_dots_kernel(TdvecLayout L) {
+__global__ void __launch_bounds__(BD_NT) band_dots_kernel(TdvecLayout L0) {
+  const TdvecLayout L = at_problem(L0, blockIdx.z);
   __shared__ double zs[RC][BD_COLS + 1];
   const int k0 = blockIdx.x * 32;
   const int n = L.n;
@@ -359,7 +386,9 @@ __global__ void __launch_bounds__(LA_NT) lowdin_apply_kernel(TdvecLayout L, doub
 
 // Full mode: Y(:, k) = s_k z_k - 1/2 sum_d E(k, k+d) s_{k+d} z_{k+d}, with
 // s_k = 1/|z_k| and E the normalised Gram band over all rows.  Y is n x n, ld n.
-__global__ void __launch_bounds__(LA_NT) lowdin_full_kernel(TdvecLayout L, double* __restrict__ Y) {
+__global__ void __launch_bounds__(LA_NT) lowdin_full_kernel(TdvecLayout L0, double* __restrict__ Y) {
+  const TdvecLayout L = at_problem(L0, blockIdx.z);
+  Y += (size_t)blockIdx.z * L.n * L.n;
   __shared__ double zs[RC][LA_COLS + 1];
   __shared__ double sc[LA_COLS];
   __shared__ double eA[32][2 * LW + 1];
@@ -411,16 +440,18 @@ __global__ void __launch_bounds__(LA_NT) lowdin_full_kernel(TdvecLayout L, doubl
 
 // Eigenvectors of the symmetric tridiagonal with diagonal dg and off-diagonal e
 // for the ascending eigenvalues mu (bp: bound, pivmin), into Y (n x n, ld n).
+// Problems mb < batch lie n (dg, e, mu), 8 (bp), n^2 (Y) and
+// large_eigen_ws_doubles(n) (ws) apart.
 cudaError_t symtri_vectors(const double* dg, const double* e, int n, const double* mu, const double* bp, double* Y,
-                           double* ws, cudaStream_t st) {
+                           double* ws, int batch, cudaStream_t st) {
   const TdvecLayout L = layout(n, ws, true, dg);
-  twisted_kernel<<<L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), TW_NT, 0, st>>>(e, mu, bp, L);
+  twisted_kernel<<<dim3(L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), 1, batch), TW_NT, 0, st>>>(e, mu, bp, L);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  band_dots_kernel<<<L.KP / 32, BD_NT, 0, st>>>(L);
+  band_dots_kernel<<<dim3(L.KP / 32, 1, batch), BD_NT, 0, st>>>(L);
   err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  lowdin_full_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC), LA_NT, 0, st>>>(L, Y);
+  lowdin_full_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC, batch), LA_NT, 0, st>>>(L, Y);
   return cudaGetLastError();
 }
 

@@ -399,6 +399,51 @@ def exp_complex_rrule(A):
     return E, pullback
 
 
+def _stack_complex(mats) -> torch.Tensor:
+    """count x n x n host complex matrices -> one device buffer, each matrix column-major."""
+    arr = np.stack([np.asarray(M, dtype=np.complex128).T for M in mats])  # row-major of A^T = column-major A
+    return torch.from_numpy(np.ascontiguousarray(arr)).cuda()
+
+
+def _unstack_complex(T: torch.Tensor):
+    return [m.T.copy() for m in T.cpu().numpy()]
+
+
+def batch_eigen_complex(mats):
+    """eigen for many ComplexF64 skew-Hermitian matrices of one size (skew_batch_eigen_z)."""
+    for M in mats:
+        M = np.asarray(M, dtype=np.complex128)
+        if not np.array_equal(M, -M.conj().T):
+            raise ValueError("Matrix is not skew-hermitian")
+    A = _stack_complex(mats)
+    count, n = A.shape[0], A.shape[1]
+    vals = torch.zeros((count, n), dtype=torch.float64, device="cuda")
+    V = torch.zeros((count, n, n), dtype=torch.complex128, device="cuda")
+    st = torch.zeros(count, dtype=torch.int32, device="cuda")
+    h = handle().bind()
+    check(_lib.load().skew_batch_eigen_z(h, _ptr(A), n, count, _ptr(vals), _ptr(V), _ptr(st)), "batch_eigen_complex")
+    return [1j * v for v in vals.cpu().numpy()], _unstack_complex(V)
+
+
+def batch_exp_complex(mats):
+    A = _stack_complex(mats)
+    count, n = A.shape[0], A.shape[1]
+    E = torch.zeros_like(A)
+    h = handle().bind()
+    check(_lib.load().skew_batch_exp_z(h, _ptr(A), n, count, _ptr(E), None), "batch_exp_complex")
+    return _unstack_complex(E)
+
+
+def batch_exp_vjp_complex(mats, cots):
+    A = _stack_complex(mats)
+    C = _stack_complex(cots)
+    count, n = A.shape[0], A.shape[1]
+    G = torch.zeros_like(A)
+    h = handle().bind()
+    check(_lib.load().skew_batch_exp_vjp_z(h, _ptr(A), n, count, _ptr(C), _ptr(G), None), "batch_exp_vjp_complex")
+    return _unstack_complex(G)
+
+
 def measure_fp64_peak() -> float:
     t = ctypes.c_double()
     check(_lib.load().skew_measure_fp64_peak(handle().bind(), ctypes.byref(t)), "measure_fp64_peak")

@@ -55,6 +55,9 @@ SIGNATURES = {
     "skew_eigen_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _i64, _vp]),
     "skew_exp_z": (_int, [_vp, _vp, _i64, _i64, _vp, _i64, _vp]),
     "skew_exp_vjp_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _i64, _vp]),
+    "skew_batch_eigen_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp]),
+    "skew_batch_exp_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp]),
+    "skew_batch_exp_vjp_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp]),
     "skew_measure_fp64_peak": (_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
 }
 

@@ -128,3 +128,29 @@ def test_exp_complex_adjoint(skewgpu, n):
     fd = (L(A + h * Ed) - L(A - h * Ed)) / (2 * h)
     an = np.real(np.trace(G.conj().T @ Ed))
     assert abs(fd - an) <= 1e-6 * max(1.0, abs(an))
+
+
+@pytest.mark.parametrize("n", [1, 5, 40, 200])
+def test_batch_complex_eigen_exp_vjp(skewgpu, n):
+    """Strided batches of one size (skew_batch_*_z) against the single-matrix calls,
+    LAPACK, expm and the block exponential."""
+    import scipy.linalg as sl
+
+    count = 6
+    mats = [skewh_random(n, 1100 + 17 * n + b, scale=2.0 / np.sqrt(n)) for b in range(count)]
+    rng = np.random.default_rng(n)
+    cots = [rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)) for _ in range(count)]
+    vals, vecs = skewgpu.batch_eigen_complex(mats)
+    Es = skewgpu.batch_exp_complex(mats)
+    Gs = skewgpu.batch_exp_vjp_complex(mats, cots)
+    for b, A in enumerate(mats):
+        rho = max(np.abs(vals[b]).max(), 1e-300)
+        np.testing.assert_allclose(vals[b].imag, -np.linalg.eigvalsh(1j * A), atol=1e-11 * rho)
+        np.testing.assert_allclose(vals[b], skewgpu.eigvals_complex(A), atol=1e-12 * rho)
+        V = vecs[b]
+        np.testing.assert_allclose(V.conj().T @ V, np.eye(n), atol=1e-11)
+        np.testing.assert_allclose(V @ np.diag(vals[b]) @ V.conj().T, A, atol=1e-11 * rho)
+        np.testing.assert_allclose(Es[b], sl.expm(A), atol=1e-11 * np.sqrt(n))
+        Z = np.zeros((n, n), dtype=np.complex128)
+        Gref = sl.expm(np.block([[A.conj().T, cots[b]], [Z, A.conj().T]]))[:n, n:]
+        np.testing.assert_allclose(Gs[b], Gref, atol=1e-10 * np.abs(Gref).max())
