@@ -68,6 +68,7 @@ struct skew_batch_plan_st {
   double** e_p_vi = nullptr;
   double** e_p_vals = nullptr;
   double** e_p_scratch = nullptr;  // 8 x count: single-call pointer arrays
+  double** e_p_work = nullptr;     // work + off_w per matrix
   int* e_status = nullptr;
   unsigned* e_counter = nullptr;
   // one instantiated CUDA graph per batched operation, keyed on its arguments
@@ -378,7 +379,7 @@ int skew_batch_plan_destroy(skew_batch_plan_t P) {
   if (P->d_gws) cudaFreeAsync(P->d_gws, st);
   void* eig[] = {P->e_refl, P->e_tau, P->e_evb, P->e_G, P->e_log, P->e_work, P->e_vr, P->e_vi, P->e_vals,
                  P->e_off_log, P->e_cap_log, P->e_log_len, P->e_off_w, P->e_p_refl, P->e_p_vr, P->e_p_vi,
-                 P->e_p_vals, P->e_p_scratch, P->e_status, P->e_counter};
+                 P->e_p_vals, P->e_p_scratch, P->e_p_work, P->e_status, P->e_counter};
   for (void* q : eig)
     if (q) cudaFreeAsync(q, st);
   cudaStreamSynchronize(st);
@@ -561,7 +562,7 @@ static int eigen_ws(skew_batch_plan_t P) {
     cap_log[b] = 3 * n * n + 64;
     lg += cap_log[b];
     off_w[b] = w;
-    w += 4 * n * n;
+    w += (int64_t)eigen_work_doubles((int)n);
   }
   P->nmax = nmax;
   bool ok = true;
@@ -584,6 +585,7 @@ static int eigen_ws(skew_batch_plan_t P) {
   alloc((void**)&P->e_p_vi, sizeof(double*) * count);
   alloc((void**)&P->e_p_vals, sizeof(double*) * count);
   alloc((void**)&P->e_p_scratch, sizeof(double*) * 8);
+  alloc((void**)&P->e_p_work, sizeof(double*) * count);
   alloc((void**)&P->e_status, sizeof(int) * count);
   alloc((void**)&P->e_counter, sizeof(unsigned));
   if (!ok) return SKEW_NO_MEMORY;
@@ -602,6 +604,7 @@ static int eigen_ws(skew_batch_plan_t P) {
   fill_ptrs_kernel<<<g, 256, 0, st>>>(P->e_p_vr, P->e_vr, d_off_sq, (int)count);
   fill_ptrs_kernel<<<g, 256, 0, st>>>(P->e_p_vi, P->e_vi, d_off_sq, (int)count);
   fill_ptrs_kernel<<<g, 256, 0, st>>>(P->e_p_vals, P->e_vals, P->d_ev_off, (int)count);
+  fill_ptrs_kernel<<<g, 256, 0, st>>>(P->e_p_work, P->e_work, P->e_off_w, (int)count);
   CK(cudaGetLastError());
   CK(cudaStreamSynchronize(st));  // host vectors go out of scope
   cudaFree(d_off_sq);
@@ -641,6 +644,7 @@ static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const*
   E.off_w = P->e_off_w;
   E.out = nullptr;
   E.cot = nullptr;
+  E.pwork = P->e_p_work;
   const int grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
   CK(launch_eigen_chain(E, st));
   CK(launch_eigen_vectors(E, grid, st));
@@ -694,8 +698,7 @@ static int func_issue(skew_batch_plan_t P, const double* const* A, double* const
   if (s) return s;
   E.out = out;
   E.cot = cot;
-  const int grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
-  CK(launch_eigen_func(E, grid, mode, P->h->stream));
+  CK(launch_eigen_func(E, mode, P->h->stream));
   return finish_status(P, status);
 }
 

@@ -28,8 +28,11 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <algorithm>
+
 #include "skew_common.cuh"
 #include "skew_internal.h"
+#include "skew_twisted.cuh"
 
 namespace skew {
 
@@ -206,111 +209,151 @@ __global__ void eigen_chain_kernel(EigenBatch E) {
 // vectors: replay the rotations, assemble Qr / Qim
 // ---------------------------------------------------------------------------
 
-// Cyclic Jacobi on the dense symmetric tridiagonal SymTridiagonal(0, e) (size
-// n <= 1024) in S (n x n, ld n); eigenvectors accumulate in Z.  Round-robin
-// pairing makes the rotations of one round disjoint.  Eigenvalues returned
-// ascending in w with Z's columns permuted to match.  The stagnation fallback
-// of the QR (rare).
-__device__ void jacobi_symtri(const double* e, int n, double* S, double* Z, double* w, int* perm, double* rc,
-                              double* rs, int* pp, int* pq) {
+// The stagnation fallback (skewtrieigen_backup!, skeweigen.jl:470-489) for one
+// matrix, by the CTA: the eigenpairs of SymTridiagonal(0, e) (the reference calls
+// LAPACK) by bisection (one positive eigenvalue per thread), twisted-factorisation
+// vectors (one per thread, skew_twisted.cuh) and one banded symmetric correction
+// of the even-row and odd-row parts, written in the fallback's layout: values
+// descending (vals = -eigvals(H)); column j of the eigenvalue -lambda_j is real on
+// odd (1-based) rows and imaginary on even rows, sign flipped every pair; the
+// vector of -sigma is the conjugate of that of sigma.  work: fallback_ws_doubles(N).
+constexpr int FB_LW = 16;
+
+__host__ __device__ inline int fallback_kp(int N) { return ((N / 2 + (N & 1)) + 31) / 32 * 32; }
+__host__ __device__ inline int64_t fallback_ws_doubles(int N) {
+  const int64_t KP = fallback_kp(N);
+  return 3 * (int64_t)N * KP + KP + 2 * KP * (FB_LW + 1) + 64;
+}
+
+__device__ void cta_fallback(const double* __restrict__ e, int N, double* __restrict__ vals, double* __restrict__ Vr,
+                             double* __restrict__ Vi, int64_t ldv, double* __restrict__ work) {
+  __shared__ double red[2][ENW];
   const int tid = threadIdx.x;
-  for (int64_t k = tid; k < (int64_t)n * n; k += ENT) {
-    const int j = (int)(k / n), i = (int)(k - (int64_t)j * n);
-    S[k] = (i == j + 1) ? e[j] : ((j == i + 1) ? e[i] : 0.0);
-    Z[k] = (i == j) ? 1.0 : 0.0;
+  const int h = N / 2, K = h + (N & 1), KP = fallback_kp(N);
+  double* dp = work;
+  double* dm = dp + (int64_t)N * KP;
+  double* z = dm + (int64_t)N * KP;
+  double* nrm2 = z + (int64_t)N * KP;
+  double* band = nrm2 + KP;  // [k][d][U, V]
+  // Gershgorin bound and pivmin
+  double bound = 0.0, e2 = 0.0;
+  for (int i = tid; i < N; i += ENT) {
+    const double l = (i > 0) ? fabs(e[i - 1]) : 0.0, r = (i + 1 < N) ? fabs(e[i]) : 0.0;
+    bound = fmax(bound, l + r);
+    if (i + 1 < N) e2 = fmax(e2, r * r);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    bound = fmax(bound, __shfl_xor_sync(0xffffffffu, bound, o));
+    e2 = fmax(e2, __shfl_xor_sync(0xffffffffu, e2, o));
+  }
+  if ((tid & 31) == 0) {
+    red[0][tid >> 5] = bound;
+    red[1][tid >> 5] = e2;
   }
   __syncthreads();
-  const int m = n + (n & 1);  // players, one dummy when n is odd
-  __shared__ double s_off, s_tot;
-  if (tid == 0) {
-    double t2 = 0.0;
-    for (int i = 0; i + 1 < n; i++) t2 = fma(e[i], e[i], t2);
-    s_tot = 2.0 * t2;
+  bound = 0.0;
+  e2 = 0.0;
+  for (int w = 0; w < ENW; w++) {
+    bound = fmax(bound, red[0][w]);
+    e2 = fmax(e2, red[1][w]);
   }
   __syncthreads();
-  for (int sweep = 0; sweep < 60; sweep++) {
-    if (tid == 0) s_off = 0.0;
-    __syncthreads();
-    double part = 0.0;
-    for (int64_t k = tid; k < (int64_t)n * n; k += ENT) {
-      const int j = (int)(k / n), i = (int)(k - (int64_t)j * n);
-      if (i != j) part = fma(S[k], S[k], part);
+  const double pivmin = 2.2250738585072014e-308 * fmax(1.0, e2);
+  bound = bound * (1.0 + 1e-14) + 1e-300;
+  // positive eigenvalues, descending: the k-th largest of SymTridiagonal(0, e)
+  for (int k = tid; k < h; k += ENT) {
+    double lo = 0.0, hi = bound;
+    for (int it = 0; it < 200 && hi - lo > fmax(2.220446049250313e-16 * hi, 2.220446049250313e-16 * bound); it++) {
+      const double mid = 0.5 * (lo + hi);
+      double q = neg(mid);
+      if (fabs(q) <= pivmin) q = neg(pivmin);
+      int c = (q < 0.0);
+      for (int i = 1; i < N; i++) {
+        const double ei = e[i - 1];
+        q = neg(mid) - (ei * ei) / q;
+        if (fabs(q) <= pivmin) q = neg(pivmin);
+        c += (q < 0.0);
+      }
+      if (c <= N - 1 - k)
+        lo = mid;
+      else
+        hi = mid;
     }
-    part = warp_sum(part);
-    if ((tid & 31) == 0) atomicAdd(&s_off, part);
+    const double x = 0.5 * (lo + hi);
+    vals[k] = x;
+    vals[N - 1 - k] = neg(x);
+  }
+  if ((N & 1) && tid == 0) vals[h] = 0.0;
+  __syncthreads();
+  // one twisted vector per thread (whole warps: KP and ENT are multiples of 32)
+  for (int kb = 0; kb < KP; kb += ENT) {
+    if (kb + (tid & ~31) >= KP) continue;
+    const int k = kb + tid;
+    const double sig = (k < h) ? vals[k] : 0.0;
+    nrm2[k] = twisted_vector(e, nullptr, N, sig, pivmin, KP, k, dp, dm, z);
+  }
+  __syncthreads();
+  // unit even-row and odd-row parts: X(i,k) = s_k z(i,k), s_k = sqrt(2)/|z_k| (sigma > 0)
+  // or 1/|z_k| (the zero-eigenvalue vector, even rows only)
+  double* X = dp;  // the pivots are no longer needed
+  double* Y = z;
+  for (int64_t q = tid; q < (int64_t)N * KP; q += ENT) {
+    const int i = (int)(q / KP), k = (int)(q - (int64_t)i * KP);
+    double x = 0.0;
+    if (k < K && !((i & 1) && k >= h)) x = ((k < h) ? 1.4142135623730951 : 1.0) * rsqrt(nrm2[k]) * z[q];
+    X[q] = x;
+  }
+  __syncthreads();
+  // symmetric corrections X <- X - 1/2 X E over a band of neighbours, E = X^T X - I
+  // per part; each pass squares the departure from orthogonality (three passes
+  // also settle clusters of nearly equal eigenvalues, whose twisted vectors mix)
+  for (int pass = 0; pass < 3; pass++) {
+    for (int q = tid; q < K * (FB_LW + 1); q += ENT) {
+      const int k = q / (FB_LW + 1), d = q - k * (FB_LW + 1), j = k + d;
+      double su = 0.0, sv = 0.0;
+      if (j < K) {
+        for (int i = 0; i < N; i += 2) su = fma(X[(int64_t)i * KP + k], X[(int64_t)i * KP + j], su);
+        for (int i = 1; i < N; i += 2) sv = fma(X[(int64_t)i * KP + k], X[(int64_t)i * KP + j], sv);
+      }
+      band[2 * q] = su - (d == 0 ? 1.0 : 0.0);
+      band[2 * q + 1] = (k >= h || j >= h) ? 0.0 : sv - (d == 0 ? 1.0 : 0.0);
+    }
     __syncthreads();
-    if (s_off <= 1e-30 * s_tot) break;
-    for (int round = 0; round < m - 1; round++) {
-      // pairs of the round: (0, round+1) rotated schedule
-      for (int k = tid; k < m / 2; k += ENT) {
-        int a = (k == 0) ? 0 : ((round + k) % (m - 1)) + 1;
-        int b = ((round + m - 1 - k) % (m - 1)) + 1;
-        if (k == 0) b = ((round) % (m - 1)) + 1;
-        int p = min(a, b), q = max(a, b);
-        double c = 1.0, s = 0.0;
-        if (q < n && p != q) {
-          const double apq = S[p + (int64_t)q * n];
-          if (apq != 0.0) {
-            const double app = S[p + (int64_t)p * n], aqq = S[q + (int64_t)q * n];
-            const double theta = (aqq - app) / (2.0 * apq);
-            double t = (theta >= 0.0 ? 1.0 : -1.0) / (fabs(theta) + sqrt(fma(theta, theta, 1.0)));
-            c = 1.0 / sqrt(fma(t, t, 1.0));
-            s = t * c;
-          }
-        } else {
-          p = q = -1;
+    for (int64_t q = tid; q < (int64_t)N * KP; q += ENT) {
+      const int i = (int)(q / KP), k = (int)(q - (int64_t)i * KP);
+      const int odd = i & 1;
+      double acc = X[q];
+      if (k < K) {
+        for (int d = -FB_LW; d <= FB_LW; d++) {
+          const int j = k + d;
+          if (j < 0 || j >= K) continue;
+          const int lo = min(k, j), off = abs(d);
+          acc = fma(-0.5 * band[2 * (lo * (FB_LW + 1) + off) + odd], X[(int64_t)i * KP + j], acc);
         }
-        pp[k] = p;
-        pq[k] = q;
-        rc[k] = c;
-        rs[k] = s;
       }
-      __syncthreads();
-      // columns p, q of S and Z:  [x_p, x_q] <- [c x_p - s x_q, s x_p + c x_q]
-      for (int64_t idx = tid; idx < (int64_t)(m / 2) * n; idx += ENT) {
-        const int k = (int)(idx / n), r = (int)(idx - (int64_t)k * n);
-        const int p = pp[k], q = pq[k];
-        if (p < 0) continue;
-        const double c = rc[k], s = rs[k];
-        double* sp = S + (int64_t)p * n + r;
-        double* sq = S + (int64_t)q * n + r;
-        const double x = *sp, y = *sq;
-        *sp = c * x - s * y;
-        *sq = s * x + c * y;
-        double* zp = Z + (int64_t)p * n + r;
-        double* zq = Z + (int64_t)q * n + r;
-        const double u = *zp, v = *zq;
-        *zp = c * u - s * v;
-        *zq = s * u + c * v;
-      }
-      __syncthreads();
-      // rows p, q of S
-      for (int64_t idx = tid; idx < (int64_t)(m / 2) * n; idx += ENT) {
-        const int k = (int)(idx / n), col = (int)(idx - (int64_t)k * n);
-        const int p = pp[k], q = pq[k];
-        if (p < 0) continue;
-        const double c = rc[k], s = rs[k];
-        double* sp = S + p + (int64_t)col * n;
-        double* sq = S + q + (int64_t)col * n;
-        const double x = *sp, y = *sq;
-        *sp = c * x - s * y;
-        *sq = s * x + c * y;
-      }
-      __syncthreads();
+      Y[q] = acc;
+    }
+    __syncthreads();
+    double* t = X;
+    X = Y;
+    Y = t;
+  }
+  // fallback layout: column N-1-k (-sigma_k) and k (+sigma_k, the conjugate); zero vector: column h
+  for (int64_t q = tid; q < (int64_t)N * K; q += ENT) {
+    const int k = (int)(q / N), i = (int)(q - (int64_t)k * N);
+    const bool odd = (i & 1);
+    if (odd && k >= h) continue;
+    double o = (k < h) ? X[(int64_t)i * KP + k] * 0.7071067811865476 : X[(int64_t)i * KP + k];
+    if ((i >> 1) & 1) o = neg(o);
+    const int col = (k < h) ? N - 1 - k : h;
+    if (!odd) {
+      Vr[i + (int64_t)col * ldv] = o;
+      if (k < h) Vr[i + (int64_t)k * ldv] = o;
+    } else {
+      Vi[i + (int64_t)col * ldv] = o;
+      Vi[i + (int64_t)k * ldv] = neg(o);
     }
   }
-  // sort eigenvalues ascending (selection by rank; n <= 1024)
-  for (int i = tid; i < n; i += ENT) {
-    const double di = S[i + (int64_t)i * n];
-    int rank = 0;
-    for (int j = 0; j < n; j++) {
-      const double dj = S[j + (int64_t)j * n];
-      rank += (dj < di) || (dj == di && j < i);
-    }
-    perm[rank] = i;
-  }
-  __syncthreads();
-  for (int i = tid; i < n; i += ENT) w[i] = S[perm[i] + (int64_t)perm[i] * n];
   __syncthreads();
 }
 
@@ -318,8 +361,6 @@ __global__ void __launch_bounds__(ENT) eigen_vectors_kernel(EigenBatch E) {
   __shared__ int s_next;
   __shared__ int s_type[1024 + 1];  // per output column: -1 none, 0..3 kinds (see below)
   __shared__ int s_src[1024 + 1];
-  __shared__ double rc[512], rs[512];
-  __shared__ int pp[512], pq[512];
   for (;;) {
     if (threadIdx.x == 0) s_next = (int)atomicAdd(E.counter, 1u);
     __syncthreads();
@@ -347,28 +388,7 @@ __global__ void __launch_bounds__(ENT) eigen_vectors_kernel(EigenBatch E) {
     }
     if (st == SKEW_NO_CONVERGENCE) continue;
     if (st == SKEW_FALLBACK_USED) {
-      // skewtrieigen_backup! (:470-489) from the original ev
-      double* S = work;
-      double* Z = work + (int64_t)N * N;
-      double* w = E.ev + E.off_n[b];  // reuse: the QR's ev copy is no longer needed
-      int* perm = (int*)(E.G + E.off_n[b]);
-      jacobi_symtri(E.evb + E.off_n[b], N, S, Z, w, perm, rc, rs, pp, pq);
-      double* vals = E.vals[b];
-      for (int j = threadIdx.x; j < N; j += ENT) vals[j] = neg(w[j]);
-      for (int64_t k = threadIdx.x; k < (int64_t)N * N; k += ENT) {
-        const int j = (int)(k / N), i = (int)(k - (int64_t)j * N);
-        const double z = Z[i + (int64_t)perm[j] * N];
-        const int pair = i >> 1;
-        const double c = (pair & 1) ? -1.0 : 1.0;  // c flips after every (odd, even) pair
-        if ((N & 1) && i == N - 1) {
-          Vr[i + (int64_t)j * ldv] = c * z;
-        } else if ((i & 1) == 0) {
-          Vr[i + (int64_t)j * ldv] = c * z;
-        } else {
-          Vi[i + (int64_t)j * ldv] = c * z;
-        }
-      }
-      __syncthreads();
+      cta_fallback(E.evb + E.off_n[b], N, E.vals[b], Vr, Vi, ldv, work);
       continue;
     }
     // Qodd (ho x ho) and Qeven (he x he), column-major, identity
@@ -600,181 +620,179 @@ __global__ void __launch_bounds__(ENT) eigen_back_kernel(EigenBatch E) {
 }
 
 // ---------------------------------------------------------------------------
-// Per-CTA product  C[i,j] = sum_s sgn_s sum_k L_s(i,k) R_s(k,j)  over 64 x 64
-// tiles; operands are strided views (transposes are stride swaps).
+// exp / cis / exp adjoint from (vals, Vr, Vi): tiled batched products
 // ---------------------------------------------------------------------------
-struct Opnd {
-  const double* p;
-  int64_t rs, cs;  // element (i, k) at p[i*rs + k*cs]
-  __device__ __forceinline__ double at(int i, int k) const { return p[i * rs + k * cs]; }
+// Operand of a batched product: matrix b is p[b] + add_sq * n_b^2 (n_b x n_b, ld n_b),
+// used transposed if trans.
+struct BOperand {
+  const double* const* p;
+  int add_sq;
+  int trans;
 };
 
-__device__ void cta_product(int n, int K, int ns, const Opnd* L, const Opnd* R, const double* sgn, double* C,
-                            int64_t crs, int64_t ccs, double* sbuf) {
-  constexpr int TT = 64, KC = 16;
-  double (*sL)[TT] = reinterpret_cast<double (*)[TT]>(sbuf);
-  double (*sR)[TT] = reinterpret_cast<double (*)[TT]>(sbuf + KC * TT);
+struct BGemm {
+  const int32_t* n;
+  const int* status;  // matrices with SKEW_NO_CONVERGENCE are skipped
+  int nterms;         // C_b = sum_t s_t op(A_t,b) op(B_t,b)
+  BOperand A[2], B[2];
+  double s[2];
+  double* const* C;
+  int c_add_sq;
+  int c_add;   // extra offset in doubles (1: imaginary parts of an interleaved output)
+  int c_step;  // 1, or 2 for a ComplexF64 output
+};
+
+constexpr int BG_T = 64, BG_K = 16;
+
+// One 64 x 64 tile of one matrix per CTA: grid (tiles^2 of the largest matrix, count);
+// tiles outside a smaller matrix return at once.
+__global__ void __launch_bounds__(256) bgemm_kernel(BGemm P) {
+  __shared__ double As[BG_K][BG_T + 1];
+  __shared__ double Bs[BG_K][BG_T + 1];
+  const int b = blockIdx.y;
+  const int n = P.n[b];
+  if (P.status && P.status[b] == SKEW_NO_CONVERGENCE) return;
+  const int nt = (n + BG_T - 1) / BG_T;
+  if ((int)blockIdx.x >= nt * nt) return;
+  const int i0 = (blockIdx.x % nt) * BG_T, j0 = (blockIdx.x / nt) * BG_T;
+  const int64_t nn = (int64_t)n * n;
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int nt = (n + TT - 1) / TT;
-  for (int tile = 0; tile < nt * nt; tile++) {
-    const int ti = tile % nt, tj = tile / nt;
-    const int R0 = ti * TT, C0 = tj * TT;
-    double acc[4][4];
+  double acc[4][4];
 #pragma unroll
-    for (int a = 0; a < 4; a++)
+  for (int a = 0; a < 4; a++)
 #pragma unroll
-      for (int q = 0; q < 4; q++) acc[a][q] = 0.0;
-    for (int sidx = 0; sidx < ns; sidx++) {
-      const double sg = sgn[sidx];
-      for (int k0 = 0; k0 < K; k0 += KC) {
-        __syncthreads();
-        for (int idx = threadIdx.x; idx < KC * TT; idx += ENT) {
-          const int kk = idx / TT, rr = idx - kk * TT;
-          const int k = k0 + kk;
-          const int gi = R0 + rr, gj = C0 + rr;
-          sL[kk][rr] = (k < K && gi < n) ? sg * L[sidx].at(gi, k) : 0.0;
-          sR[kk][rr] = (k < K && gj < n) ? R[sidx].at(k, gj) : 0.0;
+    for (int q = 0; q < 4; q++) acc[a][q] = 0.0;
+  for (int t = 0; t < P.nterms; t++) {
+    const double* A = P.A[t].p[b] + (int64_t)P.A[t].add_sq * nn;
+    const double* B = P.B[t].p[b] + (int64_t)P.B[t].add_sq * nn;
+    const int ta = P.A[t].trans, tb = P.B[t].trans;
+    const double sg = P.s[t];
+    for (int k0 = 0; k0 < n; k0 += BG_K) {
+      __syncthreads();
+      for (int idx = threadIdx.x; idx < BG_T * BG_K; idx += 256) {
+        int ii, kk;
+        if (!ta) {
+          ii = idx & 63;
+          kk = idx >> 6;
+        } else {
+          kk = idx & 15;
+          ii = idx >> 4;
         }
-        __syncthreads();
-#pragma unroll 4
-        for (int kk = 0; kk < KC; kk++) {
-          double l4[4], r4[4];
-#pragma unroll
-          for (int a = 0; a < 4; a++) {
-            l4[a] = sL[kk][tx + 16 * a];
-            r4[a] = sR[kk][ty + 16 * a];
-          }
-#pragma unroll
-          for (int a = 0; a < 4; a++)
-#pragma unroll
-            for (int q = 0; q < 4; q++) acc[a][q] = fma(l4[a], r4[q], acc[a][q]);
+        const int i = i0 + ii, k = k0 + kk;
+        double av = 0.0;
+        if (i < n && k < n) av = ta ? A[k + (int64_t)i * n] : A[i + (int64_t)k * n];
+        As[kk][ii] = sg * av;
+        int jj, kb;
+        if (!tb) {
+          kb = idx & 15;
+          jj = idx >> 4;
+        } else {
+          jj = idx & 63;
+          kb = idx >> 6;
         }
+        const int j = j0 + jj, k2 = k0 + kb;
+        double bv = 0.0;
+        if (j < n && k2 < n) bv = tb ? B[j + (int64_t)k2 * n] : B[k2 + (int64_t)j * n];
+        Bs[kb][jj] = bv;
+      }
+      __syncthreads();
+#pragma unroll
+      for (int kk = 0; kk < BG_K; kk++) {
+        double a4[4], b4[4];
+#pragma unroll
+        for (int a = 0; a < 4; a++) {
+          a4[a] = As[kk][tx + 16 * a];
+          b4[a] = Bs[kk][ty + 16 * a];
+        }
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+          for (int q = 0; q < 4; q++) acc[a][q] = fma(a4[a], b4[q], acc[a][q]);
       }
     }
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-      for (int q = 0; q < 4; q++) {
-        const int gi = R0 + tx + 16 * a, gj = C0 + ty + 16 * q;
-        if (gi < n && gj < n) C[gi * crs + gj * ccs] = acc[a][q];
-      }
   }
-  __syncthreads();
+  double* C = P.C[b] + (int64_t)P.c_add_sq * nn + P.c_add;
+#pragma unroll
+  for (int a = 0; a < 4; a++)
+#pragma unroll
+    for (int q = 0; q < 4; q++) {
+      const int i = i0 + tx + 16 * a, j = j0 + ty + 16 * q;
+      if (i < n && j < n) C[(int64_t)P.c_step * (i + (int64_t)j * n)] = acc[a][q];
+    }
 }
 
-// exp / cis / exp-vjp assembly from (vals, Vr, Vi).  mode 0: exp -> E (real, lde);
-// mode 1: cis -> Cz (complex interleaved, ldc complex); mode 2: vjp of exp with
-// cotangent Gbar -> G (real).
-__global__ void __launch_bounds__(ENT) eigen_func_kernel(EigenBatch E, int mode) {
-  __shared__ int s_next;
-  __shared__ double sbuf[2 * 16 * 64];
-  for (;;) {
-    if (threadIdx.x == 0) s_next = (int)atomicAdd(E.counter, 1u);
-    __syncthreads();
-    const int t = s_next;
-    __syncthreads();
-    if (t >= E.count) break;
-    const int b = E.order[t];
-    const int n = E.n[b];
-    const int64_t ldv = E.n[b];
-    const double* Qr = E.Vr[b];
-    const double* Qi = E.Vi[b];
-    const double* mu = E.vals[b];
-    double* work = E.work + E.off_w[b];  // >= 4 n^2 doubles
-    if (E.status[b] == SKEW_NO_CONVERGENCE) continue;
-    const int64_t nn = (int64_t)n * n;
+// Elementwise steps, grid (chunks, count):
+//   mode 0 (exp): P = Qr C + Qi S, R = Qi C - Qr S with C, S = cos, sin of mu_j per column;
+//   mode 1 (cis): P = Qr D, R = Qi D with D = exp(-mu_j);
+//   mode 2 (adjoint): M <- conj(Phi) o M on (Mr, Mi) = work blocks 2, 3, with
+//   Phi_jk = exp(i(mu_j + mu_k)/2) sinc((mu_j - mu_k)/2).
+__global__ void func_elem_kernel(EigenBatch E, int mode) {
+  const int b = blockIdx.y;
+  if (E.status[b] == SKEW_NO_CONVERGENCE) return;
+  const int n = E.n[b];
+  const int64_t nn = (int64_t)n * n;
+  const double* mu = E.vals[b];
+  double* w = E.pwork[b];
+  const double* Qr = E.Vr[b];
+  const double* Qi = E.Vi[b];
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(k / n), r = (int)(k - (int64_t)j * n);
     if (mode == 0) {
-      // P = Qr C + Qi S, R = Qi C - Qr S (column scalings); E = Qr P^T + Qi R^T
-      double* P = work;
-      double* R = work + nn;
-      for (int64_t k = threadIdx.x; k < nn; k += ENT) {
-        const int j = (int)(k / n), i = (int)(k - (int64_t)j * n);
-        double sn, cs;
-        sincos(mu[j], &sn, &cs);
-        const double qr = Qr[i + (int64_t)j * ldv], qi = Qi[i + (int64_t)j * ldv];
-        P[k] = fma(qr, cs, qi * sn);
-        R[k] = fma(qi, cs, -(qr * sn));
-      }
-      __syncthreads();
-      Opnd L[2] = {{Qr, 1, ldv}, {Qi, 1, ldv}};
-      Opnd Rt[2] = {{P, n, 1}, {R, n, 1}};  // (k, j) -> P[j, k]
-      const double sg[2] = {1.0, 1.0};
-      cta_product(n, n, 2, L, Rt, sg, E.out[b], 1, n, sbuf);
+      double sn, cs;
+      sincos(mu[j], &sn, &cs);
+      const double qr = Qr[k], qi = Qi[k];
+      w[k] = fma(qr, cs, qi * sn);
+      w[nn + k] = fma(qi, cs, -(qr * sn));
     } else if (mode == 1) {
-      // D = exp(-mu); Re = Qr D Qr^T + Qi D Qi^T, Im = Qi D Qr^T - Qr D Qi^T
-      double* P = work;       // Qr D
-      double* R = work + nn;  // Qi D
-      for (int64_t k = threadIdx.x; k < nn; k += ENT) {
-        const int j = (int)(k / n), i = (int)(k - (int64_t)j * n);
-        const double d = exp(neg(mu[j]));
-        P[k] = Qr[i + (int64_t)j * ldv] * d;
-        R[k] = Qi[i + (int64_t)j * ldv] * d;
-      }
-      __syncthreads();
-      double* Cz = E.out[b];
-      const int64_t ldc = n;  // in complex elements
-      Opnd L[2] = {{Qr, 1, ldv}, {Qi, 1, ldv}};
-      Opnd Rt[2] = {{P, n, 1}, {R, n, 1}};
-      const double sg[2] = {1.0, 1.0};
-      cta_product(n, n, 2, L, Rt, sg, Cz, 2, 2 * ldc, sbuf);
-      Opnd L2[2] = {{Qi, 1, ldv}, {Qr, 1, ldv}};
-      const double sg2[2] = {1.0, -1.0};
-      cta_product(n, n, 2, L2, Rt, sg2, Cz + 1, 2, 2 * ldc, sbuf);
+      const double d = exp(neg(mu[j]));
+      w[k] = Qr[k] * d;
+      w[nn + k] = Qi[k] * d;
     } else {
-      // Y = Gbar V, M = V^H Y, M <- conj(Phi) o M, Z = V M, G = Re(Z V^H)
-      const double* Gb = E.cot[b];  // n x n, ld n
-      double* Yr = work;
-      double* Yi = work + nn;
-      double* Mr = work + 2 * nn;
-      double* Mi = work + 3 * nn;
-      {
-        Opnd L[1] = {{Gb, 1, n}};
-        Opnd R1[1] = {{Qr, 1, ldv}};
-        const double one[1] = {1.0};
-        cta_product(n, n, 1, L, R1, one, Yr, 1, n, sbuf);
-        Opnd R2[1] = {{Qi, 1, ldv}};
-        cta_product(n, n, 1, L, R2, one, Yi, 1, n, sbuf);
-      }
-      {  // M = (Qr^T - i Qi^T)(Yr + i Yi): Mr = Qr^T Yr + Qi^T Yi, Mi = Qr^T Yi - Qi^T Yr
-        Opnd L[2] = {{Qr, ldv, 1}, {Qi, ldv, 1}};
-        Opnd R1[2] = {{Yr, 1, n}, {Yi, 1, n}};
-        const double pp2[2] = {1.0, 1.0};
-        cta_product(n, n, 2, L, R1, pp2, Mr, 1, n, sbuf);
-        Opnd R2[2] = {{Yi, 1, n}, {Yr, 1, n}};
-        const double pm[2] = {1.0, -1.0};
-        cta_product(n, n, 2, L, R2, pm, Mi, 1, n, sbuf);
-      }
-      // M_jk *= conj(Phi_jk), Phi_jk = exp(i(mu_j+mu_k)/2) sinc((mu_j-mu_k)/2)
-      for (int64_t k = threadIdx.x; k < nn; k += ENT) {
-        const int c = (int)(k / n), r = (int)(k - (int64_t)c * n);
-        const double a = mu[r], bb = mu[c];
-        const double d = 0.5 * (a - bb);
-        const double sc = (fabs(d) < 1e-8) ? fma(-d * d, 1.0 / 6.0, 1.0) : sin(d) / d;
-        double sn, cs;
-        sincos(0.5 * (a + bb), &sn, &cs);
-        const double pr = cs * sc, pi = -sn * sc;  // conj(Phi)
-        const double mr = Mr[k], mi = Mi[k];
-        Mr[k] = fma(mr, pr, -(mi * pi));
-        Mi[k] = fma(mr, pi, mi * pr);
-      }
-      __syncthreads();
-      {  // Z = (Qr + i Qi)(Mr + i Mi): Zr = Qr Mr - Qi Mi, Zi = Qr Mi + Qi Mr  (into Yr, Yi)
-        Opnd L[2] = {{Qr, 1, ldv}, {Qi, 1, ldv}};
-        Opnd R1[2] = {{Mr, 1, n}, {Mi, 1, n}};
-        const double pm[2] = {1.0, -1.0};
-        cta_product(n, n, 2, L, R1, pm, Yr, 1, n, sbuf);
-        Opnd R2[2] = {{Mi, 1, n}, {Mr, 1, n}};
-        const double pp2[2] = {1.0, 1.0};
-        cta_product(n, n, 2, L, R2, pp2, Yi, 1, n, sbuf);
-      }
-      {  // G = Re((Zr + i Zi)(Qr^T - i Qi^T)) = Zr Qr^T + Zi Qi^T
-        Opnd L[2] = {{Yr, 1, n}, {Yi, 1, n}};
-        Opnd R1[2] = {{Qr, ldv, 1}, {Qi, ldv, 1}};  // (k, j) -> Q[j, k]
-        const double pp2[2] = {1.0, 1.0};
-        cta_product(n, n, 2, L, R1, pp2, E.out[b], 1, n, sbuf);
-      }
+      const double a = mu[r], bb = mu[j];
+      const double dlt = 0.5 * (a - bb);
+      const double sc = (fabs(dlt) < 1e-8) ? fma(-dlt * dlt, 1.0 / 6.0, 1.0) : sin(dlt) / dlt;
+      double sn, cs;
+      sincos(0.5 * (a + bb), &sn, &cs);
+      const double pr = cs * sc, pi = -sn * sc;  // conj(Phi)
+      const double mr = w[2 * nn + k], mi = w[3 * nn + k];
+      w[2 * nn + k] = fma(mr, pr, -(mi * pi));
+      w[3 * nn + k] = fma(mr, pi, mi * pr);
     }
   }
+}
+
+static BOperand bop(const double* const* p, int add_sq, int trans) {
+  BOperand o;
+  o.p = p;
+  o.add_sq = add_sq;
+  o.trans = trans;
+  return o;
+}
+
+static cudaError_t bgemm(const EigenBatch& E, int nterms, BOperand A0, BOperand B0, double s0, BOperand A1,
+                         BOperand B1, double s1, double* const* C, int c_add_sq, int c_add, int c_step,
+                         cudaStream_t st) {
+  BGemm P;
+  P.n = E.n;
+  P.status = E.status;
+  P.nterms = nterms;
+  P.A[0] = A0;
+  P.B[0] = B0;
+  P.s[0] = s0;
+  P.A[1] = A1;
+  P.B[1] = B1;
+  P.s[1] = s1;
+  P.C = C;
+  P.c_add_sq = c_add_sq;
+  P.c_add = c_add;
+  P.c_step = c_step;
+  const int nt = (E.nmax + BG_T - 1) / BG_T;
+  bgemm_kernel<<<dim3(nt * nt, E.count), 256, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+size_t eigen_work_doubles(int n) {
+  return (size_t)std::max<int64_t>(4 * (int64_t)n * n, fallback_ws_doubles(n));
 }
 
 cudaError_t launch_eigen_chain(const EigenBatch& E, cudaStream_t st) {
@@ -801,11 +819,43 @@ cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStrea
   return cudaGetLastError();
 }
 
-cudaError_t launch_eigen_func(const EigenBatch& E, int grid, int mode, cudaStream_t st) {
-  cudaError_t e = cudaMemsetAsync(E.counter, 0, sizeof(unsigned), st);
-  if (e != cudaSuccess) return e;
-  eigen_func_kernel<<<grid, ENT, 0, st>>>(E, mode);
-  return cudaGetLastError();
+cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st) {
+  if (E.count <= 0) return cudaSuccess;
+  const int64_t nn = (int64_t)E.nmax * E.nmax;
+  const int chunks = (int)std::min<int64_t>((nn + 255) / 256, 512);
+  const double* const* Vr = E.Vr;
+  const double* const* Vi = E.Vi;
+  const double* const* W = E.pwork;
+  cudaError_t e;
+  if (mode == 0) {  // E = Qr P^T + Qi R^T
+    func_elem_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E, 0);
+    e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 0, 1), 1.0, bop(Vi, 0, 0), bop(W, 1, 1), 1.0, E.out, 0, 0, 1, st);
+    return e;
+  }
+  if (mode == 1) {  // Re = Qr P^T + Qi R^T, Im = Qi P^T - Qr R^T, interleaved
+    func_elem_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E, 1);
+    e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 0, 1), 1.0, bop(Vi, 0, 0), bop(W, 1, 1), 1.0, E.out, 0, 0, 2, st);
+    if (e != cudaSuccess) return e;
+    return bgemm(E, 2, bop(Vi, 0, 0), bop(W, 0, 1), 1.0, bop(Vr, 0, 0), bop(W, 1, 1), -1.0, E.out, 0, 1, 2, st);
+  }
+  // adjoint: Y = Cbar V, M = V^H Y, M <- conj(Phi) o M, Z = V M, G = Re(Z V^H)
+  const double* const* C = E.cot;
+  double* const* Wm = E.pwork;
+  if ((e = bgemm(E, 1, bop(C, 0, 0), bop(Vr, 0, 0), 1.0, bop(C, 0, 0), bop(Vr, 0, 0), 0.0, Wm, 0, 0, 1, st)))
+    return e;  // Yr
+  if ((e = bgemm(E, 1, bop(C, 0, 0), bop(Vi, 0, 0), 1.0, bop(C, 0, 0), bop(Vi, 0, 0), 0.0, Wm, 1, 0, 1, st)))
+    return e;  // Yi
+  if ((e = bgemm(E, 2, bop(Vr, 0, 1), bop(W, 0, 0), 1.0, bop(Vi, 0, 1), bop(W, 1, 0), 1.0, Wm, 2, 0, 1, st)))
+    return e;  // Mr = Qr^T Yr + Qi^T Yi
+  if ((e = bgemm(E, 2, bop(Vr, 0, 1), bop(W, 1, 0), 1.0, bop(Vi, 0, 1), bop(W, 0, 0), -1.0, Wm, 3, 0, 1, st)))
+    return e;  // Mi = Qr^T Yi - Qi^T Yr
+  func_elem_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E, 2);
+  if ((e = cudaGetLastError())) return e;
+  if ((e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 2, 0), 1.0, bop(Vi, 0, 0), bop(W, 3, 0), -1.0, Wm, 0, 0, 1, st)))
+    return e;  // Zr = Qr Mr - Qi Mi
+  if ((e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 3, 0), 1.0, bop(Vi, 0, 0), bop(W, 2, 0), 1.0, Wm, 1, 0, 1, st)))
+    return e;  // Zi = Qr Mi + Qi Mr
+  return bgemm(E, 2, bop(W, 0, 0), bop(Vr, 0, 1), 1.0, bop(W, 1, 0), bop(Vi, 0, 1), 1.0, E.out, 0, 0, 1, st);
 }
 
 }  // namespace skew

@@ -167,11 +167,16 @@ struct EigenBatch {
   const int64_t* off_w;
   double* const* out;        // [count] exp (real) / cis (complex interleaved) / adjoint (real)
   const double* const* cot;  // [count] cotangents for the adjoint
+  double* const* pwork;      // [count] work + off_w (pointer array for the tiled products)
 };
+// doubles of per-matrix work the eigen kernels need (4 n^2, or more for the fallback of small n)
+size_t eigen_work_doubles(int n);
 cudaError_t launch_eigen_chain(const EigenBatch& E, cudaStream_t st);
 cudaError_t launch_eigen_vectors(const EigenBatch& E, int grid, cudaStream_t st);
 cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStream_t st);
-cudaError_t launch_eigen_func(const EigenBatch& E, int grid, int mode, cudaStream_t st);
+// exp / cis / exp adjoint from (vals, Vr, Vi): elementwise kernels and tiled
+// batched products over the whole GPU (tiles of every matrix in one launch).
+cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st);
 
 // Multi-CTA blocked reduction of one large matrix (skew_blocked.cu).
 size_t blocked_ws_doubles(int n);

@@ -35,11 +35,11 @@
 
 #include "skew_common.cuh"
 #include "skew_internal.h"
+#include "skew_twisted.cuh"
 
 namespace skew {
 
 constexpr int TW_NT = 64;  // threads per CTA of the twisted kernel (one vector each)
-constexpr int TW_PF = 8;   // rows prefetched per chunk
 constexpr int LW = 16;     // half-width of the Lowdin band
 constexpr int WB = 64;     // reflectors per compact-WY panel
 constexpr int SW = 32;     // columns per back-transformation strip
@@ -123,132 +123,8 @@ __global__ void __launch_bounds__(TW_NT) twisted_kernel(const double* __restrict
   // sigma: the k-th eigenvalue (full mode: ascending list; skew mode: descending
   // positive values, then 0 for odd n); padded lanes solve a dummy vector
   const double sig = L.full ? (k < L.K ? vals[k] : vals[L.K - 1]) : ((k < L.h) ? vals[k] : 0.0);
-  const double nsig = neg(sig);
   const double pivmin = bp[1];
-  const double* __restrict__ dg = L.dg;
-#define TW_DIAG(i) (dg ? dg[i] - sig : nsig)
-  double* __restrict__ dp = L.dp;
-  double* __restrict__ dm = L.dm;
-  double* __restrict__ z = L.z;
-
-  // pass 1: T - sigma I = L+ D+ L+^T, D+ stored
-  double d = TW_DIAG(0);
-  for (int i = 0; i < n; i++) {
-    if (fabs(d) <= pivmin) d = neg(pivmin);
-    dp[(int64_t)i * KP + k] = d;
-    if (i + 1 < n) {
-      const double ei = e[i];
-      d = TW_DIAG(i + 1) - (ei * ei) / d;
-    }
-  }
-  // pass 2: T - sigma I = U- D- U-^T (bottom-up), D- stored; twist r = argmin |gamma|
-  double best = INFINITY;
-  int r = n - 1;
-  d = TW_DIAG(n - 1);
-  {
-    double cur[TW_PF], nxt[TW_PF];
-#pragma unroll
-    for (int j = 0; j < TW_PF; j++) cur[j] = (n - 1 - j >= 0) ? dp[(int64_t)(n - 1 - j) * KP + k] : 0.0;
-    for (int i0 = n - 1; i0 >= 0; i0 -= TW_PF) {
-#pragma unroll
-      for (int j = 0; j < TW_PF; j++) {
-        const int i = i0 - TW_PF - j;
-        nxt[j] = (i >= 0) ? dp[(int64_t)i * KP + k] : 0.0;
-      }
-#pragma unroll
-      for (int j = 0; j < TW_PF; j++) {
-        const int i = i0 - j;
-        if (i >= 0) {
-          if (fabs(d) <= pivmin) d = neg(pivmin);
-          dm[(int64_t)i * KP + k] = d;
-          const double g = fabs(cur[j] + d - TW_DIAG(i));  // gamma_i = D+_i + D-_i - (T_ii - sigma)
-          if (g < best) {
-            best = g;
-            r = i;
-          }
-          if (i > 0) {
-            const double ei = e[i - 1];
-            d = TW_DIAG(i - 1) - (ei * ei) / d;
-          }
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < TW_PF; j++) cur[j] = nxt[j];
-    }
-  }
-  // pass 3: z_r = 1; z_i = -(e_i / D+_i) z_{i+1} above r, z_{i+1} = -(e_i / D-_{i+1}) z_i below.
-  // A zero neighbour falls back on the three-term relation of the row between.
-  z[(int64_t)r * KP + k] = 1.0;
-  double nrm = 1.0;
-  int rmax = r, rmin = r;
-  for (int o = 16; o > 0; o >>= 1) {
-    rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-    rmin = min(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
-  }
-  {  // top part, rows rmax-1 .. 0 in lockstep (coalesced), lanes active below their r
-    double z1 = 1.0, z2 = 0.0;
-    double cur[TW_PF], nxt[TW_PF];
-#pragma unroll
-    for (int j = 0; j < TW_PF; j++) cur[j] = (rmax - 1 - j >= 0) ? dp[(int64_t)(rmax - 1 - j) * KP + k] : 1.0;
-    for (int i0 = rmax - 1; i0 >= 0; i0 -= TW_PF) {
-#pragma unroll
-      for (int j = 0; j < TW_PF; j++) {
-        const int i = i0 - TW_PF - j;
-        nxt[j] = (i >= 0) ? dp[(int64_t)i * KP + k] : 1.0;
-      }
-#pragma unroll
-      for (int j = 0; j < TW_PF; j++) {
-        const int i = i0 - j;
-        if (i >= 0 && i < r) {
-          const double ei = e[i];
-          double zi;
-          if (z1 != 0.0)
-            zi = neg(ei / cur[j]) * z1;
-          else
-            zi = (ei != 0.0) ? neg(e[i + 1] / ei) * z2 : 0.0;
-          z[(int64_t)i * KP + k] = zi;
-          nrm = fma(zi, zi, nrm);
-          z2 = z1;
-          z1 = zi;
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < TW_PF; j++) cur[j] = nxt[j];
-    }
-  }
-  {  // bottom part, rows rmin+1 .. n-1, lanes active above their r
-    double z1 = 1.0, z0 = 0.0;  // z_i, z_{i-1}
-    double cur[TW_PF], nxt[TW_PF];
-#pragma unroll
-    for (int j = 0; j < TW_PF; j++) cur[j] = (rmin + 1 + j < n) ? dm[(int64_t)(rmin + 1 + j) * KP + k] : 1.0;
-    for (int i0 = rmin; i0 <= n - 2; i0 += TW_PF) {
-#pragma unroll
-      for (int j = 0; j < TW_PF; j++) {
-        const int i = i0 + TW_PF + j;
-        nxt[j] = (i + 1 < n) ? dm[(int64_t)(i + 1) * KP + k] : 1.0;
-      }
-#pragma unroll
-      for (int j = 0; j < TW_PF; j++) {
-        const int i = i0 + j;
-        if (i <= n - 2 && i >= r) {
-          const double ei = e[i];
-          double zn;
-          if (z1 != 0.0)
-            zn = neg(ei / cur[j]) * z1;
-          else
-            zn = (ei != 0.0 && i > 0) ? neg(e[i - 1] / ei) * z0 : 0.0;
-          z[(int64_t)(i + 1) * KP + k] = zn;
-          nrm = fma(zn, zn, nrm);
-          z0 = z1;
-          z1 = zn;
-        }
-      }
-#pragma unroll
-      for (int j = 0; j < TW_PF; j++) cur[j] = nxt[j];
-    }
-  }
-  L.nrm2[k] = nrm;
-#undef TW_DIAG
+  L.nrm2[k] = twisted_vector(e, L.dg, n, sig, pivmin, KP, k, L.dp, L.dm, L.z);
 }
 
 // ---------------------------------------------------------------------------

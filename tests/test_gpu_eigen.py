@@ -131,3 +131,41 @@ def test_batch_eigen_exp_vjp_mixed(skewgpu, oracle):
         lam = 1j * vals[b].cpu().numpy()
         np.testing.assert_allclose(V @ np.diag(lam) @ V.conj().T, A, atol=1e-11 * max(1, np.abs(A).max()) * np.sqrt(A.shape[0]))
     plan.close()
+
+
+def test_eigen_stagnation_fallback(skewgpu, oracle):
+    """Matrix 274 (n = 200) of the seeded 4096-matrix workload makes the shifts of
+    skewtrieigen_divided! stagnate (the oracle takes the fallback too); the
+    batched eigen must take the reference's fallback (skewtrieigen_backup!:
+    values descending, fallback eigenvector layout) and still reconstruct A."""
+    import torch
+
+    import bench
+
+    sizes = bench.workload_sizes()[:275]
+    buf, offs = bench.packed_inputs(sizes)
+    A = buf[offs[274]:offs[274] + 200 * 200].reshape(200, 200, order="F")
+    assert oracle.eigen(A)[3] != 0
+    mats = [A, skew_random(31, 3), skew_random(200, 4)]
+    ns = [m.shape[0] for m in mats]
+    plan = skewgpu.BatchPlan(ns)
+    devs = [skewgpu.to_device(M) for M in mats]
+    vals = [torch.zeros(n, dtype=torch.float64, device="cuda") for n in ns]
+    Vr = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in ns]
+    Vi = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in ns]
+    st = plan.eigen(plan.pointer_array(devs), plan.pointer_array(vals), plan.pointer_array(Vr),
+                    plan.pointer_array(Vi))
+    torch.cuda.synchronize()
+    st = st.cpu().numpy()
+    assert st[0] == 8 and st[1] == 0 and st[2] == 0
+    for b, M in enumerate(mats):
+        v = vals[b].cpu().numpy()
+        V = skewgpu.from_device(Vr[b]) + 1j * skewgpu.from_device(Vi[b])
+        rho = np.abs(v).max()
+        if b == 0:
+            assert np.all(np.diff(v) <= 0.0)  # the fallback's order
+            vq, _ = oracle.eigvals(M, quad=True)
+            np.testing.assert_allclose(v, np.sort(vq)[::-1], atol=1e-11 * rho)
+        np.testing.assert_allclose(V.conj().T @ V, np.eye(ns[b]), atol=1e-11)
+        np.testing.assert_allclose(V @ np.diag(1j * v) @ V.conj().T, M, atol=1e-11 * rho)
+    plan.close()
