@@ -173,6 +173,7 @@ def main():
     ap.add_argument("--only-large", action="store_true", help="run only the single-matrix hessenberg leg")
     ap.add_argument("--no-legs", action="store_true", help="skip the eigvals / n=512 / adjoint legs")
     ap.add_argument("--only-legs", action="store_true", help="run only the eigvals / n=512 / adjoint legs")
+    ap.add_argument("--leg", default=None, help="with --only-legs: run only this leg (profiling)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -187,12 +188,13 @@ def main():
         buf, offs = packed_inputs(sizes)
         d_in = torch.from_numpy(buf).to("cuda")
         plan = skewgpu.BatchPlan(sizes)
-        out = {"eigvals_batched": leg_eigvals_batched(plan, d_in, offs, sizes, max(1, args.steps)),
-               "plain_n512": leg_plain_n512(peak, cpu=not args.no_cpu),
-               "pfaffian_adjoint_1024x128": leg_pfaffian_adjoint(peak, max(1, args.steps)),
-               "exp_adjoint_512_mixed": leg_exp_adjoint(peak, max(1, min(args.steps, 3))),
-               "exp_adjoint_complex_64x256": leg_complex_exp_adjoint(peak),
-               "complex_n4096": leg_complex_large(4096, peak)}
+        legs = {"eigvals_batched": lambda: leg_eigvals_batched(plan, d_in, offs, sizes, max(1, args.steps)),
+                "plain_n512": lambda: leg_plain_n512(peak, cpu=not args.no_cpu),
+                "pfaffian_adjoint_1024x128": lambda: leg_pfaffian_adjoint(peak, max(1, args.steps)),
+                "exp_adjoint_512_mixed": lambda: leg_exp_adjoint(peak, max(1, min(args.steps, 3))),
+                "exp_adjoint_complex_64x256": lambda: leg_complex_exp_adjoint(peak),
+                "complex_n4096": lambda: leg_complex_large(4096, peak)}
+        out = {k: f() for k, f in legs.items() if args.leg is None or k == args.leg}
         plan.close()
         print(json.dumps({"legs": out}), flush=True)
         return 0
