@@ -19,6 +19,9 @@
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
+#include <stdlib.h>
+
+#include <algorithm>
 
 #include "skew_common.cuh"
 #include "skew_internal.h"
@@ -944,12 +947,25 @@ cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double*
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persist_kernel, P_NT, smem);
   if (e != cudaSuccess) return e;
   if (occ < 1) return cudaErrorNotSupported;
-  const int grid = sms * (occ >= 2 ? 2 : 1);  // two CTAs per SM hide more load latency
+  // Two CTAs per SM hide more load latency on large matrices; below that, the two
+  // grid barriers per column cost more than the extra CTAs bring.
+  // SKEW_PERSIST_CTAS / SKEW_PERSIST_TAIL override the grid and the columns left
+  // to the one-CTA kernel (sweeps).
+  // measured on GB300: one CTA per SM is 14-22 % faster for n <= 2048, two per
+  // SM break even at n = 4096
+  int grid = sms * ((occ >= 2 && n > 3072) ? 2 : 1);
+  int tail = TAIL;
+  {
+    const char* g = getenv("SKEW_PERSIST_CTAS");
+    const char* t = getenv("SKEW_PERSIST_TAIL");
+    if (g && *g) grid = std::max(1, std::min(grid, atoi(g)));
+    if (t && *t) tail = std::max(32, std::min(TAIL, atoi(t)));
+  }
   PersistParams P;
   P.A = A;
   P.lda = lda;
   P.n = n;
-  P.pend = n - TAIL;
+  P.pend = n - tail;
   P.tau = tau;
   P.ev = ev;
   P.W = ws.W;
