@@ -290,7 +290,7 @@ __device__ void cta_fallback(const double* __restrict__ e, int N, double* __rest
     if (kb + (tid & ~31) >= KP) continue;
     const int k = kb + tid;
     const double sig = (k < h) ? vals[k] : 0.0;
-    nrm2[k] = twisted_vector(e, nullptr, N, sig, pivmin, KP, k, dp, dm, z);
+    nrm2[k] = twisted_vector(e, nullptr, N, sig, pivmin, KP, k, 0, N, dp, dm, z);
   }
   __syncthreads();
   // unit even-row and odd-row parts: X(i,k) = s_k z(i,k), s_k = sqrt(2)/|z_k| (sigma > 0)

@@ -124,7 +124,43 @@ __global__ void __launch_bounds__(TW_NT) twisted_kernel(const double* __restrict
   // positive values, then 0 for odd n); padded lanes solve a dummy vector
   const double sig = L.full ? (k < L.K ? vals[k] : vals[L.K - 1]) : ((k < L.h) ? vals[k] : 0.0);
   const double pivmin = bp[1];
-  L.nrm2[k] = twisted_vector(e, L.dg, n, sig, pivmin, KP, k, L.dp, L.dm, L.z);
+  // copy index j among equal eigenvalues (the list is sorted) -> the block of rows
+  const double scale = L.full ? fmax(fabs(bp[0]), fabs(bp[2])) : bp[0];
+  // 8 times the bisection tolerance, and above the pivot guard (counts cannot
+  // resolve below pivmin: a zero matrix has only eigenvalues there)
+  const double delta = fmax(16.0 * 2.220446049250313e-16 * (scale + fabs(sig)), 4.0 * pivmin);
+  int lo = 0, hi = n;
+  if (k < L.K) {
+    int j = 0;
+    for (int q = k - 1; q >= 0; q--) {
+      const double sq = L.full ? vals[q] : ((q < L.h) ? vals[q] : 0.0);
+      if (fabs(sq - sig) > delta) break;
+      j++;
+    }
+    tdvec_block(e, L.dg, n, sig, delta, j, pivmin, &lo, &hi);
+  }
+  L.nrm2[k] = twisted_vector(e, L.dg, n, sig, pivmin, KP, k, lo, hi, L.dp, L.dm, L.z);
+}
+
+// unit parts: X(i,k) = s_k z(i,k).  Skew mode: even-row and odd-row parts each of
+// unit length, s_k = sqrt(2)/|z_k| (sigma > 0) or 1/|z_k| (the zero-eigenvalue
+// vector, even rows only); full mode: s_k = 1/|z_k|.  X may be L.dp.
+__global__ void tdvec_normalize_kernel(TdvecLayout L0, double* X0) {
+  const TdvecLayout L = at_problem(L0, blockIdx.z);
+  double* X = X0 + (size_t)blockIdx.z * L0.mstride;
+  const int64_t KP = L.KP;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < (int64_t)L.n * KP;
+       q += (int64_t)gridDim.x * blockDim.x) {
+    const int i = (int)(q / KP), k = (int)(q - (int64_t)i * KP);
+    double x = 0.0;
+    if (k < L.K) {
+      if (L.full)
+        x = rsqrt(L.nrm2[k]) * L.z[q];
+      else if (!((i & 1) && k >= L.h))
+        x = ((k < L.h) ? 1.4142135623730951 : 1.0) * rsqrt(L.nrm2[k]) * L.z[q];
+    }
+    X[q] = x;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -136,8 +172,9 @@ constexpr int BD_COLS = 32 + LW;
 constexpr int BD_PAIRS = 32 * (LW + 1);
 constexpr int BD_PER = (BD_PAIRS + BD_NT - 1) / BD_NT;
 
-__global__ void __launch_bounds__(BD_NT) band_dots_kernel(TdvecLayout L0) {
+__global__ void __launch_bounds__(BD_NT) band_dots_kernel(TdvecLayout L0, const double* X0) {
   const TdvecLayout L = at_problem(L0, blockIdx.z);
+  const double* X = X0 + (size_t)blockIdx.z * L0.mstride;
   __shared__ double zs[RC][BD_COLS + 1];
   const int k0 = blockIdx.x * 32;
   const int n = L.n;
@@ -150,7 +187,7 @@ __global__ void __launch_bounds__(BD_NT) band_dots_kernel(TdvecLayout L0) {
     for (int idx = threadIdx.x; idx < RC * BD_COLS; idx += BD_NT) {
       const int rr = idx / BD_COLS, cc = idx - rr * BD_COLS;
       const int i = i0 + rr, k = k0 + cc;
-      zs[rr][cc] = (i < n && k < L.K) ? L.z[(int64_t)i * KP + k] : 0.0;
+      zs[rr][cc] = (i < n && k < L.K) ? X[(int64_t)i * KP + k] : 0.0;
     }
     __syncthreads();
 #pragma unroll
@@ -180,72 +217,85 @@ __global__ void __launch_bounds__(BD_NT) band_dots_kernel(TdvecLayout L0) {
   }
 }
 
-// scale s_k that makes the even-row (or odd-row) part of vector k a unit vector:
-// sqrt(2)/|z_k| for sigma_k > 0, 1/|z_k| for the zero-eigenvalue vector (no odd part)
-__device__ __forceinline__ double part_scale(const TdvecLayout& L, int k) {
-  if (k >= L.K) return 0.0;
-  const double inv = rsqrt(L.nrm2[k]);
-  return (k < L.h) ? 1.4142135623730951 * inv : inv;
-}
-
 // ---------------------------------------------------------------------------
-// 3-4. Lowdin-corrected vectors, written in the tridiagonal basis into the
-//      columns of Vr / Vi that hold the -sigma eigenvectors
+// 3. one symmetric correction pass  Y = X - 1/2 X E  over the band,
+//    E(k, j) = X_k . X_j - delta_kj per part (skew mode: even rows / odd rows;
+//    the zero-eigenvalue vector has no odd part; full mode: all rows)
 // ---------------------------------------------------------------------------
 constexpr int LA_NT = 256;
 constexpr int LA_COLS = 32 + 2 * LW;
 
-__global__ void __launch_bounds__(LA_NT) lowdin_apply_kernel(TdvecLayout L, double* __restrict__ Vr,
-                                                             double* __restrict__ Vi, int64_t ldv) {
-  __shared__ double zs[RC][LA_COLS + 1];
-  __shared__ double sc[LA_COLS];
+__global__ void __launch_bounds__(LA_NT) band_apply_kernel(TdvecLayout L0, const double* X0, double* Y0) {
+  const TdvecLayout L = at_problem(L0, blockIdx.z);
+  const double* X = X0 + (size_t)blockIdx.z * L0.mstride;
+  double* Y = Y0 + (size_t)blockIdx.z * L0.mstride;
+  __shared__ double xs[RC][LA_COLS + 1];
   __shared__ double eU[32][2 * LW + 1], eV[32][2 * LW + 1];
-  __shared__ double out[RC][33];
   const int k0 = blockIdx.x * 32, i0 = blockIdx.y * RC;
   const int n = L.n;
   const int64_t KP = L.KP;
-  for (int c = threadIdx.x; c < LA_COLS; c += LA_NT) sc[c] = (k0 - LW + c >= 0) ? part_scale(L, k0 - LW + c) : 0.0;
   for (int idx = threadIdx.x; idx < RC * LA_COLS; idx += LA_NT) {
     const int rr = idx / LA_COLS, cc = idx - rr * LA_COLS;
     const int i = i0 + rr, k = k0 - LW + cc;
-    zs[rr][cc] = (i < n && k >= 0 && k < L.K) ? L.z[(int64_t)i * KP + k] : 0.0;
+    xs[rr][cc] = (i < n && k >= 0 && k < L.K) ? X[(int64_t)i * KP + k] : 0.0;
   }
-  __syncthreads();
-  // normalised band E(k, k+d) = s_k s_{k+d} dot - delta, d in [-LW, LW]
   for (int idx = threadIdx.x; idx < 32 * (2 * LW + 1); idx += LA_NT) {
     const int kk = idx / (2 * LW + 1), dd = idx - kk * (2 * LW + 1) - LW;
     const int k = k0 + kk, j = k + dd;
     double u = 0.0, v = 0.0;
     if (k < L.K && j >= 0 && j < L.K) {
       const int lo = min(k, j), off = abs(dd);
-      const double s = sc[kk + LW] * sc[kk + LW + dd];
-      u = s * L.bandU[(int64_t)lo * (LW + 1) + off] - (dd == 0 ? 1.0 : 0.0);
-      const bool zk = (k >= L.h), zj = (j >= L.h);  // the zero-eigenvalue vector has no odd part
-      v = (zk || zj) ? 0.0 : s * L.bandV[(int64_t)lo * (LW + 1) + off] - (dd == 0 ? 1.0 : 0.0);
+      const double du = L.bandU[(int64_t)lo * (LW + 1) + off], dv = L.bandV[(int64_t)lo * (LW + 1) + off];
+      const double id = (dd == 0) ? 1.0 : 0.0;
+      if (L.full) {
+        u = v = du + dv - id;
+      } else {
+        u = du - id;
+        v = (k >= L.h || j >= L.h) ? 0.0 : dv - id;
+      }
     }
     eU[kk][dd + LW] = u;
     eV[kk][dd + LW] = v;
   }
   __syncthreads();
-  // out(i, k) = s_k z(i,k) - 1/2 sum_d E(k,k+d) s_{k+d} z(i,k+d), then back to |w| = 1 scale
   for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
-    const int kk = idx / RC, rr = idx - kk * RC;  // consecutive threads: consecutive rows
+    const int kk = idx % 32, rr = idx / 32;  // consecutive threads: consecutive k (interleaved rows)
+    const int i = i0 + rr, k = k0 + kk;
+    if (i >= n || k >= KP) continue;
+    double acc = xs[rr][kk + LW];
+    if (k < L.K) {
+      const double(*E)[2 * LW + 1] = (i & 1) ? eV : eU;
+#pragma unroll 11
+      for (int dd = -LW; dd <= LW; dd++) acc = fma(-0.5 * E[kk][dd + LW], xs[rr][kk + LW + dd], acc);
+    }
+    Y[(int64_t)i * KP + k] = acc;
+  }
+}
+
+// skew mode: the -sigma eigenvectors in the tridiagonal basis into the columns n-1-k
+// of Vr / Vi (real on even 0-based rows, imaginary on odd rows, sign flipped every
+// pair, |w| = 1); the zero-eigenvalue vector (odd n) into column h
+__global__ void __launch_bounds__(LA_NT) tdvec_write_skew_kernel(TdvecLayout L, const double* __restrict__ X,
+                                                                 double* __restrict__ Vr, double* __restrict__ Vi,
+                                                                 int64_t ldv) {
+  __shared__ double out[RC][33];
+  const int k0 = blockIdx.x * 32, i0 = blockIdx.y * RC;
+  const int n = L.n;
+  const int64_t KP = L.KP;
+  for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
+    const int kk = idx % 32, rr = idx / 32;
     const int i = i0 + rr, k = k0 + kk;
     double o = 0.0;
     if (i < n && k < L.K) {
-      const double(*E)[2 * LW + 1] = (i & 1) ? eV : eU;
-      double acc = sc[kk + LW] * zs[rr][kk + LW];
-#pragma unroll 11
-      for (int dd = -LW; dd <= LW; dd++) acc = fma(-0.5 * E[kk][dd + LW], sc[kk + LW + dd] * zs[rr][kk + LW + dd], acc);
-      o = (k < L.h) ? acc * 0.7071067811865476 : acc;
-      if ((i >> 1) & 1) o = neg(o);  // fallback pattern: sign flips every (odd, even) pair
+      o = X[(int64_t)i * KP + k];
+      if (k < L.h) o *= 0.7071067811865476;
+      if ((i >> 1) & 1) o = neg(o);
     }
     out[rr][kk] = o;
   }
   __syncthreads();
-  // column of the -sigma_k eigenvector: n-1-k; the zero-eigenvalue vector: column h
   for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
-    const int kk = idx / RC, rr = idx - kk * RC;
+    const int kk = idx / RC, rr = idx - kk * RC;  // consecutive threads: consecutive rows of a column
     const int i = i0 + rr, k = k0 + kk;
     if (i >= n || k >= L.K) continue;
     const int col = (k < L.h) ? n - 1 - k : L.h;
@@ -260,58 +310,43 @@ __global__ void __launch_bounds__(LA_NT) lowdin_apply_kernel(TdvecLayout L, doub
   }
 }
 
-// Full mode: Y(:, k) = s_k z_k - 1/2 sum_d E(k, k+d) s_{k+d} z_{k+d}, with
-// s_k = 1/|z_k| and E the normalised Gram band over all rows.  Y is n x n, ld n.
-__global__ void __launch_bounds__(LA_NT) lowdin_full_kernel(TdvecLayout L0, double* __restrict__ Y) {
-  const TdvecLayout L = at_problem(L0, blockIdx.z);
-  Y += (size_t)blockIdx.z * L.n * L.n;
-  __shared__ double zs[RC][LA_COLS + 1];
-  __shared__ double sc[LA_COLS];
-  __shared__ double eA[32][2 * LW + 1];
+// full mode: Y(:, k) = X(:, k) (n x n, ld n), problem blockIdx.z n^2 apart
+__global__ void __launch_bounds__(LA_NT) tdvec_write_full_kernel(TdvecLayout L0, const double* X0, double* Y) {
   __shared__ double out[RC][33];
+  const int n = L0.n;
+  const double* X = X0 + (size_t)blockIdx.z * L0.mstride;
+  Y += (size_t)blockIdx.z * n * n;
   const int k0 = blockIdx.x * 32, i0 = blockIdx.y * RC;
-  const int n = L.n;
-  const int64_t KP = L.KP;
-  for (int c = threadIdx.x; c < LA_COLS; c += LA_NT) {
-    const int k = k0 - LW + c;
-    sc[c] = (k >= 0 && k < L.K) ? rsqrt(L.nrm2[k]) : 0.0;
-  }
-  for (int idx = threadIdx.x; idx < RC * LA_COLS; idx += LA_NT) {
-    const int rr = idx / LA_COLS, cc = idx - rr * LA_COLS;
-    const int i = i0 + rr, k = k0 - LW + cc;
-    zs[rr][cc] = (i < n && k >= 0 && k < L.K) ? L.z[(int64_t)i * KP + k] : 0.0;
-  }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < 32 * (2 * LW + 1); idx += LA_NT) {
-    const int kk = idx / (2 * LW + 1), dd = idx - kk * (2 * LW + 1) - LW;
-    const int k = k0 + kk, j = k + dd;
-    double u = 0.0;
-    if (k < L.K && j >= 0 && j < L.K) {
-      const int lo = min(k, j), off = abs(dd);
-      const double g = L.bandU[(int64_t)lo * (LW + 1) + off] + L.bandV[(int64_t)lo * (LW + 1) + off];
-      u = sc[kk + LW] * sc[kk + LW + dd] * g - (dd == 0 ? 1.0 : 0.0);
-    }
-    eA[kk][dd + LW] = u;
+  const int64_t KP = L0.KP;
+  for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
+    const int kk = idx % 32, rr = idx / 32;
+    const int i = i0 + rr, k = k0 + kk;
+    out[rr][kk] = (i < n && k < L0.K) ? X[(int64_t)i * KP + k] : 0.0;
   }
   __syncthreads();
   for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
     const int kk = idx / RC, rr = idx - kk * RC;
     const int i = i0 + rr, k = k0 + kk;
-    double o = 0.0;
-    if (i < n && k < L.K) {
-      double acc = sc[kk + LW] * zs[rr][kk + LW];
-#pragma unroll 11
-      for (int dd = -LW; dd <= LW; dd++) acc = fma(-0.5 * eA[kk][dd + LW], sc[kk + LW + dd] * zs[rr][kk + LW + dd], acc);
-      o = acc;
-    }
-    out[rr][kk] = o;
+    if (i < n && k < L0.K) Y[i + (int64_t)k * n] = out[rr][kk];
   }
-  __syncthreads();
-  for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
-    const int kk = idx / RC, rr = idx - kk * RC;
-    const int i = i0 + rr, k = k0 + kk;
-    if (i < n && k < L.K) Y[i + (int64_t)k * n] = out[rr][kk];
+}
+
+// normalise, then three correction passes (each squares the departure from
+// orthogonality; clusters of nearly equal eigenvalues need more than one);
+// returns the array holding the result (L.dp or L.dm)
+static double* tdvec_orthogonalize(const TdvecLayout& L, int batch, cudaStream_t st) {
+  const int64_t tot = (int64_t)L.n * L.KP;
+  tdvec_normalize_kernel<<<dim3((unsigned)std::min<int64_t>((tot + 255) / 256, 4096), 1, batch), 256, 0, st>>>(L, L.dp);
+  double* X = L.dp;
+  double* Y = L.dm;
+  for (int pass = 0; pass < 3; pass++) {
+    band_dots_kernel<<<dim3(L.KP / 32, 1, batch), BD_NT, 0, st>>>(L, X);
+    band_apply_kernel<<<dim3(L.KP / 32, (L.n + RC - 1) / RC, batch), LA_NT, 0, st>>>(L, X, Y);
+    double* t = X;
+    X = Y;
+    Y = t;
   }
+  return X;
 }
 
 // Eigenvectors of the symmetric tridiagonal with diagonal dg and off-diagonal e
@@ -324,10 +359,8 @@ cudaError_t symtri_vectors(const double* dg, const double* e, int n, const doubl
   twisted_kernel<<<dim3(L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), 1, batch), TW_NT, 0, st>>>(e, mu, bp, L);
   cudaError_t err = cudaGetLastError();
   if (err != cudaSuccess) return err;
-  band_dots_kernel<<<dim3(L.KP / 32, 1, batch), BD_NT, 0, st>>>(L);
-  err = cudaGetLastError();
-  if (err != cudaSuccess) return err;
-  lowdin_full_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC, batch), LA_NT, 0, st>>>(L, Y);
+  double* X = tdvec_orthogonalize(L, batch, st);
+  tdvec_write_full_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC, batch), LA_NT, 0, st>>>(L, X, Y);
   return cudaGetLastError();
 }
 
@@ -573,10 +606,8 @@ cudaError_t large_eigen_vectors(const double* A, int64_t lda, int n, const doubl
   twisted_kernel<<<L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), TW_NT, 0, st>>>(ev, vals, bp, L);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  band_dots_kernel<<<L.KP / 32, BD_NT, 0, st>>>(L);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  lowdin_apply_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC), LA_NT, 0, st>>>(L, Vr, Vi, ldv);
+  double* X = tdvec_orthogonalize(L, 1, st);
+  tdvec_write_skew_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC), LA_NT, 0, st>>>(L, X, Vr, Vi, ldv);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   wy_factor_kernel<<<L.npan, WT_NT, 0, st>>>(A, lda, tau, L);

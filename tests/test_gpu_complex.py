@@ -154,3 +154,27 @@ def test_batch_complex_eigen_exp_vjp(skewgpu, n):
         Z = np.zeros((n, n), dtype=np.complex128)
         Gref = sl.expm(np.block([[A.conj().T, cots[b]], [Z, A.conj().T]]))[:n, n:]
         np.testing.assert_allclose(Gs[b], Gref, atol=1e-10 * np.abs(Gref).max())
+
+
+def test_eigen_complex_repeated_eigenvalues(skewgpu):
+    """Exact splits with repeated eigenvalues: i*diag(1, 1, 2, 1), a direct sum of
+    two equal blocks, and the same at n > 1024 (the reference's LAPACK handles
+    these; each copy of an eigenvalue must get its own block's vector)."""
+    cases = [np.diag(1j * np.array([1.0, 1.0, 2.0, 1.0])), np.diag(1j * np.zeros(5))]
+    Bk = skewh_random(40, 2)
+    D = np.zeros((80, 80), dtype=np.complex128)
+    D[:40, :40] = Bk
+    D[40:, 40:] = Bk
+    cases.append(D)
+    Bl = skewh_random(600, 3)
+    Dl = np.zeros((1200, 1200), dtype=np.complex128)
+    Dl[:600, :600] = Bl
+    Dl[600:, 600:] = Bl
+    cases.append(Dl)
+    for A in cases:
+        n = A.shape[0]
+        lam, V = skewgpu.eigen_complex(A)
+        rho = max(np.abs(lam).max(), 1.0)
+        np.testing.assert_allclose(lam.imag, -np.linalg.eigvalsh(1j * A), atol=1e-11 * rho)
+        np.testing.assert_allclose(V.conj().T @ V, np.eye(n), atol=1e-11)
+        np.testing.assert_allclose(V @ np.diag(lam) @ V.conj().T, A, atol=1e-11 * rho)

@@ -77,3 +77,13 @@ def test_large_eigvals_agree(skewgpu):
     lam, _ = skewgpu.eigen(A)
     v = skewgpu.eigvals(A)
     np.testing.assert_array_equal(lam.imag, v.imag)
+
+
+def test_large_eigen_identical_blocks(skewgpu, oracle):
+    """A direct sum of two identical blocks: the tridiagonal splits exactly and
+    every eigenvalue is double; each copy must get its own block's vector."""
+    B = skew_random(560, 21)
+    A = np.zeros((1120, 1120))
+    A[:560, :560] = B
+    A[560:, 560:] = B
+    _check(skewgpu, oracle, A)
