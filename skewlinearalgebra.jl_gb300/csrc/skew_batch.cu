@@ -769,9 +769,23 @@ static int global_threads() {
   return nt;
 }
 
+// Shared-memory buckets: SKEW_BATCH_SMEM_NT_SMALL (128 | 256) for n <= 96 and
+// SKEW_BATCH_SMEM_NT_LARGE (256 | 512) above (sweeps).
+static int smem_threads(bool small) {
+  static const int s = [] {
+    const char* v = getenv("SKEW_BATCH_SMEM_NT_SMALL");
+    return (v && atoi(v) == 256) ? 256 : NT_SMALL;
+  }();
+  static const int l = [] {
+    const char* v = getenv("SKEW_BATCH_SMEM_NT_LARGE");
+    return (v && atoi(v) == 512) ? 512 : NT_LARGE;
+  }();
+  return small ? s : l;
+}
+
 static int threads_for(int nmax, bool smem_matrix) {
   if (!smem_matrix) return global_threads();
-  return nmax <= 96 ? NT_SMALL : NT_LARGE;
+  return smem_threads(nmax <= 96);
 }
 
 size_t batch_smem_bytes(int nmax, bool smem_matrix) {
@@ -798,8 +812,9 @@ cudaError_t launch_batch_pf(const BatchParams& P, int grid, cudaStream_t st, boo
   const bool sm = P.smem_matrix != 0;
   const size_t smem = batch_smem_bytes(P.nmax, sm);
   const int nt = threads_for(P.nmax, sm);
-  if (sm && nt == NT_SMALL) return launch_t<NT_SMALL, true>(P, grid, smem, st, tridiag_only);
-  if (sm) return launch_t<NT_LARGE, true>(P, grid, smem, st, tridiag_only);
+  if (sm && nt == 128) return launch_t<128, true>(P, grid, smem, st, tridiag_only);
+  if (sm && nt == 256) return launch_t<256, true>(P, grid, smem, st, tridiag_only);
+  if (sm) return launch_t<512, true>(P, grid, smem, st, tridiag_only);
   if (nt == NT_LARGE) return launch_t<NT_LARGE, false>(P, grid, smem, st, tridiag_only);
   return launch_t<NT_GLOBAL, false>(P, grid, smem, st, tridiag_only);
 }
@@ -831,8 +846,9 @@ static int occ_t(size_t smem) {
 int batch_occupancy(int nmax, bool smem_matrix) {
   const size_t smem = batch_smem_bytes(nmax, smem_matrix);
   const int nt = threads_for(nmax, smem_matrix);
-  if (smem_matrix && nt == NT_SMALL) return occ_t<NT_SMALL, true>(smem);
-  if (smem_matrix) return occ_t<NT_LARGE, true>(smem);
+  if (smem_matrix && nt == 128) return occ_t<128, true>(smem);
+  if (smem_matrix && nt == 256) return occ_t<256, true>(smem);
+  if (smem_matrix) return occ_t<512, true>(smem);
   if (nt == NT_LARGE) return occ_t<NT_LARGE, false>(smem);
   return occ_t<NT_GLOBAL, false>(smem);
 }
