@@ -43,6 +43,25 @@ typedef enum {
   SKEW_TIMEOUT = 9          /* a bounded device-side wait gave up; outputs are not valid */
 } skew_status_t;
 
+/* Matrix functions of a skew matrix from its eigendecomposition (exp.jl:3-283):
+ * F = V diag(f(lambda)) V^H; cos/cosh are returned Hermitian (symmetric), sin, sinh,
+ * tan, tanh, cot, coth skew(-Hermitian), as the reference's Hermitian / skewhermitian!
+ * wrappers.  sincos is SKEW_FUNC_SIN and SKEW_FUNC_COS.  log, cot, coth of a matrix
+ * with a zero eigenvalue (every odd n) report SKEW_SINGULAR (the reference's
+ * DomainError / singular solve). */
+typedef enum {
+  SKEW_FUNC_EXP = 0,
+  SKEW_FUNC_COS = 1,
+  SKEW_FUNC_SIN = 2,
+  SKEW_FUNC_COSH = 3,
+  SKEW_FUNC_SINH = 4,
+  SKEW_FUNC_TAN = 5,
+  SKEW_FUNC_TANH = 6,
+  SKEW_FUNC_COT = 7,
+  SKEW_FUNC_COTH = 8,
+  SKEW_FUNC_LOG = 9
+} skew_func_t;
+
 typedef struct skew_handle_st* skew_handle_t;
 typedef struct skew_batch_plan_st* skew_batch_plan_t;
 
@@ -195,6 +214,20 @@ SKEW_API int skew_batch_exp_z(skew_handle_t h, const double* A, int64_t n, int64
 /* Adjoint of exp for every matrix: G_b = V_b (conj(Phi_b) o (V_b^H Cbar_b V_b)) V_b^H. */
 SKEW_API int skew_batch_exp_vjp_z(skew_handle_t h, const double* A, int64_t n, int64_t count, const double* Cbar,
                                   double* G, int* status);
+
+/* Base.cos/sin/sinh/cosh/tan/tanh/cot/coth/log(A::SkewHermitian{Float64})  exp.jl:50-283
+ * (and exp): F = f(A) (real n x n, ldf).  A is destroyed; lda == ldf == n, n <= 1024. */
+SKEW_API int skew_func_d(skew_handle_t h, double* A, int64_t n, int64_t lda, int func, double* F, int64_t ldf,
+                         int* info);
+/* The same for every matrix of a batch plan: F[b] (n[b] x n[b], leading dimension n[b]). */
+SKEW_API int skew_batch_func_d(skew_batch_plan_t plan, const double* const* A, int func, double* const* F,
+                               int* status);
+/* ComplexF64: F = f(A) (ComplexF64, ldf).  A is destroyed. */
+SKEW_API int skew_func_z(skew_handle_t h, double* A, int64_t n, int64_t lda, int func, double* F, int64_t ldf,
+                         int* info);
+/* ComplexF64 batches of one size (matrices back to back, as skew_batch_exp_z). */
+SKEW_API int skew_batch_func_z(skew_handle_t h, const double* A, int64_t n, int64_t count, int func, double* F,
+                               int* status);
 
 /* Diagnostics: measured FP64 DFMA throughput of the current device in TFLOP/s
  * (runs a short microbenchmark on the handle's stream and synchronizes). */

@@ -645,6 +645,7 @@ static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const*
   E.out = nullptr;
   E.cot = nullptr;
   E.pwork = P->e_p_work;
+  E.func = SKEW_FUNC_EXP;
   const int grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
   CK(launch_eigen_chain(E, st));
   CK(launch_eigen_vectors(E, grid, st));
@@ -674,30 +675,32 @@ int skew_batch_eigen_d(skew_batch_plan_t P, const double* const* A, double* cons
 }
 
 static int func_issue(skew_batch_plan_t P, const double* const* A, double* const* out, const double* const* cot,
-                      int mode, int* status);
+                      int mode, int func, int* status);
 
-// exp / cis / exp adjoint as one graph per mode (batched entry points).
+// matrix functions / cis / exp adjoint as one graph per mode (batched entry points);
+// the function id is part of the key, so another function re-captures
 static int func_run_graph(skew_batch_plan_t P, const double* const* A, double* const* out,
-                          const double* const* cot, int mode, int* status) {
+                          const double* const* cot, int mode, int func, int* status) {
   int s = eigen_ws(P);
   if (s) return s;
   const GraphOp op = mode == 0 ? G_EXP : (mode == 1 ? G_CIS : G_EXPVJP);
-  return graph_issue(P, op, {A, out, cot, status, nullptr, nullptr},
-                     [&] { return func_issue(P, A, out, cot, mode, status); });
+  return graph_issue(P, op, {A, out, cot, status, reinterpret_cast<const void*>((intptr_t)func), nullptr},
+                     [&] { return func_issue(P, A, out, cot, mode, func, status); });
 }
 
 static int func_run(skew_batch_plan_t P, const double* const* A, double* const* out, const double* const* cot,
-                    int mode, int* status) {
-  return func_issue(P, A, out, cot, mode, status);
+                    int mode, int func, int* status) {
+  return func_issue(P, A, out, cot, mode, func, status);
 }
 
 static int func_issue(skew_batch_plan_t P, const double* const* A, double* const* out, const double* const* cot,
-                      int mode, int* status) {
+                      int mode, int func, int* status) {
   EigenBatch E;
   int s = eigen_run(P, A, nullptr, nullptr, nullptr, &E);
   if (s) return s;
   E.out = out;
   E.cot = cot;
+  E.func = func;
   CK(launch_eigen_func(E, mode, P->h->stream));
   return finish_status(P, status);
 }
@@ -705,20 +708,26 @@ static int func_issue(skew_batch_plan_t P, const double* const* A, double* const
 int skew_batch_exp_d(skew_batch_plan_t P, const double* const* A, double* const* E, int* status) {
   if (!P || (P->count > 0 && (!A || !E))) return SKEW_BAD_ARG;
   if (P->count == 0) return SKEW_OK;
-  return func_run_graph(P, A, E, nullptr, 0, status);
+  return func_run_graph(P, A, E, nullptr, 0, SKEW_FUNC_EXP, status);
+}
+
+int skew_batch_func_d(skew_batch_plan_t P, const double* const* A, int func, double* const* F, int* status) {
+  if (!P || (P->count > 0 && (!A || !F)) || func < SKEW_FUNC_EXP || func > SKEW_FUNC_LOG) return SKEW_BAD_ARG;
+  if (P->count == 0) return SKEW_OK;
+  return func_run_graph(P, A, F, nullptr, 0, func, status);
 }
 
 int skew_batch_cis_d(skew_batch_plan_t P, const double* const* A, double* const* C, int* status) {
   if (!P || (P->count > 0 && (!A || !C))) return SKEW_BAD_ARG;
   if (P->count == 0) return SKEW_OK;
-  return func_run_graph(P, A, C, nullptr, 1, status);
+  return func_run_graph(P, A, C, nullptr, 1, SKEW_FUNC_EXP, status);
 }
 
 int skew_batch_exp_vjp_d(skew_batch_plan_t P, const double* const* A, const double* const* Cbar, double* const* G,
                          int* status) {
   if (!P || (P->count > 0 && (!A || !Cbar || !G))) return SKEW_BAD_ARG;
   if (P->count == 0) return SKEW_OK;
-  return func_run_graph(P, A, G, Cbar, 2, status);
+  return func_run_graph(P, A, G, Cbar, 2, SKEW_FUNC_EXP, status);
 }
 
 // Single matrices run as a batch of one through a plan cached on the handle.
@@ -744,7 +753,8 @@ static int single_plan(skew_handle_t h, int64_t n, skew_batch_plan_t* out) {
 }
 
 static int single_func(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,
-                       int64_t ldv, double* out, int64_t ldo, const double* cot, int mode, int* info) {
+                       int64_t ldv, double* out, int64_t ldo, const double* cot, int mode, int* info,
+                       int func = SKEW_FUNC_EXP) {
   if (!h || n < 1 || !A || lda != n || (ldv && ldv != n) || (ldo && ldo != n)) return n < 1 ? SKEW_BAD_ARG
                                                                                             : SKEW_UNSUPPORTED;
   if (n > kSingleMax) return SKEW_UNSUPPORTED;
@@ -758,7 +768,7 @@ static int single_func(skew_handle_t h, double* A, int64_t n, int64_t lda, doubl
     EigenBatch E;
     s = eigen_run(P, (const double* const*)arr, arr + 1, arr + 2, arr + 3, &E);
   } else {
-    s = func_run(P, (const double* const*)arr, arr + 4, (const double* const*)(arr + 5), mode, nullptr);
+    s = func_run(P, (const double* const*)arr, arr + 4, (const double* const*)(arr + 5), mode, func, nullptr);
   }
   if (s) return s;
   if (info) {
@@ -799,6 +809,10 @@ int skew_eigen_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* val
 int skew_exp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, int64_t lde, int* info) {
   if (!E) return SKEW_BAD_ARG;
   return single_func(h, A, n, lda, nullptr, nullptr, nullptr, 0, E, lde, nullptr, 0, info);
+}
+int skew_func_d(skew_handle_t h, double* A, int64_t n, int64_t lda, int func, double* F, int64_t ldf, int* info) {
+  if (!F || func < SKEW_FUNC_EXP || func > SKEW_FUNC_LOG) return SKEW_BAD_ARG;
+  return single_func(h, A, n, lda, nullptr, nullptr, nullptr, 0, F, ldf, nullptr, 0, info, func);
 }
 int skew_cis_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* C, int64_t ldc, int* info) {
   if (!C) return SKEW_BAD_ARG;
@@ -931,7 +945,7 @@ int skew_eigen_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* val
 }
 
 static int zfunc(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* C, double* O, int64_t ldo,
-                 int mode, int* info) {
+                 int mode, int func, int* info) {
   int st = zcheck(h, A, n, lda);
   if (st) return st;
   if (n > 0 && (!O || ldo < n || (mode == 1 && !C))) return SKEW_BAD_ARG;
@@ -943,22 +957,22 @@ static int zfunc(skew_handle_t h, double* A, int64_t n, int64_t lda, const doubl
   st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws);
   if (st) return st;
   CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, L.vals, L.V, n, L.ews, 1, h->stream));
-  CK(zfunc_from_eigen(mode, (int)n, L.vals, L.V, n, C, n, O, ldo, L.fws, 1, h->stream));
+  CK(zfunc_from_eigen(mode, func, (int)n, L.vals, L.V, n, C, n, O, ldo, L.fws, 1, info, h->stream));
   return SKEW_OK;
 }
 
 int skew_exp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, int64_t lde, int* info) {
-  return zfunc(h, A, n, lda, nullptr, E, lde, 0, info);
+  return zfunc(h, A, n, lda, nullptr, E, lde, 0, SKEW_FUNC_EXP, info);
 }
 
 int skew_exp_vjp_z(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* Cbar, double* G, int64_t ldg,
                    int* info) {
-  return zfunc(h, A, n, lda, Cbar, G, ldg, 1, info);
+  return zfunc(h, A, n, lda, Cbar, G, ldg, 1, SKEW_FUNC_EXP, info);
 }
 
 // Batched ComplexF64 of one size: count matrices n^2 apart (inputs read only).
 static int zbatch(skew_handle_t h, const double* A, int64_t n, int64_t count, double* vals_im, double* V,
-                  const double* C, double* O, int mode, int* status) {
+                  const double* C, double* O, int mode, int func, int* status) {
   if (!h || n < 0 || count < 0 || (count > 0 && n > 0 && !A)) return SKEW_BAD_ARG;
   if (n > 1024) return SKEW_UNSUPPORTED;
   if (count == 0 || n == 0) return SKEW_OK;
@@ -974,22 +988,33 @@ static int zbatch(skew_handle_t h, const double* A, int64_t n, int64_t count, do
   double* vv = mode < 0 ? vals_im : L.vals;
   double* VV = mode < 0 ? V : L.V;
   CK(zeigen_from_tridiag(L.W, n, (int)n, L.tau, L.ev, L.dvim, vv, VV, n, L.ews, (int)count, h->stream));
-  if (mode >= 0) CK(zfunc_from_eigen(mode, (int)n, vv, VV, n, C, n, O, n, L.fws, (int)count, h->stream));
+  if (mode >= 0) CK(zfunc_from_eigen(mode, func, (int)n, vv, VV, n, C, n, O, n, L.fws, (int)count, status, h->stream));
   return SKEW_OK;
 }
 
 int skew_batch_eigen_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* vals_im, double* V,
                        int* status) {
-  return zbatch(h, A, n, count, vals_im, V, nullptr, nullptr, -1, status);
+  return zbatch(h, A, n, count, vals_im, V, nullptr, nullptr, -1, 0, status);
 }
 
 int skew_batch_exp_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* E, int* status) {
-  return zbatch(h, A, n, count, nullptr, nullptr, nullptr, E, 0, status);
+  return zbatch(h, A, n, count, nullptr, nullptr, nullptr, E, 0, SKEW_FUNC_EXP, status);
 }
 
 int skew_batch_exp_vjp_z(skew_handle_t h, const double* A, int64_t n, int64_t count, const double* Cbar, double* G,
                          int* status) {
-  return zbatch(h, A, n, count, nullptr, nullptr, Cbar, G, 1, status);
+  return zbatch(h, A, n, count, nullptr, nullptr, Cbar, G, 1, SKEW_FUNC_EXP, status);
+}
+
+int skew_func_z(skew_handle_t h, double* A, int64_t n, int64_t lda, int func, double* F, int64_t ldf, int* info) {
+  if (func < SKEW_FUNC_EXP || func > SKEW_FUNC_LOG) return SKEW_BAD_ARG;
+  return zfunc(h, A, n, lda, nullptr, F, ldf, 0, func, info);
+}
+
+int skew_batch_func_z(skew_handle_t h, const double* A, int64_t n, int64_t count, int func, double* F,
+                      int* status) {
+  if (func < SKEW_FUNC_EXP || func > SKEW_FUNC_LOG) return SKEW_BAD_ARG;
+  return zbatch(h, A, n, count, nullptr, nullptr, nullptr, F, 0, func, status);
 }
 
 // ---------------------------------------------------------------------------

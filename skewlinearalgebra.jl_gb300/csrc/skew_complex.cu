@@ -28,6 +28,7 @@
 
 #include "skew_common.cuh"
 #include "skew_complex.cuh"
+#include "skew_funcs.cuh"
 #include "skew_internal.h"
 
 namespace skew {
@@ -767,10 +768,10 @@ __global__ void __launch_bounds__(256) zgemm_kernel(int n, const zc* __restrict_
     }
 }
 
-// mode 0: P(:, k) = V(:, k) e^{i mu_k}   (exp: E = P V^H)
+// mode 0: P(:, k) = V(:, k) f(i mu_k)   (F = P V^H for the function `func`)
 // mode 1: M(j, k) <- conj(Phi(j, k)) M(j, k), Phi(j,k) = e^{i(mu_j+mu_k)/2} sinc((mu_j-mu_k)/2)
-__global__ void zscale_kernel(int mode, int n, const double* __restrict__ mu, const zc* __restrict__ V, int64_t ldv,
-                              zc* __restrict__ M, int64_t ldm) {
+__global__ void zscale_kernel(int mode, int func, int n, const double* __restrict__ mu, const zc* __restrict__ V,
+                              int64_t ldv, zc* __restrict__ M, int64_t ldm, int* __restrict__ status) {
   const size_t mb = blockIdx.z;  // problem mb: mu n, V ldv*n, M ldm*n apart
   mu += mb * n;
   V += mb * (size_t)ldv * n;
@@ -778,9 +779,11 @@ __global__ void zscale_kernel(int mode, int n, const double* __restrict__ mu, co
   const int k = blockIdx.y;
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
     if (mode == 0) {
-      double s, c;
-      sincos(mu[k], &s, &c);
-      M[j + (int64_t)k * ldm] = zmul(V[j + (int64_t)k * ldv], zc{c, s});
+      double fa, fb;
+      bool sing = false;
+      skew_scalar_func(func, mu[k], &fa, &fb, &sing);
+      if (sing && j == 0 && status) status[mb] = SKEW_SINGULAR;
+      M[j + (int64_t)k * ldm] = zmul(V[j + (int64_t)k * ldv], zc{fa, fb});
     } else {
       const double a = mu[j], bb = mu[k];
       const double d = 0.5 * (a - bb);
@@ -792,22 +795,52 @@ __global__ void zscale_kernel(int mode, int n, const double* __restrict__ mu, co
   }
 }
 
-cudaError_t zfunc_from_eigen(int mode, int n, const double* vals_im, const double* Vd, int64_t ldv, const double* Cd,
-                             int64_t ldc, double* Od, int64_t ldo, double* ws, int batch, cudaStream_t st) {
+// O <- (O + s O^H) / 2 in place (s = +1 Hermitian part, -1 skew-Hermitian part)
+__global__ void zsymmetrize_kernel(int n, zc* __restrict__ O, int64_t ldo, int s) {
+  O += (size_t)blockIdx.z * ldo * n;
+  const int64_t tot = (int64_t)n * n;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(q / n), i = (int)(q - (int64_t)j * n);
+    if (i < j) continue;
+    zc* pij = O + i + (int64_t)j * ldo;
+    if (i == j) {  // Hermitian: real diagonal; skew-Hermitian: imaginary diagonal
+      if (s > 0)
+        pij->im = 0.0;
+      else
+        pij->re = 0.0;
+      continue;
+    }
+    zc* pji = O + j + (int64_t)i * ldo;
+    const zc x = *pij, y = *pji;
+    const zc u = zc{0.5 * (x.re + s * y.re), 0.5 * (x.im - s * y.im)};  // (x + s conj(y)) / 2
+    *pij = u;
+    *pji = zc{s * u.re, neg(s * u.im)};  // s conj(u)
+  }
+}
+
+cudaError_t zfunc_from_eigen(int mode, int func, int n, const double* vals_im, const double* Vd, int64_t ldv,
+                             const double* Cd, int64_t ldc, double* Od, int64_t ldo, double* ws, int batch,
+                             int* status, cudaStream_t st) {
   const zc* V = reinterpret_cast<const zc*>(Vd);
   zc* O = reinterpret_cast<zc*>(Od);
   zc* T1 = reinterpret_cast<zc*>(ws);
   zc* T2 = T1 + (size_t)batch * n * n;
   const dim3 g((n + 31) / 32, (n + 31) / 32, batch);
   const dim3 gs((n + 255) / 256, n, batch);
-  if (mode == 0) {  // exp(A) = V diag(e^{i mu}) V^H
-    zscale_kernel<<<gs, 256, 0, st>>>(0, n, vals_im, V, ldv, T1, n);
+  if (mode == 0) {  // F = V diag(f(i mu)) V^H, then its (skew-)Hermitian part
+    zscale_kernel<<<gs, 256, 0, st>>>(0, func, n, vals_im, V, ldv, T1, n, status);
     zgemm_kernel<<<g, 256, 0, st>>>(n, T1, n, 0, V, ldv, 1, O, ldo);
+    const int sym = skew_func_symmetry(func);
+    if (sym != 0) {
+      const int64_t tot = (int64_t)n * n;
+      zsymmetrize_kernel<<<dim3((unsigned)std::min<int64_t>((tot + 255) / 256, 1024), 1, batch), 256, 0, st>>>(
+          n, O, ldo, sym);
+    }
   } else {  // G = V (conj(Phi) o (V^H C V)) V^H
     const zc* C = reinterpret_cast<const zc*>(Cd);
     zgemm_kernel<<<g, 256, 0, st>>>(n, V, ldv, 1, C, ldc, 0, T1, n);   // V^H C
     zgemm_kernel<<<g, 256, 0, st>>>(n, T1, n, 0, V, ldv, 0, T2, n);    // (V^H C) V
-    zscale_kernel<<<gs, 256, 0, st>>>(1, n, vals_im, V, ldv, T2, n);
+    zscale_kernel<<<gs, 256, 0, st>>>(1, 0, n, vals_im, V, ldv, T2, n, nullptr);
     zgemm_kernel<<<g, 256, 0, st>>>(n, V, ldv, 0, T2, n, 0, T1, n);    // V M
     zgemm_kernel<<<g, 256, 0, st>>>(n, T1, n, 0, V, ldv, 1, O, ldo);   // (V M) V^H
   }

@@ -33,6 +33,7 @@
 #include "skew_common.cuh"
 #include "skew_internal.h"
 #include "skew_twisted.cuh"
+#include "skew_funcs.cuh"
 
 namespace skew {
 
@@ -737,12 +738,14 @@ __global__ void func_elem_kernel(EigenBatch E, int mode) {
   const double* Qi = E.Vi[b];
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (int64_t)gridDim.x * blockDim.x) {
     const int j = (int)(k / n), r = (int)(k - (int64_t)j * n);
-    if (mode == 0) {
-      double sn, cs;
-      sincos(mu[j], &sn, &cs);
+    if (mode == 0) {  // P = Qr a + Qi b, R = Qi a - Qr b for f(i mu_j) = a + i b
+      double fa, fb;
+      bool sing = false;
+      skew_scalar_func(E.func, mu[j], &fa, &fb, &sing);
+      if (sing && r == 0) E.status[b] = SKEW_SINGULAR;
       const double qr = Qr[k], qi = Qi[k];
-      w[k] = fma(qr, cs, qi * sn);
-      w[nn + k] = fma(qi, cs, -(qr * sn));
+      w[k] = fma(qr, fa, qi * fb);
+      w[nn + k] = fma(qi, fa, -(qr * fb));
     } else if (mode == 1) {
       const double d = exp(neg(mu[j]));
       w[k] = Qr[k] * d;
@@ -758,6 +761,28 @@ __global__ void func_elem_kernel(EigenBatch E, int mode) {
       w[2 * nn + k] = fma(mr, pr, -(mi * pi));
       w[3 * nn + k] = fma(mr, pi, mi * pr);
     }
+  }
+}
+
+// F <- (F + s F^T) / 2 in place (s = +1 symmetric part, -1 skew part), grid (chunks, count)
+__global__ void symmetrize_kernel(const int32_t* __restrict__ nn_, const int* __restrict__ status,
+                                  double* const* F, int s) {
+  const int b = blockIdx.y;
+  if (status && status[b] == SKEW_NO_CONVERGENCE) return;
+  const int n = nn_[b];
+  double* A = F[b];
+  const int64_t tot = (int64_t)n * n;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < tot; q += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(q / n), i = (int)(q - (int64_t)j * n);
+    if (i < j) continue;
+    if (i == j) {
+      if (s < 0) A[q] = 0.0;
+      continue;
+    }
+    const double x = A[i + (int64_t)j * n], y = A[j + (int64_t)i * n];
+    const double u = 0.5 * (x + s * y);
+    A[i + (int64_t)j * n] = u;
+    A[j + (int64_t)i * n] = s * u;
   }
 }
 
@@ -827,9 +852,15 @@ cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st) {
   const double* const* Vi = E.Vi;
   const double* const* W = E.pwork;
   cudaError_t e;
-  if (mode == 0) {  // E = Qr P^T + Qi R^T
+  if (mode == 0) {  // F = Qr P^T + Qi R^T = Re(V f V^H), then its (skew-)symmetric part
     func_elem_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E, 0);
     e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 0, 1), 1.0, bop(Vi, 0, 0), bop(W, 1, 1), 1.0, E.out, 0, 0, 1, st);
+    if (e != cudaSuccess) return e;
+    const int sym = skew_func_symmetry(E.func);
+    if (sym != 0) {
+      symmetrize_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E.n, E.status, E.out, sym);
+      e = cudaGetLastError();
+    }
     return e;
   }
   if (mode == 1) {  // Re = Qr P^T + Qi R^T, Im = Qi P^T - Qr R^T, interleaved

@@ -125,11 +125,14 @@ size_t zeigen_ws_doubles(int n, int batch);
 cudaError_t zeigen_from_tridiag(const double* A, int64_t lda, int n, const double* tau, const double* ev,
                                 const double* dvim, double* vals_im, double* V, int64_t ldv, double* ws, int batch,
                                 cudaStream_t st);
-// exp (mode 0: O = V e^{i mu} V^H) or its adjoint (mode 1: O = V (conj(Phi) o (V^H C V)) V^H),
-// `batch` problems with operands ld*n apart
+// mode 0: O = V f(i mu) V^H for the matrix function `func` (skew_func_t), projected on
+// the Hermitian / skew-Hermitian part where the function's result has that symmetry;
+// mode 1: the adjoint of exp, O = V (conj(Phi) o (V^H C V)) V^H.  `batch` problems with
+// operands ld*n apart; status (count, or null) gets SKEW_SINGULAR where f has no value.
 size_t zfunc_ws_doubles(int n, int batch);
-cudaError_t zfunc_from_eigen(int mode, int n, const double* vals_im, const double* V, int64_t ldv, const double* C,
-                             int64_t ldc, double* O, int64_t ldo, double* ws, int batch, cudaStream_t st);
+cudaError_t zfunc_from_eigen(int mode, int func, int n, const double* vals_im, const double* V, int64_t ldv,
+                             const double* C, int64_t ldc, double* O, int64_t ldo, double* ws, int batch, int* status,
+                             cudaStream_t st);
 
 // Eigenvectors of one large skew matrix after the blocked reduction (skew_tdvec.cu):
 // vals (descending, from launch_tridiag_bisect) and its scratch bp (bound, pivmin);
@@ -168,6 +171,7 @@ struct EigenBatch {
   double* const* out;        // [count] exp (real) / cis (complex interleaved) / adjoint (real)
   const double* const* cot;  // [count] cotangents for the adjoint
   double* const* pwork;      // [count] work + off_w (pointer array for the tiled products)
+  int func;                  // skew_func_t of mode 0 (exp and the other matrix functions)
 };
 // doubles of per-matrix work the eigen kernels need (4 n^2, or more for the fallback of small n)
 size_t eigen_work_doubles(int n);

@@ -285,6 +285,40 @@ def exp_rrule(A):
     return E, pullback
 
 
+# matrix functions of exp.jl (skew_func_t)
+FUNCS = {"exp": 0, "cos": 1, "sin": 2, "cosh": 3, "sinh": 4, "tan": 5, "tanh": 6, "cot": 7, "coth": 8, "log": 9}
+
+
+def matrix_function(A, name: str):
+    """Base.<name>(A::SkewHermitian) for name in exp, cos, sin, cosh, sinh, tan, tanh,
+    cot, coth, log (exp.jl:3-283): real n x n for a real skew matrix, ComplexF64 for a
+    complex skew-Hermitian one.  Raises ValueError where the reference throws
+    (log / cot / coth of a matrix with a zero eigenvalue)."""
+    f = FUNCS[name]
+    h = handle().bind()
+    info = _info_tensor()
+    if np.iscomplexobj(A) or (isinstance(A, torch.Tensor) and A.is_complex()):
+        W = _skew_hermitian_complex(A)
+        n = W.shape[0]
+        F = torch.zeros((n, n), dtype=torch.complex128, device="cuda")
+        check(_lib.load().skew_func_z(h, _ptr(W), n, n, f, _ptr(F), n, _ptr(info)), name)
+        out = from_device_complex(F)
+    else:
+        S = _as_skew(A).copy()
+        n = S.n
+        F = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        check(_lib.load().skew_func_d(h, _ptr(S.data), n, n, f, _ptr(F), n, _ptr(info)), name)
+        out = from_device(F)
+    if int(info.item()) == _lib.SKEW_SINGULAR:
+        raise ValueError(f"{name} of a singular matrix doesn't exist")
+    return out
+
+
+def sincos(A):
+    """sincos(A::SkewHermitian) (exp.jl:206-245): (sin(A), cos(A))."""
+    return matrix_function(A, "sin"), matrix_function(A, "cos")
+
+
 # ---------------------------------------------------------------------------
 # ComplexF64 skew-Hermitian matrices
 # ---------------------------------------------------------------------------
@@ -511,6 +545,14 @@ class BatchPlan:
         status = torch.empty(self.count, dtype=torch.int32, device="cuda") if status is None else status
         self._h.bind()
         check(_lib.load().skew_batch_cis_d(self.plan, _ptr(A_ptrs), _ptr(out_ptrs), _ptr(status)), "skew_batch_cis_d")
+        return status
+
+    def func(self, A_ptrs, out_ptrs, name: str, status=None):
+        """A matrix function (FUNCS: exp, cos, sin, ...) of every matrix (skew_batch_func_d)."""
+        status = torch.empty(self.count, dtype=torch.int32, device="cuda") if status is None else status
+        self._h.bind()
+        check(_lib.load().skew_batch_func_d(self.plan, _ptr(A_ptrs), FUNCS[name], _ptr(out_ptrs), _ptr(status)),
+              "skew_batch_func_d")
         return status
 
     def exp_vjp(self, A_ptrs, cot_ptrs, out_ptrs, status=None):
