@@ -101,6 +101,18 @@ SKEW_API int skew_logabspf_grad_d(skew_handle_t h, double* A, int64_t n, int64_t
  * (skewtrieigvals!, skeweigen.jl:105-156).  A is destroyed. */
 SKEW_API int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info);
 
+/* LA.eigvals!(A::SkewHermitian{Float64}, irange)  eigen.jl:8-11, :57-64: vals_im[0 .. iu-il] =
+ * -lambda_{il..iu} for the ascending eigenvalues lambda of SymTridiagonal(0, ev), i.e. the
+ * imaginary parts in descending order from the il-th largest; 1 <= il <= iu <= n.  A destroyed. */
+SKEW_API int skew_eigvals_irange_d(skew_handle_t h, double* A, int64_t n, int64_t lda, int64_t il, int64_t iu,
+                                   double* vals_im, int* info);
+
+/* LA.eigvals!(A::SkewHermitian{Float64}, vl, vh)  eigen.jl:13-16, :66-73: the eigenvalues whose
+ * imaginary part lies in [vl, vh), descending, in vals_im (room for n); *count (device int)
+ * receives how many.  A destroyed. */
+SKEW_API int skew_eigvals_interval_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double vl, double vh,
+                                     double* vals_im, int* count, int* info);
+
 /* eigvals without any device allocation.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc (a host that owns all device memory
  * through its own pool, or a path where an allocation's synchronisation or
@@ -185,6 +197,12 @@ SKEW_API int skew_hessenberg_z(skew_handle_t h, double* A, int64_t n, int64_t ld
  * descending (the reference returns -eigvals(Hermitian(i A)), eigenvalues ascending).
  * A is destroyed. */
 SKEW_API int skew_eigvals_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info);
+
+/* LA.eigvals!(A::SkewHermitian{ComplexF64}, vl, vh)  eigen.jl:36-41: imaginary parts in [vl, vh),
+ * descending, *count (device int) of them (vals_im room for n).  A destroyed.  (The reference's
+ * complex irange method passes a negated range to LAPACK and fails; it has no counterpart.) */
+SKEW_API int skew_eigvals_interval_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double vl, double vh,
+                                     double* vals_im, int* count, int* info);
 
 /* LA.eigen!(A::SkewHermitian{ComplexF64})  eigen.jl:101-106: vals_im[n] (descending) and
  * the eigenvectors V (n x n ComplexF64, ldv).  Eigenvectors are defined up to a

@@ -271,6 +271,49 @@ int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* v
 }
 
 
+// Selected eigenvalues (eigvals(A, irange) / eigvals(A, vl, vh)): the reduction,
+// then multisection on the selected indices only.
+static int eigvals_select_d(skew_handle_t h, double* A, int64_t n, int64_t lda, int by_index, int64_t il, int64_t iu,
+                            double vl, double vh, double* vals_im, int* count, int* info) {
+  if (!h || n < 0 || (n > 0 && (!A || !vals_im || lda < n))) return SKEW_BAD_ARG;
+  if (by_index && (il < 1 || iu < il || iu > n)) return SKEW_BAD_ARG;
+  if (!by_index && !(vl < vh)) return SKEW_BAD_ARG;
+  if (n == 0) {
+    if (count) CK(cudaMemsetAsync(count, 0, sizeof(int), h->stream));
+    return SKEW_OK;
+  }
+  double* ev = nullptr;
+  double* bnd = nullptr;
+  if (n >= blocked_min_n()) {
+    double* extra = nullptr;
+    int st = blocked(h, A, n, lda, nullptr, nullptr, info, 2 * (size_t)n + 8, &extra);
+    if (st) return st;
+    ev = extra;
+    bnd = extra + 2 * n;
+  } else {
+    int st = ensure_ws(h, sizeof(double) * (size_t)(n + 8));
+    if (st) return st;
+    ev = (double*)h->ws;
+    bnd = ev + n;
+    st = single(h, A, n, lda, nullptr, 0, nullptr, nullptr, n > 1 ? ev : nullptr, nullptr, info, 0, 0);
+    if (st) return st;
+  }
+  CK(launch_tridiag_bounds(ev, (int)n, bnd, h->stream));
+  CK(launch_select(ev, nullptr, (int)n, bnd, 1, by_index, (int)il, (int)iu, vl, vh, vals_im, count, h->stream));
+  return SKEW_OK;
+}
+
+int skew_eigvals_irange_d(skew_handle_t h, double* A, int64_t n, int64_t lda, int64_t il, int64_t iu, double* vals_im,
+                          int* info) {
+  return eigvals_select_d(h, A, n, lda, 1, il, iu, 0.0, 0.0, vals_im, nullptr, info);
+}
+
+int skew_eigvals_interval_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double vl, double vh,
+                            double* vals_im, int* count, int* info) {
+  if (!count) return SKEW_BAD_ARG;
+  return eigvals_select_d(h, A, n, lda, 0, 0, 0, vl, vh, vals_im, count, info);
+}
+
 // ---------------------------------------------------------------------------
 // Batched plans
 // ---------------------------------------------------------------------------
@@ -1004,6 +1047,30 @@ int skew_batch_exp_z(skew_handle_t h, const double* A, int64_t n, int64_t count,
 int skew_batch_exp_vjp_z(skew_handle_t h, const double* A, int64_t n, int64_t count, const double* Cbar, double* G,
                          int* status) {
   return zbatch(h, A, n, count, nullptr, nullptr, Cbar, G, 1, SKEW_FUNC_EXP, status);
+}
+
+int skew_eigvals_interval_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double vl, double vh,
+                            double* vals_im, int* count, int* info) {
+  int st = zcheck(h, A, n, lda);
+  if (st) return st;
+  if (n > 0 && (!vals_im || !count)) return SKEW_BAD_ARG;
+  if (!(vl < vh)) return SKEW_BAD_ARG;
+  if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+  if (n == 0) return count ? (cudaMemsetAsync(count, 0, sizeof(int), h->stream) == cudaSuccess ? SKEW_OK
+                                                                                              : SKEW_CUDA_ERROR)
+                           : SKEW_OK;
+  ZLayout L;
+  st = zlayout(h, n, 1, false, false, false, &L);
+  if (st) return st;
+  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws);
+  if (st) return st;
+  double* dg = L.ews;
+  double* off = dg + ((n + 31) & ~(int64_t)31);
+  double* ph = off + ((n + 31) & ~(int64_t)31);
+  double* bnd = ph + 2 * ((n + 31) & ~(int64_t)31);
+  CK(zsymtri_prep(L.ev, L.dvim, (int)n, dg, off, ph, bnd, h->stream));
+  CK(launch_select(off, dg, (int)n, bnd, 0, 0, 0, 0, vl, vh, vals_im, count, h->stream));
+  return SKEW_OK;
 }
 
 int skew_func_z(skew_handle_t h, double* A, int64_t n, int64_t lda, int func, double* F, int64_t ldf, int* info) {

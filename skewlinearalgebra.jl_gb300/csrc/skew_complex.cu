@@ -468,6 +468,12 @@ __global__ void __launch_bounds__(1024) zprep_kernel(const double* __restrict__ 
   }
 }
 
+cudaError_t zsymtri_prep(const double* ev, const double* dvim, int n, double* dg, double* off, double* ph,
+                         double* bnd, cudaStream_t st) {
+  zprep_kernel<<<1, 1024, 0, st>>>(ev, dvim, n, dg, off, reinterpret_cast<zc*>(ph), bnd);
+  return cudaGetLastError();
+}
+
 // number of eigenvalues of S smaller than x (pivots of LDL^T(S - x I), pivmin guard)
 __device__ int zsturm(const double* dg, const double* off, int n, double x, double pivmin) {
   double q = dg[0] - x;

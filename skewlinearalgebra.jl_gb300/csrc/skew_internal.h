@@ -93,6 +93,16 @@ cudaError_t launch_batch_trieig(const TrieigParams& P, cudaStream_t st);
 // Eigenvalues of one skew tridiagonal by bisection on the equivalent zero-diagonal
 // symmetric tridiagonal; vals_im sorted descending.
 cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, double* scratch2, cudaStream_t st);
+// selected eigenvalues (by 1-based index range or by the interval [vl, vh) of the
+// imaginary parts), negated eigenvalues of the symmetric tridiagonal (dg or zero, e);
+// bnd: sym_bound ? {bound, pivmin} : {lo, pivmin, hi}; *count (device) = how many
+cudaError_t launch_select(const double* e, const double* dg, int n, const double* bnd, int sym_bound, int by_index,
+                          int il, int iu, double vl, double vh, double* out, int* count, cudaStream_t st);
+cudaError_t launch_tridiag_bounds(const double* ev, int n, double* bnd, cudaStream_t st);
+// complex: the real symmetric tridiagonal of i T (diagonal -dvim, off-diagonal |ev|) and
+// its bounds {lo, pivmin, hi} (plus the phases, unused here)
+cudaError_t zsymtri_prep(const double* ev, const double* dvim, int n, double* dg, double* off, double* ph,
+                         double* bnd, cudaStream_t st);
 
 // ComplexF64 Householder tridiagonalisation (skew_complex.cu).  Complex values are
 // interleaved (re, im).  Batched: W[b] (in place, ld n[b]), tau/ev/dvim at off[b];

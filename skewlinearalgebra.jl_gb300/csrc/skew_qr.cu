@@ -22,6 +22,7 @@
 
 #include "skew_common.cuh"
 #include "skew_internal.h"
+#include "skew_twisted.cuh"
 
 namespace skew {
 
@@ -311,6 +312,58 @@ cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, doub
   const long long threads = ((long long)std::max(h, 1) * p + 31) / 32 * 32;
   const int bs = 128;
   bisect_kernel_dev<<<(unsigned)((threads + bs - 1) / bs), bs, 0, st>>>(ev, n, scratch2, vals_im, p);
+  return cudaGetLastError();
+}
+
+// Selected eigenvalues of a symmetric tridiagonal (diagonal dg or zero, off-diagonal
+// e): the ascending eigenvalues lambda_{i0 .. i0+m-1} with
+//   irange (il, iu, 1-based):  i0 = il - 1, m = iu - il + 1;
+//   interval [-vh, -vl):       i0 = #lambda < -vh, m = #lambda < -vl - i0;
+// written negated (out[k] = -lambda_{i0+k}, i.e. descending), as the reference's
+// eigvals!(A, irange) / eigvals!(A, vl, vh) negate the eigenvalues of
+// SymTridiagonal(0, ev) (eigen.jl:57-73) or of Hermitian(iA) (eigen.jl:29-41).
+// bnd: sym_bound ? {bound, pivmin} (spectrum in [-bound, bound]) : {lo, pivmin, hi}.
+// *count = m.  Groups of p lanes, one eigenvalue each; groups beyond m idle.
+__global__ void select_kernel(const double* __restrict__ e, const double* __restrict__ dg, int n,
+                              const double* __restrict__ bnd, int sym_bound, int by_index, int il, int iu, double vl,
+                              double vh, double* __restrict__ out, int* __restrict__ count, int p) {
+  const double lo = sym_bound ? neg(bnd[0]) : bnd[0];
+  const double hi = sym_bound ? bnd[0] : bnd[2];
+  const double pivmin = bnd[1];
+  int i0, m;
+  if (by_index) {
+    i0 = il - 1;
+    m = iu - il + 1;
+  } else {
+    i0 = block_sturm(e, dg, 0, n, neg(vh), pivmin);
+    m = block_sturm(e, dg, 0, n, neg(vl), pivmin) - i0;
+  }
+  const int k = (blockIdx.x * blockDim.x + threadIdx.x) / p;
+  const int gl = (threadIdx.x & 31) % p;
+  if (blockIdx.x == 0 && threadIdx.x == 0 && count) *count = m;
+  const bool active = k < m;
+  double x = group_multisect(lo, hi, active ? i0 + k : 0, 2.220446049250313e-16 * fmax(fabs(lo), fabs(hi)), p,
+                             active, [&](double y) { return block_sturm(e, dg, 0, n, y, pivmin); });
+  if (n == 1) x = dg ? dg[0] : 0.0;  // the 1 x 1 eigenvalue itself (the reference returns A[1,1])
+  if (active && gl == 0) out[k] = neg(x);
+}
+
+cudaError_t launch_select(const double* e, const double* dg, int n, const double* bnd, int sym_bound, int by_index,
+                          int il, int iu, double vl, double vh, double* out, int* count, cudaStream_t st) {
+  if (n <= 0) return cudaSuccess;
+  int dev = 0, sms = 148;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int m = by_index ? std::max(iu - il + 1, 1) : n;  // eigenvalues to find (at most)
+  const int p = multisect_lanes(m, sms);
+  const long long threads = ((long long)m * p + 31) / 32 * 32;
+  select_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(e, dg, n, bnd, sym_bound, by_index, il, iu, vl, vh,
+                                                                   out, count, p);
+  return cudaGetLastError();
+}
+
+// Gershgorin bound and pivmin of SymTridiagonal(0, e) into bnd[0..1] (no eigenvalue search)
+cudaError_t launch_tridiag_bounds(const double* ev, int n, double* bnd, cudaStream_t st) {
+  bisect_prep_kernel<<<1, 256, 0, st>>>(ev, n, bnd);
   return cudaGetLastError();
 }
 

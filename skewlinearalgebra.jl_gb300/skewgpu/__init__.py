@@ -219,6 +219,40 @@ def eigvals(A) -> np.ndarray:
     return 1j * vals.cpu().numpy()
 
 
+def eigvals_irange(A, il: int, iu: int) -> np.ndarray:
+    """eigvals(A::SkewHermitian{Float64}, il:iu) (eigen.jl:8-11, :57-64): the
+    eigenvalues il..iu counted from the largest imaginary part, as 0 + i*vals."""
+    S = _as_skew(A).copy()
+    n = S.n
+    vals = torch.zeros(max(iu - il + 1, 1), dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_eigvals_irange_d(h, _ptr(S.data), n, n, il, iu, _ptr(vals), _ptr(info)), "eigvals_irange")
+    return 1j * vals.cpu().numpy()[: iu - il + 1]
+
+
+def eigvals_interval(A, vl: float, vh: float) -> np.ndarray:
+    """eigvals(A::SkewHermitian, vl, vh) (eigen.jl:13-16, :36-41, :66-73): the
+    eigenvalues with imaginary part in [vl, vh), descending; real or complex A."""
+    h = handle().bind()
+    info = _info_tensor()
+    count = _info_tensor()
+    if np.iscomplexobj(A):
+        W = _skew_hermitian_complex(A)
+        n = W.shape[0]
+        vals = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
+        check(_lib.load().skew_eigvals_interval_z(h, _ptr(W), n, n, float(vl), float(vh), _ptr(vals), _ptr(count),
+                                                  _ptr(info)), "eigvals_interval")
+    else:
+        S = _as_skew(A).copy()
+        n = S.n
+        vals = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
+        check(_lib.load().skew_eigvals_interval_d(h, _ptr(S.data), n, n, float(vl), float(vh), _ptr(vals),
+                                                  _ptr(count), _ptr(info)), "eigvals_interval")
+    m = int(count.item())
+    return 1j * vals.cpu().numpy()[:m]
+
+
 def _info_ok(info: torch.Tensor, where: str) -> int:
     st = int(info.item())
     if st == _lib.SKEW_NO_CONVERGENCE:
