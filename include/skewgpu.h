@@ -247,6 +247,28 @@ SKEW_API int skew_func_z(skew_handle_t h, double* A, int64_t n, int64_t lda, int
 SKEW_API int skew_batch_func_z(skew_handle_t h, const double* A, int64_t n, int64_t count, int func, double* F,
                                int* status);
 
+/* ---------------------------------------------------------------------------
+ * SkewHermTridiagonal inputs (tridiag.jl): ev[n-1] the subdiagonal on the device, no
+ * reduction (Q = I).
+ * ------------------------------------------------------------------------- */
+/* LA.eigvals!(::SkewHermTridiagonal{Float64})  tridiag.jl:446-450 (skewtrieigvals!): the
+ * reference's QR order for n <= 1024; larger n sorted descending (bisection).  ev unchanged. */
+SKEW_API int skew_tridiag_eigvals_d(skew_handle_t h, const double* ev, int64_t n, double* vals_im, int* info);
+/* LA.eigen!(::SkewHermTridiagonal{Float64})  tridiag.jl:506 (skewtrieigen_merged!): vals_im, Vr + i Vi
+ * (ldv == n for n <= 1024); larger n: bisection and twisted vectors, values descending. */
+SKEW_API int skew_tridiag_eigen_d(skew_handle_t h, const double* ev, int64_t n, double* vals_im, double* Vr,
+                                  double* Vi, int64_t ldv, int* info);
+/* exp.jl functions of a SkewHermTridiagonal{Float64} (n <= 1024): F = f(T), ldf == n. */
+SKEW_API int skew_tridiag_func_d(skew_handle_t h, const double* ev, int64_t n, int func, double* F, int64_t ldf,
+                                 int* info);
+/* LA.eigvals! / LA.eigen!(::SkewHermTridiagonal{ComplexF64})  tridiag.jl:462-468, :508-515: ev[n-1]
+ * ComplexF64 subdiagonal, dvim[n] the imaginary diagonal (or NULL); through to_symtridiagonal
+ * (:558-583): values descending, V = D Y (V may be NULL for eigvals). */
+SKEW_API int skew_tridiag_eigvals_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n,
+                                    double* vals_im, int* info);
+SKEW_API int skew_tridiag_eigen_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n,
+                                  double* vals_im, double* V, int64_t ldv, int* info);
+
 /* Diagnostics: measured FP64 DFMA throughput of the current device in TFLOP/s
  * (runs a short microbenchmark on the handle's stream and synchronizes). */
 SKEW_API int skew_measure_fp64_peak(skew_handle_t h, double* tflops);

@@ -656,12 +656,18 @@ static int eigen_ws(skew_batch_plan_t P) {
 }
 
 // Reduction, QR with logged rotations, vectors, back-transformation.
+// A != null: dense matrices (reduction, QR of skewtrieigen_divided!, vectors,
+// back-transformation).  ev_in != null instead: the subdiagonals of
+// SkewHermTridiagonal matrices (skewtrieigen_merged!, no reduction, Q = I).
 static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const* vals, double* const* Vr,
-                     double* const* Vi, EigenBatch* Eout) {
+                     double* const* Vi, EigenBatch* Eout, const double* const* ev_in = nullptr) {
   int s = eigen_ws(P);
   if (s) return s;
   cudaStream_t st = P->h->stream;
-  s = run_buckets(P, A, nullptr, nullptr, nullptr, nullptr, true, P->e_tau, P->e_p_refl);
+  if (ev_in)
+    CK(launch_copy_ev(ev_in, P->d_n, P->d_ev_off, (int)P->count, P->d_ev, st));
+  else
+    s = run_buckets(P, A, nullptr, nullptr, nullptr, nullptr, true, P->e_tau, P->e_p_refl);
   if (s) return s;
   EigenBatch E;
   E.count = (int32_t)P->count;
@@ -689,10 +695,11 @@ static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const*
   E.cot = nullptr;
   E.pwork = P->e_p_work;
   E.func = SKEW_FUNC_EXP;
+  E.merged = ev_in ? 1 : 0;
   const int grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
   CK(launch_eigen_chain(E, st));
   CK(launch_eigen_vectors(E, grid, st));
-  CK(launch_eigen_back(E, grid, P->nmax, st));
+  if (!ev_in) CK(launch_eigen_back(E, grid, P->nmax, st));
   *Eout = E;
   return SKEW_OK;
 }
@@ -1082,6 +1089,117 @@ int skew_batch_func_z(skew_handle_t h, const double* A, int64_t n, int64_t count
                       int* status) {
   if (func < SKEW_FUNC_EXP || func > SKEW_FUNC_LOG) return SKEW_BAD_ARG;
   return zbatch(h, A, n, count, nullptr, nullptr, nullptr, F, 0, func, status);
+}
+
+// ---------------------------------------------------------------------------
+// SkewHermTridiagonal entry points (tridiag.jl): no reduction, Q = I
+// ---------------------------------------------------------------------------
+int skew_tridiag_eigvals_d(skew_handle_t h, const double* ev, int64_t n, double* vals_im, int* info) {
+  if (!h || n < 0 || (n > 1 && !ev) || (n > 0 && !vals_im)) return SKEW_BAD_ARG;
+  if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+  if (n == 0) return SKEW_OK;
+  if (n > kSingleMax) {  // bisection, values sorted descending
+    int st = ensure_ws(h, sizeof(double) * 8);
+    if (st) return st;
+    CK(launch_tridiag_bisect(ev, (int)n, vals_im, (double*)h->ws, h->stream));
+    return SKEW_OK;
+  }
+  // skewtrieigvals! (tridiag.jl:446-450): the QR in the reference's order, batch of one
+  skew_batch_plan_t P = nullptr;
+  int st = single_plan(h, n, &P);
+  if (st) return st;
+  double** arr = P->e_p_scratch;
+  set8_kernel<<<1, 1, 0, h->stream>>>(arr, const_cast<double*>(ev), vals_im, nullptr, nullptr, nullptr, nullptr,
+                                      nullptr, nullptr);
+  CK(cudaGetLastError());
+  CK(launch_copy_ev((const double* const*)arr, P->d_n, P->d_ev_off, 1, P->d_ev, h->stream));
+  TrieigParams tp;
+  tp.ev_all = P->d_ev;
+  tp.ev_off = P->d_ev_off;
+  tp.n = P->d_n;
+  tp.order = P->d_order;
+  tp.count = 1;
+  tp.evwork = P->d_ev;
+  tp.vals = arr + 1;
+  tp.status = info;
+  tp.fallback = P->d_fallback;
+  tp.grid = 1;
+  CK(launch_batch_trieig(tp, h->stream));
+  return SKEW_OK;
+}
+
+int skew_tridiag_eigen_d(skew_handle_t h, const double* ev, int64_t n, double* vals_im, double* Vr, double* Vi,
+                         int64_t ldv, int* info) {
+  if (!h || n < 1 || (n > 1 && !ev) || !vals_im || !Vr || !Vi || ldv < n) return SKEW_BAD_ARG;
+  if (n > kSingleMax) {  // bisection + twisted vectors, Q = I (values sorted descending)
+    if (n > (1LL << 15)) return SKEW_UNSUPPORTED;
+    const size_t need = 8 + large_eigen_ws_doubles((int)n);
+    int st = ensure_ws(h, sizeof(double) * need);
+    if (st) return st;
+    double* bp = (double*)h->ws;
+    if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+    CK(launch_tridiag_bisect(ev, (int)n, vals_im, bp, h->stream));
+    CK(large_eigen_vectors(nullptr, 0, (int)n, nullptr, ev, vals_im, bp, Vr, Vi, ldv, bp + 8, h->stream));
+    return SKEW_OK;
+  }
+  if (ldv != n) return SKEW_UNSUPPORTED;
+  // skewtrieigen_merged! (tridiag.jl:506), batch of one
+  skew_batch_plan_t P = nullptr;
+  int st = single_plan(h, n, &P);
+  if (st) return st;
+  double** arr = P->e_p_scratch;  // [0] ev, [1] vals, [2] Vr, [3] Vi
+  set8_kernel<<<1, 1, 0, h->stream>>>(arr, const_cast<double*>(ev), vals_im, Vr, Vi, nullptr, nullptr, nullptr,
+                                      nullptr);
+  CK(cudaGetLastError());
+  EigenBatch E;
+  st = eigen_run(P, nullptr, arr + 1, arr + 2, arr + 3, &E, (const double* const*)arr);
+  if (st) return st;
+  if (info) {
+    copy_status_kernel<<<1, 1, 0, h->stream>>>(P->e_status, info);
+    CK(cudaGetLastError());
+  }
+  return SKEW_OK;
+}
+
+int skew_tridiag_func_d(skew_handle_t h, const double* ev, int64_t n, int func, double* F, int64_t ldf, int* info) {
+  if (!h || n < 1 || (n > 1 && !ev) || !F || ldf != n || func < SKEW_FUNC_EXP || func > SKEW_FUNC_LOG)
+    return SKEW_BAD_ARG;
+  if (n > kSingleMax) return SKEW_UNSUPPORTED;
+  skew_batch_plan_t P = nullptr;
+  int st = single_plan(h, n, &P);
+  if (st) return st;
+  double** arr = P->e_p_scratch;  // [0] ev, [4] out
+  set8_kernel<<<1, 1, 0, h->stream>>>(arr, const_cast<double*>(ev), nullptr, nullptr, nullptr, F, nullptr, nullptr,
+                                      nullptr);
+  CK(cudaGetLastError());
+  EigenBatch E;
+  st = eigen_run(P, nullptr, nullptr, nullptr, nullptr, &E, (const double* const*)arr);
+  if (st) return st;
+  E.out = arr + 4;
+  E.cot = nullptr;
+  E.func = func;
+  CK(launch_eigen_func(E, 0, h->stream));
+  if (info) {
+    copy_status_kernel<<<1, 1, 0, h->stream>>>(P->e_status, info);
+    CK(cudaGetLastError());
+  }
+  return SKEW_OK;
+}
+
+int skew_tridiag_eigen_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n, double* vals_im,
+                         double* V, int64_t ldv, int* info) {
+  if (!h || n < 1 || (n > 1 && !ev) || !vals_im || (V && ldv < n)) return SKEW_BAD_ARG;
+  if (n > (1LL << 15)) return SKEW_UNSUPPORTED;
+  int st = ensure_ws(h, sizeof(double) * (zeigen_ws_doubles((int)n, 1) + 64));
+  if (st) return st;
+  if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+  CK(zeigen_tridiag(ev, dvim, (int)n, vals_im, V, ldv, (double*)h->ws, h->stream));
+  return SKEW_OK;
+}
+
+int skew_tridiag_eigvals_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n, double* vals_im,
+                           int* info) {
+  return skew_tridiag_eigen_z(h, ev, dvim, n, vals_im, nullptr, 0, info);
 }
 
 // ---------------------------------------------------------------------------

@@ -468,6 +468,57 @@ __global__ void __launch_bounds__(1024) zprep_kernel(const double* __restrict__ 
   }
 }
 
+// SkewHermTridiagonal{ComplexF64} input (complex subdiagonal ev, imaginary diagonal
+// dvim or none): to_symtridiagonal (tridiag.jl:558-583) gives S = SymTridiagonal(-dvim,
+// |ev|) and the phases d_1 = 1, d_{k+1} = d_k (i ev_k) / |ev_k|; bnd = {lo, pivmin, hi}.
+__global__ void __launch_bounds__(1024) zprep_tri_kernel(const zc* __restrict__ ev, const double* __restrict__ dvim,
+                                                        int n, double* __restrict__ dg, double* __restrict__ off,
+                                                        zc* __restrict__ ph, double* __restrict__ bp) {
+  __shared__ double red[3][32];
+  double lo = INFINITY, hi = -INFINITY, e2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double d = dvim ? neg(dvim[i]) : 0.0;
+    const double l = (i > 0) ? hypot(ev[i - 1].re, ev[i - 1].im) : 0.0;
+    const double r = (i + 1 < n) ? hypot(ev[i].re, ev[i].im) : 0.0;
+    dg[i] = d;
+    if (i + 1 < n) {
+      off[i] = r;
+      e2 = fmax(e2, r * r);
+    }
+    lo = fmin(lo, d - l - r);
+    hi = fmax(hi, d + l + r);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    lo = fmin(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+    hi = fmax(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+    e2 = fmax(e2, __shfl_xor_sync(0xffffffffu, e2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = lo;
+    red[1][threadIdx.x >> 5] = hi;
+    red[2][threadIdx.x >> 5] = e2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++) {
+      lo = fmin(lo, red[0][w]);
+      hi = fmax(hi, red[1][w]);
+      e2 = fmax(e2, red[2][w]);
+    }
+    const double span = fmax(fabs(lo), fabs(hi));
+    bp[0] = lo - 1e-14 * span - 1e-300;
+    bp[1] = 2.2250738585072014e-308 * fmax(1.0, e2);
+    bp[2] = hi + 1e-14 * span + 1e-300;
+    zc d{1.0, 0.0};
+    ph[0] = d;
+    for (int k = 0; k + 1 < n; k++) {
+      const double a = hypot(ev[k].re, ev[k].im);
+      if (a > 0.0) d = zmul(d, zc{neg(ev[k].im) / a, ev[k].re / a});  // (i ev_k) / |ev_k|
+      ph[k + 1] = d;
+    }
+  }
+}
+
 cudaError_t zsymtri_prep(const double* ev, const double* dvim, int n, double* dg, double* off, double* ph,
                          double* bnd, cudaStream_t st) {
   zprep_kernel<<<1, 1024, 0, st>>>(ev, dvim, n, dg, off, reinterpret_cast<zc*>(ph), bnd);
@@ -854,5 +905,31 @@ cudaError_t zfunc_from_eigen(int mode, int func, int n, const double* vals_im, c
 }
 
 size_t zfunc_ws_doubles(int n, int batch) { return 4 * (size_t)batch * n * n + 32; }
+
+// eigen of a SkewHermTridiagonal{ComplexF64}: vals_im (descending) and, if V != null,
+// V = D Y (no reflectors); ws: zeigen_ws_doubles(n, 1)
+cudaError_t zeigen_tridiag(const double* evd, const double* dvim, int n, double* vals_im, double* Vd, int64_t ldv,
+                           double* ws, cudaStream_t st) {
+  double* dg = ws;
+  double* off = dg + seg(n);
+  double* mu = off + seg(n);
+  zc* ph = reinterpret_cast<zc*>(mu + seg(n));
+  double* bp = mu + seg(n) + seg(2 * (size_t)n);
+  double* Y = bp + seg(8);
+  const int npan = (n - 1 + ZWB - 1) / ZWB;
+  double* tws = Y + seg((size_t)n * n) + seg(2 * (size_t)std::max(npan, 1) * ZWB * ZWB);
+  zprep_tri_kernel<<<1, 1024, 0, st>>>(reinterpret_cast<const zc*>(evd), dvim, n, dg, off, ph, bp);
+  int dev = 0, sms = 148;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int p = multisect_lanes(n, sms);
+  const long long threads = ((long long)n * p + 31) / 32 * 32;
+  zbisect_kernel<<<(unsigned)((threads + 127) / 128), 128, 0, st>>>(dg, off, n, 1, bp, mu, vals_im, p);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess || !Vd) return e;
+  e = symtri_vectors(dg, off, n, mu, bp, Y, tws, 1, st);
+  if (e != cudaSuccess) return e;
+  zassemble_kernel<<<dim3((n + 255) / 256, n, 1), 256, 0, st>>>(Y, ph, n, reinterpret_cast<zc*>(Vd), ldv);
+  return cudaGetLastError();
+}
 
 }  // namespace skew

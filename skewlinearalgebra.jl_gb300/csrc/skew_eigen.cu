@@ -171,7 +171,7 @@ __global__ void eigen_chain_kernel(EigenBatch E) {
         vals[n - 1] = neg(ev[n - 2]);
         n -= 2;
       }
-      if (n > 2 && fabs(ev[n - 2] - mem) < tol) {  // skeweigen.jl:355-358
+      if (!E.merged && n > 2 && fabs(ev[n - 2] - mem) < tol) {  // skeweigen.jl:355-358 (divided only)
         vals[n - 2] = ev[n - 2];
         vals[n - 1] = neg(ev[n - 2]);
         n -= 2;
@@ -211,31 +211,37 @@ __global__ void eigen_chain_kernel(EigenBatch E) {
 // ---------------------------------------------------------------------------
 
 // The stagnation fallback (skewtrieigen_backup!, skeweigen.jl:470-489) for one
-// matrix, by the CTA: the eigenpairs of SymTridiagonal(0, e) (the reference calls
-// LAPACK) by bisection (one positive eigenvalue per thread), twisted-factorisation
-// vectors (one per thread, skew_twisted.cuh) and one banded symmetric correction
-// of the even-row and odd-row parts, written in the fallback's layout: values
-// descending (vals = -eigvals(H)); column j of the eigenvalue -lambda_j is real on
-// odd (1-based) rows and imaginary on even rows, sign flipped every pair; the
-// vector of -sigma is the conjugate of that of sigma.  work: fallback_ws_doubles(N).
+// matrix, by the CTA: all N eigenpairs (lambda_j ascending, w_j) of
+// SymTridiagonal(0, e) (the reference calls LAPACK there), written as the
+// fallback does: vals_j = -lambda_j (descending) and column j real on odd (1-based)
+// rows and imaginary on even rows, sign flipped every pair.
+//   - eigenvalues by bisection to relative precision (the zero-diagonal Sturm
+//     count resolves tiny singular values of the bidiagonal coupling);
+//   - one twisted-factorisation vector per eigenvalue (skew_twisted.cuh), each
+//     copy of a repeated eigenvalue confined to its own block where the
+//     tridiagonal splits (several odd blocks give several zero eigenvalues);
+//   - three passes of the banded symmetric correction over whole vectors, which
+//     settle clusters of nearly equal eigenvalues.
+// work: fallback_ws_doubles(N).
 constexpr int FB_LW = 16;
 
-__host__ __device__ inline int fallback_kp(int N) { return ((N / 2 + (N & 1)) + 31) / 32 * 32; }
+__host__ __device__ inline int fallback_kp(int N) { return (N + 31) / 32 * 32; }
 __host__ __device__ inline int64_t fallback_ws_doubles(int N) {
   const int64_t KP = fallback_kp(N);
-  return 3 * (int64_t)N * KP + KP + 2 * KP * (FB_LW + 1) + 64;
+  return 3 * (int64_t)N * KP + 2 * KP + KP * (FB_LW + 1) + 64;
 }
 
 __device__ void cta_fallback(const double* __restrict__ e, int N, double* __restrict__ vals, double* __restrict__ Vr,
                              double* __restrict__ Vi, int64_t ldv, double* __restrict__ work) {
   __shared__ double red[2][ENW];
   const int tid = threadIdx.x;
-  const int h = N / 2, K = h + (N & 1), KP = fallback_kp(N);
+  const int KP = fallback_kp(N);
   double* dp = work;
   double* dm = dp + (int64_t)N * KP;
   double* z = dm + (int64_t)N * KP;
   double* nrm2 = z + (int64_t)N * KP;
-  double* band = nrm2 + KP;  // [k][d][U, V]
+  double* lam = nrm2 + KP;   // ascending eigenvalues
+  double* band = lam + KP;   // [k][d]
   // Gershgorin bound and pivmin
   double bound = 0.0, e2 = 0.0;
   for (int i = tid; i < N; i += ENT) {
@@ -261,77 +267,66 @@ __device__ void cta_fallback(const double* __restrict__ e, int N, double* __rest
   __syncthreads();
   const double pivmin = 2.2250738585072014e-308 * fmax(1.0, e2);
   bound = bound * (1.0 + 1e-14) + 1e-300;
-  // positive eigenvalues, descending: the k-th largest of SymTridiagonal(0, e)
+  // all eigenvalues, ascending, to relative precision (the spectrum is symmetric:
+  // the k-th smallest for k < N/2 is minus the k-th largest)
+  const int h = N / 2;
   for (int k = tid; k < h; k += ENT) {
-    double lo = 0.0, hi = bound;
-    for (int it = 0; it < 200 && hi - lo > fmax(2.220446049250313e-16 * hi, 2.220446049250313e-16 * bound); it++) {
+    double lo = 0.0, hi = bound;  // the k-th largest, positive
+    for (int it = 0; it < 1100 && hi - lo > fmax(2.220446049250313e-16 * hi, 4.0 * pivmin); it++) {
       const double mid = 0.5 * (lo + hi);
-      double q = neg(mid);
-      if (fabs(q) <= pivmin) q = neg(pivmin);
-      int c = (q < 0.0);
-      for (int i = 1; i < N; i++) {
-        const double ei = e[i - 1];
-        q = neg(mid) - (ei * ei) / q;
-        if (fabs(q) <= pivmin) q = neg(pivmin);
-        c += (q < 0.0);
-      }
-      if (c <= N - 1 - k)
+      if (block_sturm(e, nullptr, 0, N, mid, pivmin) <= N - 1 - k)
         lo = mid;
       else
         hi = mid;
     }
     const double x = 0.5 * (lo + hi);
-    vals[k] = x;
-    vals[N - 1 - k] = neg(x);
+    lam[N - 1 - k] = x;
+    lam[k] = neg(x);
   }
-  if ((N & 1) && tid == 0) vals[h] = 0.0;
+  if ((N & 1) && tid == 0) lam[h] = 0.0;
   __syncthreads();
-  // one twisted vector per thread (whole warps: KP and ENT are multiples of 32)
+  // one twisted vector per eigenvalue (whole warps: KP and ENT are multiples of 32)
   for (int kb = 0; kb < KP; kb += ENT) {
     if (kb + (tid & ~31) >= KP) continue;
     const int k = kb + tid;
-    const double sig = (k < h) ? vals[k] : 0.0;
-    nrm2[k] = twisted_vector(e, nullptr, N, sig, pivmin, KP, k, 0, N, dp, dm, z);
+    const double sig = lam[min(k, N - 1)];
+    int lo = 0, hi = N;
+    if (k < N) {
+      const double delta = fmax(16.0 * 2.220446049250313e-16 * fabs(sig), 4.0 * pivmin);
+      int j = 0;
+      for (int q = k - 1; q >= 0 && fabs(lam[q] - sig) <= delta; q--) j++;
+      tdvec_block(e, nullptr, N, sig, delta, j, pivmin, &lo, &hi);
+    }
+    nrm2[k] = twisted_vector(e, nullptr, N, sig, pivmin, KP, k, lo, hi, dp, dm, z);
   }
   __syncthreads();
-  // unit even-row and odd-row parts: X(i,k) = s_k z(i,k), s_k = sqrt(2)/|z_k| (sigma > 0)
-  // or 1/|z_k| (the zero-eigenvalue vector, even rows only)
-  double* X = dp;  // the pivots are no longer needed
+  // unit vectors X = z / |z|, then X <- X - 1/2 X E (E = X^T X - I over the band), three passes
+  double* X = dp;
   double* Y = z;
   for (int64_t q = tid; q < (int64_t)N * KP; q += ENT) {
-    const int i = (int)(q / KP), k = (int)(q - (int64_t)i * KP);
-    double x = 0.0;
-    if (k < K && !((i & 1) && k >= h)) x = ((k < h) ? 1.4142135623730951 : 1.0) * rsqrt(nrm2[k]) * z[q];
-    X[q] = x;
+    const int k = (int)(q % KP);
+    X[q] = (k < N) ? z[q] * rsqrt(nrm2[k]) : 0.0;
   }
   __syncthreads();
-  // symmetric corrections X <- X - 1/2 X E over a band of neighbours, E = X^T X - I
-  // per part; each pass squares the departure from orthogonality (three passes
-  // also settle clusters of nearly equal eigenvalues, whose twisted vectors mix)
   for (int pass = 0; pass < 3; pass++) {
-    for (int q = tid; q < K * (FB_LW + 1); q += ENT) {
+    for (int q = tid; q < N * (FB_LW + 1); q += ENT) {
       const int k = q / (FB_LW + 1), d = q - k * (FB_LW + 1), j = k + d;
-      double su = 0.0, sv = 0.0;
-      if (j < K) {
-        for (int i = 0; i < N; i += 2) su = fma(X[(int64_t)i * KP + k], X[(int64_t)i * KP + j], su);
-        for (int i = 1; i < N; i += 2) sv = fma(X[(int64_t)i * KP + k], X[(int64_t)i * KP + j], sv);
-      }
-      band[2 * q] = su - (d == 0 ? 1.0 : 0.0);
-      band[2 * q + 1] = (k >= h || j >= h) ? 0.0 : sv - (d == 0 ? 1.0 : 0.0);
+      double sum = 0.0;
+      if (j < N)
+        for (int i = 0; i < N; i++) sum = fma(X[(int64_t)i * KP + k], X[(int64_t)i * KP + j], sum);
+      band[q] = sum - (d == 0 ? 1.0 : 0.0);
     }
     __syncthreads();
     for (int64_t q = tid; q < (int64_t)N * KP; q += ENT) {
       const int i = (int)(q / KP), k = (int)(q - (int64_t)i * KP);
-      const int odd = i & 1;
       double acc = X[q];
-      if (k < K) {
+      if (k < N)
         for (int d = -FB_LW; d <= FB_LW; d++) {
           const int j = k + d;
-          if (j < 0 || j >= K) continue;
+          if (j < 0 || j >= N) continue;
           const int lo = min(k, j), off = abs(d);
-          acc = fma(-0.5 * band[2 * (lo * (FB_LW + 1) + off) + odd], X[(int64_t)i * KP + j], acc);
+          acc = fma(-0.5 * band[lo * (FB_LW + 1) + off], X[(int64_t)i * KP + j], acc);
         }
-      }
       Y[q] = acc;
     }
     __syncthreads();
@@ -339,20 +334,18 @@ __device__ void cta_fallback(const double* __restrict__ e, int N, double* __rest
     X = Y;
     Y = t;
   }
-  // fallback layout: column N-1-k (-sigma_k) and k (+sigma_k, the conjugate); zero vector: column h
-  for (int64_t q = tid; q < (int64_t)N * K; q += ENT) {
-    const int k = (int)(q / N), i = (int)(q - (int64_t)k * N);
-    const bool odd = (i & 1);
-    if (odd && k >= h) continue;
-    double o = (k < h) ? X[(int64_t)i * KP + k] * 0.7071067811865476 : X[(int64_t)i * KP + k];
+  // the fallback's layout: column j from w_j, vals_j = -lambda_j
+  for (int j = tid; j < N; j += ENT) vals[j] = neg(lam[j]);
+  for (int64_t q = tid; q < (int64_t)N * N; q += ENT) {
+    const int j = (int)(q / N), i = (int)(q - (int64_t)j * N);
+    double o = X[(int64_t)i * KP + j];
     if ((i >> 1) & 1) o = neg(o);
-    const int col = (k < h) ? N - 1 - k : h;
-    if (!odd) {
-      Vr[i + (int64_t)col * ldv] = o;
-      if (k < h) Vr[i + (int64_t)k * ldv] = o;
+    if ((i & 1) == 0 || ((N & 1) && i == N - 1)) {
+      Vr[i + (int64_t)j * ldv] = o;
+      Vi[i + (int64_t)j * ldv] = 0.0;
     } else {
-      Vi[i + (int64_t)col * ldv] = o;
-      Vi[i + (int64_t)k * ldv] = neg(o);
+      Vr[i + (int64_t)j * ldv] = 0.0;
+      Vi[i + (int64_t)j * ldv] = o;
     }
   }
   __syncthreads();
@@ -813,6 +806,21 @@ static cudaError_t bgemm(const EigenBatch& E, int nterms, BOperand A0, BOperand 
   P.c_step = c_step;
   const int nt = (E.nmax + BG_T - 1) / BG_T;
   bgemm_kernel<<<dim3(nt * nt, E.count), 256, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+__global__ void copy_ev_kernel(const double* const* ev_in, const int32_t* n, const int64_t* off, int count,
+                               double* ev) {
+  const int b = blockIdx.y;
+  if (b >= count) return;
+  const int m = n[b] - 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) ev[off[b] + i] = ev_in[b][i];
+}
+
+cudaError_t launch_copy_ev(const double* const* ev_in, const int32_t* n, const int64_t* off, int count, double* ev,
+                           cudaStream_t st) {
+  if (count <= 0) return cudaSuccess;
+  copy_ev_kernel<<<dim3(4, count), 256, 0, st>>>(ev_in, n, off, count, ev);
   return cudaGetLastError();
 }
 

@@ -103,6 +103,9 @@ cudaError_t launch_tridiag_bounds(const double* ev, int n, double* bnd, cudaStre
 // its bounds {lo, pivmin, hi} (plus the phases, unused here)
 cudaError_t zsymtri_prep(const double* ev, const double* dvim, int n, double* dg, double* off, double* ph,
                          double* bnd, cudaStream_t st);
+// eigen of a SkewHermTridiagonal{ComplexF64} (complex ev, dvim or null): vals_im, V = D Y
+cudaError_t zeigen_tridiag(const double* ev, const double* dvim, int n, double* vals_im, double* V, int64_t ldv,
+                           double* ws, cudaStream_t st);
 
 // ComplexF64 Householder tridiagonalisation (skew_complex.cu).  Complex values are
 // interleaved (re, im).  Batched: W[b] (in place, ld n[b]), tau/ev/dvim at off[b];
@@ -182,7 +185,11 @@ struct EigenBatch {
   const double* const* cot;  // [count] cotangents for the adjoint
   double* const* pwork;      // [count] work + off_w (pointer array for the tiled products)
   int func;                  // skew_func_t of mode 0 (exp and the other matrix functions)
+  int merged;                // 1: skewtrieigen_merged! (tridiagonal input; no mem deflation of :355)
 };
+// copies n[b] - 1 subdiagonal entries from ev_in[b] to ev + off[b] for every matrix
+cudaError_t launch_copy_ev(const double* const* ev_in, const int32_t* n, const int64_t* off, int count, double* ev,
+                           cudaStream_t st);
 // doubles of per-matrix work the eigen kernels need (4 n^2, or more for the fallback of small n)
 size_t eigen_work_doubles(int n);
 cudaError_t launch_eigen_chain(const EigenBatch& E, cudaStream_t st);

@@ -284,8 +284,10 @@ __global__ void bisect_prep_kernel(const double* __restrict__ e, int n, double* 
 }
 
 // The positive eigenvalues of SymTridiagonal(0, e): the k-th largest (k < n/2) by
-// a group of p lanes (multisection, absolute tolerance eps * bound); vals[k] and
-// vals[n-1-k] = -vals[k] written together; odd n: vals[n/2] = 0.
+// a group of p lanes (multisection to relative precision: the zero-diagonal Sturm
+// count resolves the tiny singular values of the bidiagonal coupling, and their
+// twisted eigenvectors need them accurate); vals[k] and vals[n-1-k] = -vals[k]
+// written together; odd n: vals[n/2] = 0.
 __global__ void bisect_kernel_dev(const double* __restrict__ e, int n, const double* __restrict__ bp,
                                   double* __restrict__ vals, int p) {
   const int h = n / 2;
@@ -294,8 +296,8 @@ __global__ void bisect_kernel_dev(const double* __restrict__ e, int n, const dou
   if ((n & 1) && gid == 0 && gl == 0 && blockIdx.x == 0) vals[h] = 0.0;
   const double bound = bp[0], pivmin = bp[1];
   const bool active = gid < h;
-  const double x = group_multisect(0.0, bound, n - 1 - (active ? gid : 0), 2.220446049250313e-16 * bound, p,
-                                   active, [&](double y) { return sturm_count(e, n, y, pivmin); });
+  const double x = group_multisect(0.0, bound, n - 1 - (active ? gid : 0), 4.0 * pivmin, p, active,
+                                   [&](double y) { return sturm_count(e, n, y, pivmin); });
   if (active && gl == 0) {
     vals[gid] = x;
     vals[n - 1 - gid] = neg(x);

@@ -610,27 +610,29 @@ cudaError_t large_eigen_vectors(const double* A, int64_t lda, int n, const doubl
   tdvec_write_skew_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC), LA_NT, 0, st>>>(L, X, Vr, Vi, ldv);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  wy_factor_kernel<<<L.npan, WT_NT, 0, st>>>(A, lda, tau, L);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  StripParams P;
-  P.A = A;
-  P.lda = lda;
-  P.tau = tau;
-  P.L = L;
-  P.Xr = Vr;
-  P.Xi = Vi;
-  P.ldv = ldv;
-  P.cr0 = L.h;                // -sigma columns and the zero vector
-  P.ci0 = L.h + (n & 1);      // -sigma columns
-  P.nstr_r = (n - P.cr0 + SW - 1) / SW;
-  const int nstr_i = (n - P.ci0 + SW - 1) / SW;
-  static std::atomic<uint64_t> raised{0};
-  e = raise_smem_limit_once((const void*)back_strip_kernel, raised);
-  if (e != cudaSuccess) return e;
-  back_strip_kernel<<<P.nstr_r + nstr_i, BT_NT, strip_smem_bytes(), st>>>(P);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
+  if (A) {  // A == null: a tridiagonal input, Q = I
+    wy_factor_kernel<<<L.npan, WT_NT, 0, st>>>(A, lda, tau, L);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    StripParams P;
+    P.A = A;
+    P.lda = lda;
+    P.tau = tau;
+    P.L = L;
+    P.Xr = Vr;
+    P.Xi = Vi;
+    P.ldv = ldv;
+    P.cr0 = L.h;                // -sigma columns and the zero vector
+    P.ci0 = L.h + (n & 1);      // -sigma columns
+    P.nstr_r = (n - P.cr0 + SW - 1) / SW;
+    const int nstr_i = (n - P.ci0 + SW - 1) / SW;
+    static std::atomic<uint64_t> raised{0};
+    e = raise_smem_limit_once((const void*)back_strip_kernel, raised);
+    if (e != cudaSuccess) return e;
+    back_strip_kernel<<<P.nstr_r + nstr_i, BT_NT, strip_smem_bytes(), st>>>(P);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
   mirror_kernel<<<dim3((n + 255) / 256, L.h + (n & 1)), 256, 0, st>>>(Vr, Vi, ldv, n);
   return cudaGetLastError();
 }

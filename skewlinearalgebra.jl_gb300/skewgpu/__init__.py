@@ -353,6 +353,60 @@ def sincos(A):
     return matrix_function(A, "sin"), matrix_function(A, "cos")
 
 
+class SkewHermTridiagonal:
+    """SkewHermTridiagonal(ev) / SkewHermTridiagonal(ev, dvim) (tridiag.jl): the
+    subdiagonal ev (real, or complex with the imaginary diagonal dvim) on the device."""
+
+    def __init__(self, ev, dvim=None):
+        ev = np.asarray(ev)
+        self.complex = np.iscomplexobj(ev) or dvim is not None
+        self.n = len(ev) + 1
+        dt = torch.complex128 if self.complex else torch.float64
+        self.ev = torch.from_numpy(np.ascontiguousarray(ev.astype(np.complex128 if self.complex else np.float64))).to(
+            "cuda") if len(ev) else torch.zeros(1, dtype=dt, device="cuda")
+        self.dvim = None if dvim is None else torch.from_numpy(np.asarray(dvim, dtype=np.float64)).cuda()
+
+    def eigvals(self) -> np.ndarray:
+        n = self.n
+        vals = torch.zeros(n, dtype=torch.float64, device="cuda")
+        info = _info_tensor()
+        h = handle().bind()
+        if self.complex:
+            check(_lib.load().skew_tridiag_eigvals_z(h, _ptr(self.ev), _ptr(self.dvim), n, _ptr(vals), _ptr(info)),
+                  "tridiag eigvals")
+        else:
+            check(_lib.load().skew_tridiag_eigvals_d(h, _ptr(self.ev), n, _ptr(vals), _ptr(info)), "tridiag eigvals")
+        _info_ok(info, "tridiag eigvals")
+        return 1j * vals.cpu().numpy()
+
+    def eigen(self):
+        n = self.n
+        vals = torch.zeros(n, dtype=torch.float64, device="cuda")
+        info = _info_tensor()
+        h = handle().bind()
+        if self.complex:
+            V = torch.zeros((n, n), dtype=torch.complex128, device="cuda")
+            check(_lib.load().skew_tridiag_eigen_z(h, _ptr(self.ev), _ptr(self.dvim), n, _ptr(vals), _ptr(V), n,
+                                                   _ptr(info)), "tridiag eigen")
+            return 1j * vals.cpu().numpy(), from_device_complex(V)
+        Vr = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        Vi = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        check(_lib.load().skew_tridiag_eigen_d(h, _ptr(self.ev), n, _ptr(vals), _ptr(Vr), _ptr(Vi), n, _ptr(info)),
+              "tridiag eigen")
+        _info_ok(info, "tridiag eigen")
+        return 1j * vals.cpu().numpy(), from_device(Vr) + 1j * from_device(Vi)
+
+    def function(self, name: str) -> np.ndarray:
+        n = self.n
+        F = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        info = _info_tensor()
+        h = handle().bind()
+        check(_lib.load().skew_tridiag_func_d(h, _ptr(self.ev), n, FUNCS[name], _ptr(F), n, _ptr(info)), name)
+        if int(info.item()) == _lib.SKEW_SINGULAR:
+            raise ValueError(f"{name} of a singular matrix doesn't exist")
+        return from_device(F)
+
+
 # ---------------------------------------------------------------------------
 # ComplexF64 skew-Hermitian matrices
 # ---------------------------------------------------------------------------

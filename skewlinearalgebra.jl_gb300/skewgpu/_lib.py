@@ -59,6 +59,11 @@ SIGNATURES = {
     "skew_batch_exp_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp]),
     "skew_batch_exp_vjp_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp]),
     "skew_func_d": (_int, [_vp, _vp, _i64, _i64, _int, _vp, _i64, _vp]),
+    "skew_tridiag_eigvals_d": (_int, [_vp, _vp, _i64, _vp, _vp]),
+    "skew_tridiag_eigen_d": (_int, [_vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp]),
+    "skew_tridiag_func_d": (_int, [_vp, _vp, _i64, _int, _vp, _i64, _vp]),
+    "skew_tridiag_eigvals_z": (_int, [_vp, _vp, _vp, _i64, _vp, _vp]),
+    "skew_tridiag_eigen_z": (_int, [_vp, _vp, _vp, _i64, _vp, _vp, _i64, _vp]),
     "skew_eigvals_irange_d": (_int, [_vp, _vp, _i64, _i64, _i64, _i64, _vp, _vp]),
     "skew_eigvals_interval_d": (_int, [_vp, _vp, _i64, _i64, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp]),
     "skew_eigvals_interval_z": (_int, [_vp, _vp, _i64, _i64, ctypes.c_double, ctypes.c_double, _vp, _vp, _vp]),
