@@ -193,7 +193,8 @@ def main():
                 "pfaffian_adjoint_1024x128": lambda: leg_pfaffian_adjoint(peak, max(1, args.steps)),
                 "exp_adjoint_512_mixed": lambda: leg_exp_adjoint(peak, max(1, min(args.steps, 3))),
                 "exp_adjoint_complex_64x256": lambda: leg_complex_exp_adjoint(peak),
-                "complex_n4096": lambda: leg_complex_large(4096, peak)}
+                "complex_n4096": lambda: leg_complex_large(4096, peak),
+                "complex_pfaffian_2048x128": lambda: leg_complex_pfaffian(peak, cpu=not args.no_cpu)}
         out = {k: f() for k, f in legs.items() if args.leg is None or k == args.leg}
         plan.close()
         print(json.dumps({"legs": out}), flush=True)
@@ -378,6 +379,7 @@ def main():
         legs["exp_adjoint_512_mixed"] = leg_exp_adjoint(fp64_peak, max(1, min(args.steps, 3)))
         legs["exp_adjoint_complex_64x256"] = leg_complex_exp_adjoint(fp64_peak)
         legs["complex_n4096"] = leg_complex_large(4096, fp64_peak)
+        legs["complex_pfaffian_2048x128"] = leg_complex_pfaffian(fp64_peak, cpu=not args.no_cpu)
 
     if rank == 0:
         line = {
@@ -617,6 +619,111 @@ def leg_complex_exp_adjoint(fp64_peak, count=64, n=256, steps=3):
     return {"value": count / sec, "unit": "matrices/s", "ms_per_step": sec * 1e3, "count": count, "n": n,
             "steps": steps, "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
             "status_ok": int((st.cpu().numpy() == 0).sum())}
+
+
+def pfz_flops(n):
+    """Real flops of the complex Parlett-Reid elimination on the lower triangle:
+    8 complex-multiply-adds (16 real flops) per trailing entry and step."""
+    return float(sum(16 * (n - k - 2) * (n - k - 3) // 2 for k in range(0, n - 1, 2)))
+
+
+def leg_complex_pfaffian(fp64_peak, count=2048, n=128, large_n=4096, steps=3, cpu=True):
+    """Complex skew-symmetric Pfaffian (Parlett-Reid, pfaffian.jl:98-137, :193-233):
+    a batch of `count` matrices n x n (C iid complex N(0, 1/n), A = (C - C^T)/2) in one
+    skew_batch_logabspf_z call, inputs resident in HBM (count*n^2*16 B > L2); the same
+    through host buffers (e2e); one n = large_n matrix on the cooperative grid; the
+    oracle's FP64 restatement on a sample of the batch, one thread."""
+    import ctypes
+    import time
+
+    import torch
+
+    import skewgpu
+
+    rng = np.random.default_rng(SEED + 77)
+    host = np.empty((count, n, n), dtype=np.complex128)
+    for b in range(count):
+        C = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n)
+        host[b] = ((C - C.T) / 2).T  # row-major storage of A^T = column-major A
+    dA = torch.from_numpy(host).cuda()
+    lp = torch.zeros(count, dtype=torch.float64, device="cuda")
+    ph = torch.zeros(count, dtype=torch.complex128, device="cuda")
+    st = torch.zeros(count, dtype=torch.int32, device="cuda")
+    L = skewgpu._lib.load()
+    h = skewgpu.handle().bind()
+    stream = torch.cuda.current_stream()
+    P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+    def run():
+        assert L.skew_batch_logabspf_z(h, P(dA), n, count, P(lp), P(ph), None, 1, P(st)) == 0
+
+    for _ in range(3):
+        run()
+    torch.cuda.synchronize()
+    sec = _time_events(run, steps, stream)
+    flops = count * pfz_flops(n)
+    out = {"value": count / sec, "unit": "matrices/s", "ms_per_step": sec * 1e3, "count": count, "n": n,
+           "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
+           "algorithmic_flops_per_step": flops, "status_ok": int((st.cpu().numpy() == 0).sum())}
+    # e2e: pinned host input -> device, the call, log|Pf| and cis(phase) back to the host
+    pin = torch.from_numpy(host).pin_memory()
+    out_lp = torch.zeros(count, dtype=torch.float64).pin_memory()
+    out_ph = torch.zeros(count, dtype=torch.complex128).pin_memory()
+
+    def e2e():
+        dA.copy_(pin, non_blocking=True)
+        run()
+        out_lp.copy_(lp, non_blocking=True)
+        out_ph.copy_(ph, non_blocking=True)
+
+    e2e()
+    torch.cuda.synchronize()
+    sec_e = _time_events(e2e, steps, stream)
+    out["e2e"] = {"value": count / sec_e, "unit": "matrices/s", "h2d_bytes_per_step": int(host.nbytes),
+                  "d2h_bytes_per_step": int(count * 24)}
+    # parity of a sample against the oracle (FP64 restatement)
+    if cpu:
+        from oracle import oracle as O
+
+        k = 48
+        mats = [host[b].T for b in range(k)]
+        t0 = time.perf_counter()
+        refs = [O.pfaffian_complex(M) for M in mats]
+        cpu_sec = time.perf_counter() - t0
+        glp = lp[:k].cpu().numpy()
+        gph = ph[:k].cpu().numpy()
+        out["check"] = {"matrices": k,
+                        "max_rel_logpf_vs_oracle": float(max(abs(glp[b] - refs[b][0]) / max(1.0, abs(refs[b][0]))
+                                                             for b in range(k))),
+                        "max_phase_diff_vs_oracle": float(max(abs(gph[b] - refs[b][1]) for b in range(k)))}
+        out["cpu_baseline"] = {"value": k / cpu_sec, "unit": "matrices/s", "cores": 1, "kind": "port",
+                               "sample": f"{k} of the {count} matrices, oracle FP64 restatement (full-matrix "
+                                         "update as the reference), one thread"}
+    # one large matrix on the cooperative grid (in place on a fresh copy per repetition)
+    if large_n:
+        C = (rng.standard_normal((large_n, large_n)) + 1j * rng.standard_normal((large_n, large_n))) / np.sqrt(large_n)
+        src = skewgpu.to_device_complex((C - C.T) / 2)
+        W = torch.empty_like(src)
+        o = torch.zeros(3, dtype=torch.float64, device="cuda")
+        info = torch.zeros(1, dtype=torch.int32, device="cuda")
+        times = []
+        for r in range(3):
+            W.copy_(src)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            assert L.skew_logabspf_z(h, P(W), large_n, large_n, P(o), ctypes.c_void_p(o.data_ptr() + 8), 0,
+                                     P(info)) == 0
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if r:
+                times.append(e0.elapsed_time(e1) / 1e3)
+        sec_l = float(np.median(times))
+        fl = pfz_flops(large_n)
+        sign, logdet = np.linalg.slogdet(skewgpu.from_device_complex(src)) if large_n <= 4096 else (None, None)
+        out[f"single_n{large_n}"] = {"ms": sec_l * 1e3, "gflops": fl / sec_l / 1e9, "frac_fp64": fl / sec_l / 1e12 / fp64_peak,
+                                     "info": int(info.item()),
+                                     "logpf_minus_half_logdet": None if logdet is None else float(o[0].item() - logdet / 2)}
+    return out
 
 
 def _time_events(fn, reps, stream):

@@ -248,6 +248,27 @@ SKEW_API int skew_batch_func_z(skew_handle_t h, const double* A, int64_t n, int6
                                int* status);
 
 /* ---------------------------------------------------------------------------
+ * Complex skew-symmetric matrices (A == -transpose(A), ComplexF64): the Pfaffian by
+ * Parlett-Reid elimination with pivoting (pfaffian.jl:98-137 and :193-233).
+ * check != 0 verifies A == -transpose(A) exactly first (pfaffian.jl:162, :261; isskewsymmetric,
+ * skewhermitian.jl:101-110)
+ * -> info / status = SKEW_NOT_SKEW and NaN outputs.  A zero Pfaffian (odd n, or a zero
+ * pivot column) gives log|Pf| = -Inf, phase 0, Pf 0 and info = SKEW_SINGULAR.
+ * ------------------------------------------------------------------------- */
+/* logabspfaffian!(A::AbstractMatrix{ComplexF64})  pfaffian.jl:193-233, :259-263:
+ * logpf[0] = log|Pf(A)|, phase[0..1] = cis(phase) (re, im) with Pf(A) = cis(phase) exp(logpf).
+ * A (n x n, lda) is overwritten (its strictly lower triangle) for n above one CTA's size. */
+SKEW_API int skew_logabspf_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* phase,
+                             int check, int* info);
+/* pfaffian!(A::AbstractMatrix{ComplexF64})  pfaffian.jl:98-137, :160-164: pf[0..1] = Pf(A),
+ * the running product of the pivots (overflows where the reference's does). */
+SKEW_API int skew_pfaffian_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* pf, int check, int* info);
+/* Batches of one size (matrices back to back, leading dimension n, read only): logpf[count],
+ * phase[2 count], pf[2 count] (each nullable, not all), status[count] (nullable). */
+SKEW_API int skew_batch_logabspf_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* logpf,
+                                   double* phase, double* pf, int check, int* status);
+
+/* ---------------------------------------------------------------------------
  * SkewHermTridiagonal inputs (tridiag.jl): ev[n-1] the subdiagonal on the device, no
  * reduction (Q = I).
  * ------------------------------------------------------------------------- */

@@ -68,6 +68,8 @@ def lib():
         _lib.orc_exp_vjp_q.argtypes = [_D, _D, _I64, _D]
         _lib.orc_expm_dense_q.argtypes = [_D, _I64, _D]
         _lib.orc_symtri_eigvals_q.argtypes = [_D, _D, _I64, _D]
+        for name in ("orc_pfaffian_z", "orc_pfaffian_zq"):
+            getattr(_lib, name).argtypes = [_D, _I64, _D, _D, _D]
         _lib.orc_batch_logabspf_d.argtypes = [_D, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _I64, _D, _D,
                                               ctypes.c_int]
         _lib.orc_batch_logabspf_grad_d.argtypes = [_D, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _I64, _D, _D,
@@ -134,6 +136,21 @@ def logabspfaffian(A, quad: bool = False):
     fn = lib().orc_logabspf_q if quad else lib().orc_logabspf_d
     fn(_p(F), n, _p(lp), _p(sg))
     return float(lp[0]), float(sg[0])
+
+
+def pfaffian_complex(A, quad: bool = False):
+    """Parlett-Reid elimination with pivoting for complex skew-symmetric A
+    (pfaffian.jl:98-137 and :193-233).  Returns (log|Pf A|, cis(phase), Pf A):
+    the two outputs of _logabspfaffian! and the product of _pfaffian!."""
+    A = np.asarray(A, dtype=np.complex128)
+    n = A.shape[0]
+    buf = np.ascontiguousarray(A.ravel(order="F")).view(np.float64)
+    lp = np.zeros(1)
+    ph = np.zeros(2)
+    pf = np.zeros(2)
+    fn = lib().orc_pfaffian_zq if quad else lib().orc_pfaffian_z
+    fn(_p(buf), n, _p(lp), _p(ph), _p(pf))
+    return float(lp[0]), complex(ph[0], ph[1]), complex(pf[0], pf[1])
 
 
 def skewtrieigvals(ev, quad: bool = False):
@@ -317,3 +334,83 @@ def exact_pfaffian(A) -> Fraction:
 
 
 exact_pfaffian_gm = exact_pfaffian
+
+
+class GaussQ:
+    """Gaussian rational a + b i with Fraction parts: the field the reference's
+    Complex{Rational{BigInt}} exact Pfaffians are taken in (runtests.jl:410-416)."""
+
+    __slots__ = ("re", "im")
+
+    def __init__(self, re, im=0):
+        self.re = Fraction(re)
+        self.im = Fraction(im)
+
+    @staticmethod
+    def of(z) -> "GaussQ":
+        if isinstance(z, GaussQ):
+            return z
+        z = complex(z)
+        return GaussQ(Fraction(z.real), Fraction(z.imag))
+
+    def __add__(self, o):
+        o = GaussQ.of(o)
+        return GaussQ(self.re + o.re, self.im + o.im)
+
+    def __sub__(self, o):
+        o = GaussQ.of(o)
+        return GaussQ(self.re - o.re, self.im - o.im)
+
+    def __neg__(self):
+        return GaussQ(-self.re, -self.im)
+
+    def __mul__(self, o):
+        o = GaussQ.of(o)
+        return GaussQ(self.re * o.re - self.im * o.im, self.re * o.im + self.im * o.re)
+
+    def __truediv__(self, o):
+        o = GaussQ.of(o)
+        d = o.re * o.re + o.im * o.im
+        return GaussQ((self.re * o.re + self.im * o.im) / d, (self.im * o.re - self.re * o.im) / d)
+
+    def __eq__(self, o):
+        o = GaussQ.of(o)
+        return self.re == o.re and self.im == o.im
+
+    def __complex__(self):
+        return complex(float(self.re), float(self.im))
+
+
+def exact_pfaffian_complex(A) -> GaussQ:
+    """Exact Pfaffian of a complex skew-symmetric matrix whose entries are exact
+    binary fractions (integers, halves, ...), by the same Galbiati-Maffioli
+    elimination as exact_pfaffian, over the Gaussian rationals."""
+    n = len(A)
+    if n == 0:
+        return GaussQ(1)
+    if n % 2 == 1:
+        return GaussQ(0)
+    B = [[GaussQ.of(A[i][j]) for j in range(n)] for i in range(n)]
+    c = GaussQ(1)
+    flip = False
+    h = n // 2
+    while h > 1:
+        m = 2 * h
+        k = m
+        while k > 0 and B[m - 2][k - 1] == 0:
+            k -= 1
+        if k == 0:
+            return GaussQ(0)
+        if k != m:
+            B[k - 1], B[m - 1] = B[m - 1], B[k - 1]
+            for row in B:
+                row[k - 1], row[m - 1] = row[m - 1], row[k - 1]
+            flip = not flip
+        for j in range(m - 2):
+            for i in range(j):
+                d = B[m - 2][m - 1] * B[i][j] - B[i][m - 2] * B[j][m - 1] + B[j][m - 2] * B[i][m - 1]
+                B[i][j] = d / c
+                B[j][i] = -B[i][j]
+        c = B[m - 2][m - 1]
+        h -= 1
+    return -B[0][1] if flip else B[0][1]

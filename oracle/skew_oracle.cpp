@@ -37,6 +37,7 @@ static inline quad qhypot(quad a, quad b) { return hypotq(a, b); }
 static inline quad qsin(quad x) { return sinq(x); }
 static inline quad qcos(quad x) { return cosq(x); }
 static inline quad qexp(quad x) { return expq(x); }
+static inline quad qatan2(quad y, quad x) { return atan2q(y, x); }
 static const quad QEPS = (quad)1 / ((quad)(1ULL << 56) * (quad)(1ULL << 56));  // 2^-112
 #else
 typedef long double quad;  // IEEE binary128 on aarch64 Linux
@@ -47,6 +48,7 @@ static inline quad qhypot(quad a, quad b) { return hypotl(a, b); }
 static inline quad qsin(quad x) { return sinl(x); }
 static inline quad qcos(quad x) { return cosl(x); }
 static inline quad qexp(quad x) { return expl(x); }
+static inline quad qatan2(quad y, quad x) { return atan2l(y, x); }
 static const quad QEPS = (quad)1 / ((quad)(1ULL << 56) * (quad)(1ULL << 56));  // 2^-112
 #endif
 
@@ -59,6 +61,8 @@ template <> struct M<double> {
   static double sin(double x) { return std::sin(x); }
   static double cos(double x) { return std::cos(x); }
   static double exp(double x) { return std::exp(x); }
+  static double atan2(double y, double x) { return std::atan2(y, x); }
+  static double pi() { return 3.141592653589793; }
   static double eps() { return std::numeric_limits<double>::epsilon(); }
 };
 template <> struct M<quad> {
@@ -69,6 +73,8 @@ template <> struct M<quad> {
   static quad sin(quad x) { return qsin(x); }
   static quad cos(quad x) { return qcos(x); }
   static quad exp(quad x) { return qexp(x); }
+  static quad atan2(quad y, quad x) { return qatan2(y, x); }
+  static quad pi() { return qatan2((quad)0, (quad)-1); }
   static quad eps() { return QEPS; }
 };
 
@@ -377,6 +383,65 @@ template <typename T> static void logabspf(const double* Ain, int64_t n, double*
   if (nz & 1) sg = -sg;
   *logpf = (double)lp;
   *sign = (double)sg;
+}
+
+// ---------------------------------------------------------------------------
+// Complex skew-symmetric Pfaffian by Parlett-Reid elimination with pivoting,
+// pfaffian.jl:98-137 (_pfaffian!, the running product) and :193-233
+// (_logabspfaffian!, log|Pf| and the accumulated phase).  The whole matrix is
+// updated, both triangles, as the reference does.  A is n x n ComplexF64
+// (interleaved re, im; column-major).  Outputs: logpf, ph = cis(phase) (2 doubles),
+// pf (2 doubles).  Odd n: (-Inf, 0, 0); a zero pivot column: the same.
+// ---------------------------------------------------------------------------
+template <typename T> static void pfaffian_z(const double* Ain, int64_t n, double* logpf, double* ph, double* pf) {
+  typedef cx<T> C;
+  const double ninf = -std::numeric_limits<double>::infinity();
+  if (n % 2 == 1) {  // :97, :195
+    *logpf = ninf;
+    ph[0] = ph[1] = pf[0] = pf[1] = 0;
+    return;
+  }
+  std::vector<C> A((size_t)n * n);
+  for (int64_t i = 0; i < n * n; i++) A[i] = C(T(Ain[2 * i]), T(Ain[2 * i + 1]));
+  auto at = [&](int64_t i, int64_t j) -> C& { return A[i + j * n]; };
+  std::vector<C> tau(std::max<int64_t>(n, 1));
+  T lp = 0, phase = 0;
+  C prod(T(1), T(0));
+  for (int64_t k = 0; k + 1 < n; k += 2) {
+    // :102 / :201  kp = k + argmaxabs(A[k+1:end, k]) (first maximum)
+    int64_t kp = k + 1;
+    T best = cabs(at(k + 1, k));
+    for (int64_t i = k + 2; i < n; i++) {
+      const T v = cabs(at(i, k));
+      if (v > best) {
+        best = v;
+        kp = i;
+      }
+    }
+    if (kp != k + 1) {  // :103-111 / :202-210
+      for (int64_t l = k; l < n; l++) std::swap(at(k + 1, l), at(kp, l));
+      for (int64_t l = k; l < n; l++) std::swap(at(l, k + 1), at(l, kp));
+      prod = -prod;
+      phase += M<T>::pi();
+    }
+    if (is_zero(at(k + 1, k))) {  // :127-129 / :226-228
+      *logpf = ninf;
+      ph[0] = ph[1] = pf[0] = pf[1] = 0;
+      return;
+    }
+    const C piv = at(k, k + 1);  // :115-117 / :214-216
+    for (int64_t j = k + 2; j < n; j++) tau[j] = at(k, j) / piv;
+    prod = prod * piv;
+    lp += M<T>::log(cabs(piv));
+    phase += M<T>::atan2(piv.im, piv.re);
+    for (int64_t c = k + 2; c < n; c++)  // :118-125 / :217-224
+      for (int64_t r = k + 2; r < n; r++) at(r, c) = at(r, c) + (tau[r] * at(c, k + 1) - tau[c] * at(r, k + 1));
+  }
+  *logpf = (double)lp;
+  ph[0] = (double)M<T>::cos(phase);
+  ph[1] = (double)M<T>::sin(phase);
+  pf[0] = (double)prod.re;
+  pf[1] = (double)prod.im;
 }
 
 // ---------------------------------------------------------------------------
@@ -970,6 +1035,13 @@ void orc_formq_d(const double* A, int64_t n, const double* tau, double* Q) { for
 
 void orc_logabspf_d(const double* A, int64_t n, double* logpf, double* sign) { logabspf<double>(A, n, logpf, sign); }
 void orc_logabspf_q(const double* A, int64_t n, double* logpf, double* sign) { logabspf<quad>(A, n, logpf, sign); }
+
+void orc_pfaffian_z(const double* A, int64_t n, double* logpf, double* ph, double* pf) {
+  pfaffian_z<double>(A, n, logpf, ph, pf);
+}
+void orc_pfaffian_zq(const double* A, int64_t n, double* logpf, double* ph, double* pf) {
+  pfaffian_z<quad>(A, n, logpf, ph, pf);
+}
 
 int orc_skewtrieigvals_d(double* ev, int64_t N, double* vals) { return skewtrieigvals<double>(ev, N, vals); }
 int orc_skewtrieigvals_q(double* ev, int64_t N, double* vals) {

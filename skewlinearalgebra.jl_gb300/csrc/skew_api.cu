@@ -1092,6 +1092,104 @@ int skew_batch_func_z(skew_handle_t h, const double* A, int64_t n, int64_t count
 }
 
 // ---------------------------------------------------------------------------
+// Complex skew-symmetric Pfaffian (pfaffian.jl:98-137, :193-233): one CTA per
+// matrix up to pfz_cta_max(), above that one cooperative grid per matrix.
+// ---------------------------------------------------------------------------
+static int pfz_cta_max() {
+  static int v = -1;
+  if (v < 0) {
+    const char* s = getenv("SKEW_PFZ_CTA_MAX");
+    v = (s && *s) ? std::max(0, std::min(160, atoi(s))) : 160;
+  }
+  return v;
+}
+
+static int pfz_run(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* phase, double* pf,
+                   int check, int* info) {
+  if (!h || n < 0 || (n > 0 && (!A || lda < n))) return SKEW_BAD_ARG;
+  if (n > (1LL << 15)) return SKEW_UNSUPPORTED;
+  if (n > pfz_cta_max()) {
+    int st = ensure_ws(h, sizeof(double) * pfz_grid_ws_doubles((int)n));
+    if (st) return st;
+    if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+    CK(launch_pfz_grid((zc*)A, lda, (int)n, check, logpf, phase, pf, info, (double*)h->ws, h->sms, h->stream));
+    return SKEW_OK;
+  }
+  PfzParams P{};
+  P.A = (const zc*)A;
+  P.lda = lda;
+  P.stride = 0;
+  P.n = (int)n;
+  P.count = 1;
+  P.check = check;
+  P.smem_matrix = 1;
+  P.logpf = logpf;
+  P.phase = phase;
+  P.pf = pf;
+  P.status = info;
+  CK(launch_pfz_cta(P, 1, h->stream));
+  return SKEW_OK;
+}
+
+int skew_logabspf_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* phase, int check,
+                    int* info) {
+  if (!logpf || !phase) return SKEW_BAD_ARG;
+  return pfz_run(h, A, n, lda, logpf, phase, nullptr, check, info);
+}
+
+int skew_pfaffian_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* pf, int check, int* info) {
+  if (!pf) return SKEW_BAD_ARG;
+  return pfz_run(h, A, n, lda, nullptr, nullptr, pf, check, info);
+}
+
+int skew_batch_logabspf_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* logpf, double* phase,
+                          double* pf, int check, int* status) {
+  if (!h || n < 0 || count < 0 || (count > 0 && n > 0 && !A)) return SKEW_BAD_ARG;
+  if (!logpf && !phase && !pf) return SKEW_BAD_ARG;
+  if (n > (1LL << 15) || count > INT32_MAX) return SKEW_UNSUPPORTED;
+  if (count == 0) return SKEW_OK;
+  const int nn = (int)n;
+  const bool even = nn % 2 == 0 && nn > 0;
+  const bool sm = !even || pfz_smem_fits(nn);
+  if (even && !sm && nn > pfz_cta_max() && count < h->sms) {
+    // few large matrices: one grid per matrix, on a copy (the input is read only)
+    const size_t mat = 2 * (size_t)n * n, gw = pfz_grid_ws_doubles(nn);
+    int st = ensure_ws(h, sizeof(double) * (mat + gw));
+    if (st) return st;
+    double* W = (double*)h->ws;
+    if (status) CK(cudaMemsetAsync(status, 0, sizeof(int) * count, h->stream));
+    for (int64_t b = 0; b < count; b++) {
+      CK(cudaMemcpyAsync(W, A + b * mat, sizeof(double) * mat, cudaMemcpyDeviceToDevice, h->stream));
+      CK(launch_pfz_grid((zc*)W, n, nn, check, logpf ? logpf + b : nullptr, phase ? phase + 2 * b : nullptr,
+                         pf ? pf + 2 * b : nullptr, status ? status + b : nullptr, W + mat, h->sms, h->stream));
+    }
+    return SKEW_OK;
+  }
+  PfzParams P{};
+  P.A = (const zc*)A;
+  P.lda = n;
+  P.stride = n * n;
+  P.n = nn;
+  P.count = (int)count;
+  P.check = check;
+  P.smem_matrix = (sm && even) ? 1 : 0;
+  P.logpf = logpf;
+  P.phase = phase;
+  P.pf = pf;
+  P.status = status;
+  const int occ = pfz_cta_occupancy(nn, P.smem_matrix != 0);
+  int64_t grid = std::min<int64_t>(count, (int64_t)h->sms * (P.smem_matrix || !even ? occ : std::min(occ, 2)));
+  if (even && !P.smem_matrix) {
+    P.slot = n * (n - 1) / 2;
+    int st = ensure_ws(h, sizeof(double) * 2 * (size_t)P.slot * grid);
+    if (st) return st;
+    P.gws = (zc*)h->ws;
+  }
+  CK(launch_pfz_cta(P, (int)grid, h->stream));
+  return SKEW_OK;
+}
+
+// ---------------------------------------------------------------------------
 // SkewHermTridiagonal entry points (tridiag.jl): no reduction, Q = I
 // ---------------------------------------------------------------------------
 int skew_tridiag_eigvals_d(skew_handle_t h, const double* ev, int64_t n, double* vals_im, int* info) {

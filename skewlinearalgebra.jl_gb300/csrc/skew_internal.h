@@ -211,6 +211,46 @@ cudaError_t launch_pf_from_tridiag(const double* ev, const double* tau, int n, d
                                    const double* notskew, cudaStream_t st);
 cudaError_t launch_check_skew(const double* A, int64_t lda, int n, double* flag, int sms, cudaStream_t st);
 
+// Complex skew-symmetric Pfaffian, Parlett-Reid with pivoting (skew_pfz.cu).
+struct zc;
+struct PfzParams {
+  const zc* A;  // matrix b at A + b * stride, column-major, leading dimension lda; read only
+  int64_t lda, stride;
+  int n, count, check;
+  int smem_matrix;  // 1: packed triangle in shared memory, 0: in the per-CTA slot of gws
+  zc* gws;
+  int64_t slot;  // complex entries per slot (n (n - 1) / 2)
+  double* logpf;  // [count] (nullable)
+  double* phase;  // [2 count] cis(phase) (nullable)
+  double* pf;     // [2 count] the product (nullable)
+  int* status;    // [count] (nullable)
+};
+struct PfzGridParams {
+  zc* A;  // in place on the strictly lower triangle
+  int64_t lda;
+  int n;
+  zc* tau;
+  zc* cc;
+  zc* piv;  // n/2 recorded pivots
+  unsigned long long* part_v;  // argmax keys
+  int* part_i;
+  unsigned* sync;
+  int* err;
+  const double* notskew;
+  double* logpf;
+  double* phase;
+  double* pf;
+  int* info;
+};
+size_t pfz_cta_smem(int n, bool smem_matrix);
+bool pfz_smem_fits(int n);
+int pfz_cta_occupancy(int n, bool smem_matrix);
+cudaError_t launch_pfz_cta(const PfzParams& P, int grid, cudaStream_t st);
+size_t pfz_grid_ws_doubles(int n);
+// n >= 1 (odd n: Pf = 0); check != 0 tests A == -transpose(A) first (info = SKEW_NOT_SKEW).
+cudaError_t launch_pfz_grid(zc* A, int64_t lda, int n, int check, double* logpf, double* phase, double* pf,
+                            int* info, double* ws, int sms, cudaStream_t st);
+
 // FP64 DFMA microbenchmark kernel (skew_api.cu).
 cudaError_t launch_dfma_probe(double* out, int blocks, int iters, cudaStream_t st);
 

@@ -169,17 +169,33 @@ def logabspfaffian_(A, check_skew: bool = False) -> Tuple[float, float]:
     return lp, sg
 
 
-def logabspfaffian(A) -> Tuple[float, float]:
+def _is_complex(A) -> bool:
+    if isinstance(A, SkewHermitian):
+        return False
+    if isinstance(A, torch.Tensor):
+        return A.is_complex()
+    return np.iscomplexobj(A)
+
+
+def logabspfaffian(A):
     """logabspfaffian(A) (pfaffian.jl:236, :246): (log|Pf(A)|, sign); A is not modified.
-    Plain matrices are checked for exact skew-symmetry first (pfaffian.jl:255)."""
+    Plain matrices are checked for exact skew-symmetry first (pfaffian.jl:255).
+    Complex matrices must be skew-symmetric (A == -transpose(A)); they take the
+    Parlett-Reid path and return (log|Pf(A)|, cis(phase)) (pfaffian.jl:193-233)."""
+    if _is_complex(A):
+        return logabspfaffian_complex(A)
     if isinstance(A, SkewHermitian):
         return logabspfaffian_(A.copy())
     S = SkewHermitian(A, check_skew=False)
     return logabspfaffian_(S.copy(), check_skew=True)
 
 
-def pfaffian(A) -> float:
-    """pfaffian(A) for real A, returned as sign * exp(log|Pf|) (pfaffian.jl:74-84)."""
+def pfaffian(A):
+    """pfaffian(A) for real A, returned as sign * exp(log|Pf|) (pfaffian.jl:74-84);
+    for complex skew-symmetric A the product of the Parlett-Reid pivots
+    (pfaffian.jl:98-137)."""
+    if _is_complex(A):
+        return pfaffian_complex(A)
     lp, sg = logabspfaffian(A)
     return float(sg * np.exp(lp))
 
@@ -564,6 +580,79 @@ def batch_exp_vjp_complex(mats, cots):
     h = handle().bind()
     check(_lib.load().skew_batch_exp_vjp_z(h, _ptr(A), n, count, _ptr(C), _ptr(G), None), "batch_exp_vjp_complex")
     return _unstack_complex(G)
+
+
+# ---------------------------------------------------------------------------
+# Complex skew-symmetric Pfaffian (pfaffian.jl:98-137, :193-233)
+# ---------------------------------------------------------------------------
+def _complex_work(A) -> torch.Tensor:
+    """A device copy of A (complex128, column-major storage)."""
+    if isinstance(A, torch.Tensor):
+        if A.dim() != 2 or A.shape[0] != A.shape[1]:
+            raise ValueError("a square matrix is required")
+        return A.to(torch.complex128).cuda().contiguous().clone()
+    A = np.asarray(A, dtype=np.complex128)
+    if A.ndim != 2 or A.shape[0] != A.shape[1]:
+        raise ValueError("a square matrix is required")
+    return to_device_complex(A)
+
+
+def _pfz_info(info: torch.Tensor, where: str):
+    st = int(info.item())
+    if st == _lib.SKEW_NOT_SKEW:
+        raise ValueError("Pfaffian requires a skew-symmetric matrix")
+    if st not in (_lib.SKEW_OK, _lib.SKEW_SINGULAR):
+        raise RuntimeError(f"{where}: {_lib.load().skew_status_string(st).decode()}")
+
+
+def logabspfaffian_complex_(T: torch.Tensor, check_skew: bool = True):
+    """logabspfaffian!(A) for a complex skew-symmetric device matrix (column-major
+    storage), in place: (log|Pf(A)|, cis(phase)) with Pf(A) = cis(phase) exp(log|Pf|)."""
+    n = T.shape[0]
+    out = torch.zeros(3, dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_logabspf_z(h, _ptr(T), n, n, _ptr(out), ctypes.c_void_p(out.data_ptr() + 8),
+                                      int(check_skew), _ptr(info)), "logabspfaffian")
+    _pfz_info(info, "logabspfaffian")
+    lp, c, s_ = out.tolist()
+    return lp, complex(c, s_)
+
+
+def logabspfaffian_complex(A):
+    """logabspfaffian(A::AbstractMatrix{ComplexF64}) (pfaffian.jl:193-233, :259-263)."""
+    return logabspfaffian_complex_(_complex_work(A), check_skew=True)
+
+
+def pfaffian_complex(A) -> complex:
+    """pfaffian(A::AbstractMatrix{ComplexF64}) (pfaffian.jl:98-137, :160-164): the
+    running product of the Parlett-Reid pivots."""
+    T = _complex_work(A)
+    n = T.shape[0]
+    out = torch.zeros(2, dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    check(_lib.load().skew_pfaffian_z(h, _ptr(T), n, n, _ptr(out), 1, _ptr(info)), "pfaffian")
+    _pfz_info(info, "pfaffian")
+    re, im = out.tolist()
+    return complex(re, im)
+
+
+def batch_logabspfaffian_complex(mats, check_skew: bool = True):
+    """logabspfaffian and pfaffian of many complex skew-symmetric matrices of one
+    size (skew_batch_logabspf_z).  ``mats``: a list of host matrices, or a device
+    tensor count x n x n holding each matrix column-major.  Returns numpy arrays
+    (log|Pf|, cis(phase), Pf, status)."""
+    A = mats if isinstance(mats, torch.Tensor) else _stack_complex(mats)
+    count, n = A.shape[0], A.shape[1]
+    lp = torch.zeros(count, dtype=torch.float64, device="cuda")
+    ph = torch.zeros(count, dtype=torch.complex128, device="cuda")
+    pf = torch.zeros(count, dtype=torch.complex128, device="cuda")
+    st = torch.zeros(count, dtype=torch.int32, device="cuda")
+    h = handle().bind()
+    check(_lib.load().skew_batch_logabspf_z(h, _ptr(A), n, count, _ptr(lp), _ptr(ph), _ptr(pf), int(check_skew),
+                                            _ptr(st)), "batch_logabspfaffian_complex")
+    return lp.cpu().numpy(), ph.cpu().numpy(), pf.cpu().numpy(), st.cpu().numpy()
 
 
 def measure_fp64_peak() -> float:

@@ -245,3 +245,61 @@ def test_complex_hessenberg(oracle):
         T = np.diag(1j * dvim) + np.diag(ev.astype(complex), -1) - np.diag(ev.astype(complex), 1)
         # eigenvalues of T equal those of A (unitary similarity)
         np.testing.assert_allclose(np.sort(np.linalg.eigvals(T).imag), np.sort(np.linalg.eigvals(A).imag), atol=1e-12)
+
+
+# --- complex skew-symmetric Pfaffian (pfaffian.jl:98-137, :193-233) ---------
+def complex_int_skew(n, seed):
+    """The reference's recipe (runtests.jl:408-409): R with entries in
+    (-10:10) + i(-10:10), A = (R - transpose(R)) / 2."""
+    rng = np.random.default_rng(seed)
+    R = rng.integers(-10, 11, (n, n)) + 1j * rng.integers(-10, 11, (n, n))
+    return (R - R.T) / 2
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 10, 20])
+def test_complex_pfaffian_exact(oracle, n):
+    """runtests.jl:406-420: Pf(A) ~ exactpfaffian(Complex{Rational{BigInt}}), Pf^2 ~ det(A)
+    (atol sqrt(eps) max(1, |det A|)), Pf ~ sign * exp(logpf); the FP64 restatement is
+    held to 1e-13 here, binary128 is exact to FP64 rounding."""
+    for seed in range(3):
+        A = complex_int_skew(n, 1000 * n + seed)
+        exact = complex(oracle.exact_pfaffian_complex(A.tolist()))
+        for quad, tol in ((False, 1e-13), (True, 1e-16)):
+            lp, ph, pf = oracle.pfaffian_complex(A, quad=quad)
+            assert abs(pf - exact) <= tol * max(1.0, abs(exact))
+            if exact != 0:
+                assert abs(ph * np.exp(lp) - exact) <= 1e-13 * abs(exact)
+            else:
+                assert lp == -np.inf and ph == 0
+        d = np.linalg.det(A)
+        assert abs(exact**2 - d) <= np.sqrt(np.finfo(float).eps) * max(1.0, abs(d))
+
+
+def test_complex_pfaffian_known_answers(oracle):
+    """The real known answers (runtests.jl:423, :426-430, :433) through the complex path."""
+    A = np.array(GOLD["issue49"]["A"], dtype=np.complex128)
+    _, _, pf = oracle.pfaffian_complex(A, quad=True)
+    assert abs(pf - GOLD["issue49"]["pfaffian"]) <= 1e-9
+    A = np.array(GOLD["issue121"]["A"], dtype=np.complex128)
+    lp, ph, pf = oracle.pfaffian_complex(A)
+    assert pf == 1 and lp == 0 and ph == 1
+    rng = np.random.default_rng(5)
+    for _ in range(10):
+        a, b, c, d, e, f = rng.integers(-10, 11, 6)
+        M = np.array([[0, a, b, c], [-a, 0, d, e], [-b, -d, 0, f], [-c, -e, -f, 0]], dtype=np.complex128)
+        _, _, pf = oracle.pfaffian_complex(M * (1 + 2j))  # Pf(s M) = s^2 Pf(M)
+        assert abs(pf - (c * d - b * e + a * f) * (1 + 2j) ** 2) <= 1e-12 * max(1, abs(pf))
+
+
+def test_complex_pfaffian_random_double_vs_quad(oracle):
+    rng = np.random.default_rng(3)
+    for n in (6, 31, 64):
+        R = rng.standard_normal((n + n % 2, n + n % 2)) + 1j * rng.standard_normal((n + n % 2, n + n % 2))
+        A = (R - R.T) / 2
+        lp, ph, _ = oracle.pfaffian_complex(A)
+        lq, pq, _ = oracle.pfaffian_complex(A, quad=True)
+        assert abs(lp - lq) <= 1e-12 * max(1.0, abs(lq))
+        assert abs(ph - pq) <= 1e-12
+        sign, logdet = np.linalg.slogdet(A)
+        assert abs(2 * lq - logdet) <= 1e-11 * max(1.0, abs(logdet))
+        assert abs(pq**2 - sign) <= 1e-11
