@@ -248,6 +248,27 @@ SKEW_API int skew_batch_func_z(skew_handle_t h, const double* A, int64_t n, int6
                                int* status);
 
 /* ---------------------------------------------------------------------------
+ * Singular values and vectors from the eigenpairs (eigen.jl:110-144): the eigenvalues'
+ * imaginary parts lambda stably sorted by |lambda| descending (sortperm(vals; by = abs,
+ * rev = true)); S = |lambda|; U = the eigenvectors in that order; V = -i U with the
+ * columns of negative lambda negated, so that A = U diag(S) V^H (the reference returns
+ * SVD(U, S, adjoint(V))).  A is destroyed.
+ * ------------------------------------------------------------------------- */
+/* LA.svdvals!(A::SkewHermitian{Float64})  eigen.jl:110-114: S[n] descending. */
+SKEW_API int skew_svdvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* S, int* info);
+/* LA.svd!(A::SkewHermitian{Float64})  eigen.jl:119-136: S[n], U = Ur + i Ui, V = Vr + i Vi (n x n,
+ * ldu; ldu == lda == n for n <= 1024, as skew_eigen_d). */
+SKEW_API int skew_svd_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* S, double* Ur, double* Ui,
+                        double* Vr, double* Vi, int64_t ldu, int* info);
+/* LA.svdvals!(A::SkewHermitian{ComplexF64})  eigen.jl:116 (svdvals of Hermitian(i A)): S[n] descending. */
+SKEW_API int skew_svdvals_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* S, int* info);
+/* LA.svd(A::SkewHermitian{ComplexF64})  eigen.jl:138-142 (svd of Hermitian(i A), which LinearAlgebra
+ * forms from its eigenpairs by the same rule): S[n], U, V ComplexF64 (n x n, ldu).  Singular
+ * vectors are defined up to a phase per column (LAPACK's choice in the reference). */
+SKEW_API int skew_svd_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* S, double* U, double* V,
+                        int64_t ldu, int* info);
+
+/* ---------------------------------------------------------------------------
  * Complex skew-symmetric matrices (A == -transpose(A), ComplexF64): the Pfaffian by
  * Parlett-Reid elimination with pivoting (pfaffian.jl:98-137 and :193-233).
  * check != 0 verifies A == -transpose(A) exactly first (pfaffian.jl:162, :261; isskewsymmetric,
@@ -289,6 +310,15 @@ SKEW_API int skew_tridiag_eigvals_z(skew_handle_t h, const double* ev, const dou
                                     double* vals_im, int* info);
 SKEW_API int skew_tridiag_eigen_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n,
                                   double* vals_im, double* V, int64_t ldv, int* info);
+/* LA.svdvals! / LA.svd! of a SkewHermTridiagonal  tridiag.jl:526-555: as skew_svdvals_d /
+ * skew_svd_d on its eigenpairs (Float64: ev[n-1]; ComplexF64: ev[n-1] complex and dvim[n] or NULL). */
+SKEW_API int skew_tridiag_svdvals_d(skew_handle_t h, const double* ev, int64_t n, double* S, int* info);
+SKEW_API int skew_tridiag_svd_d(skew_handle_t h, const double* ev, int64_t n, double* S, double* Ur, double* Ui,
+                                double* Vr, double* Vi, int64_t ldu, int* info);
+SKEW_API int skew_tridiag_svdvals_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n, double* S,
+                                    int* info);
+SKEW_API int skew_tridiag_svd_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n, double* S,
+                                double* U, double* V, int64_t ldu, int* info);
 
 /* Diagnostics: measured FP64 DFMA throughput of the current device in TFLOP/s
  * (runs a short microbenchmark on the handle's stream and synchronizes). */

@@ -23,6 +23,8 @@ struct skew_handle_st {
   int sms = 0;
   void* ws = nullptr;  // grow-only workspace, stream ordered
   size_t ws_bytes = 0;
+  void* aux = nullptr;  // small grow-only scratch kept across calls that use ws themselves
+  size_t aux_bytes = 0;
   struct skew_batch_plan_st* plan1 = nullptr;  // batch-of-one plan for single-matrix eigen/exp/cis
   int64_t plan1_n = 0;
 };
@@ -99,6 +101,16 @@ static int ensure_ws(skew_handle_t h, size_t bytes) {
   return SKEW_OK;
 }
 
+static int ensure_aux(skew_handle_t h, size_t bytes) {
+  if (bytes <= h->aux_bytes) return SKEW_OK;
+  if (h->aux) CK(cudaFreeAsync(h->aux, h->stream));
+  h->aux = nullptr;
+  h->aux_bytes = 0;
+  CK(cudaMallocAsync(&h->aux, bytes, h->stream));
+  h->aux_bytes = bytes;
+  return SKEW_OK;
+}
+
 extern "C" {
 
 int skew_version(void) { return 100; }
@@ -135,17 +147,16 @@ int skew_create(skew_handle_t* handle) {
 int skew_destroy(skew_handle_t h) {
   if (!h) return SKEW_BAD_ARG;
   if (h->plan1) skew_batch_plan_destroy(h->plan1);
-  if (h->ws) {
-    cudaFreeAsync(h->ws, h->stream);
-    cudaStreamSynchronize(h->stream);
-  }
+  if (h->ws) cudaFreeAsync(h->ws, h->stream);
+  if (h->aux) cudaFreeAsync(h->aux, h->stream);
+  if (h->ws || h->aux) cudaStreamSynchronize(h->stream);
   delete h;
   return SKEW_OK;
 }
 
 int skew_set_stream(skew_handle_t h, skew_stream_t s) {
   if (!h) return SKEW_BAD_ARG;
-  if (h->ws && (cudaStream_t)s != h->stream) {  // keep the workspace ordered on the new stream
+  if ((h->ws || h->aux) && (cudaStream_t)s != h->stream) {  // keep the workspaces ordered on the new stream
     cudaEvent_t ev;
     CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     CK(cudaEventRecord(ev, h->stream));
@@ -1190,6 +1201,88 @@ int skew_batch_logabspf_z(skew_handle_t h, const double* A, int64_t n, int64_t c
 }
 
 // ---------------------------------------------------------------------------
+// svdvals / svd from the eigenpairs (eigen.jl:110-144, tridiag.jl:526-555)
+// ---------------------------------------------------------------------------
+// aux layout: vals (n doubles), signs (n doubles), perm (n ints)
+static int svd_aux(skew_handle_t h, int64_t n, double** vals, double** sgn, int** perm) {
+  const size_t nn = (size_t)std::max<int64_t>(n, 1);
+  int st = ensure_aux(h, nn * (2 * sizeof(double) + sizeof(int)));
+  if (st) return st;
+  *vals = (double*)h->aux;
+  *sgn = *vals + nn;
+  *perm = (int*)(*sgn + nn);
+  return SKEW_OK;
+}
+
+// S from eigenvalue imaginary parts already in aux
+static int svdvals_finish(skew_handle_t h, int64_t n, const double* vals, double* S) {
+  CK(launch_svd_rank(vals, (int)n, n, 1, nullptr, S, n, nullptr, h->stream));
+  return SKEW_OK;
+}
+
+int skew_svdvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* S, int* info) {
+  if (!h || n < 0 || (n > 0 && (!A || !S || lda < n))) return SKEW_BAD_ARG;
+  if (n == 0) return info ? (cudaMemsetAsync(info, 0, sizeof(int), h->stream) == cudaSuccess ? SKEW_OK
+                                                                                          : SKEW_CUDA_ERROR)
+                          : SKEW_OK;
+  double *vals, *sgn;
+  int* perm;
+  int st = svd_aux(h, n, &vals, &sgn, &perm);
+  if (st) return st;
+  st = skew_eigvals_d(h, A, n, lda, vals, info);
+  if (st) return st;
+  return svdvals_finish(h, n, vals, S);
+}
+
+int skew_svd_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* S, double* Ur, double* Ui, double* Vr,
+               double* Vi, int64_t ldu, int* info) {
+  if (!h || n < 0 || (n > 0 && (!A || !S || !Ur || !Ui || !Vr || !Vi || lda < n || ldu < n))) return SKEW_BAD_ARG;
+  if (n == 0) return info ? (cudaMemsetAsync(info, 0, sizeof(int), h->stream) == cudaSuccess ? SKEW_OK
+                                                                                          : SKEW_CUDA_ERROR)
+                          : SKEW_OK;
+  double *vals, *sgn;
+  int* perm;
+  int st = svd_aux(h, n, &vals, &sgn, &perm);
+  if (st) return st;
+  st = skew_eigen_d(h, A, n, lda, vals, Vr, Vi, ldu, info);  // eigenvectors W in the V planes
+  if (st) return st;
+  CK(launch_svd_rank(vals, (int)n, n, 1, perm, S, n, sgn, h->stream));
+  CK(launch_svd_vectors_d(Vr, Vi, (int)n, ldu, perm, sgn, Ur, Ui, Vr, Vi, h->stream));
+  return SKEW_OK;
+}
+
+int skew_svdvals_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* S, int* info) {
+  if (!h || n < 0 || (n > 0 && (!A || !S || lda < n))) return SKEW_BAD_ARG;
+  if (n == 0) return info ? (cudaMemsetAsync(info, 0, sizeof(int), h->stream) == cudaSuccess ? SKEW_OK
+                                                                                          : SKEW_CUDA_ERROR)
+                          : SKEW_OK;
+  double *vals, *sgn;
+  int* perm;
+  int st = svd_aux(h, n, &vals, &sgn, &perm);
+  if (st) return st;
+  st = skew_eigvals_z(h, A, n, lda, vals, info);
+  if (st) return st;
+  return svdvals_finish(h, n, vals, S);
+}
+
+int skew_svd_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* S, double* U, double* V, int64_t ldu,
+               int* info) {
+  if (!h || n < 0 || (n > 0 && (!A || !S || !U || !V || lda < n || ldu < n))) return SKEW_BAD_ARG;
+  if (n == 0) return info ? (cudaMemsetAsync(info, 0, sizeof(int), h->stream) == cudaSuccess ? SKEW_OK
+                                                                                          : SKEW_CUDA_ERROR)
+                          : SKEW_OK;
+  double *vals, *sgn;
+  int* perm;
+  int st = svd_aux(h, n, &vals, &sgn, &perm);
+  if (st) return st;
+  st = skew_eigen_z(h, A, n, lda, vals, V, ldu, info);
+  if (st) return st;
+  CK(launch_svd_rank(vals, (int)n, n, 1, perm, S, n, sgn, h->stream));
+  CK(launch_svd_vectors_z(V, (int)n, ldu, perm, sgn, U, V, h->stream));
+  return SKEW_OK;
+}
+
+// ---------------------------------------------------------------------------
 // SkewHermTridiagonal entry points (tridiag.jl): no reduction, Q = I
 // ---------------------------------------------------------------------------
 int skew_tridiag_eigvals_d(skew_handle_t h, const double* ev, int64_t n, double* vals_im, int* info) {
@@ -1298,6 +1391,57 @@ int skew_tridiag_eigen_z(skew_handle_t h, const double* ev, const double* dvim, 
 int skew_tridiag_eigvals_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n, double* vals_im,
                            int* info) {
   return skew_tridiag_eigen_z(h, ev, dvim, n, vals_im, nullptr, 0, info);
+}
+
+// svdvals! / svd! of a SkewHermTridiagonal (tridiag.jl:526-555): the same sort on its eigenpairs
+int skew_tridiag_svdvals_d(skew_handle_t h, const double* ev, int64_t n, double* S, int* info) {
+  if (!h || n < 1 || !S) return SKEW_BAD_ARG;
+  double *vals, *sgn;
+  int* perm;
+  int st = svd_aux(h, n, &vals, &sgn, &perm);
+  if (st) return st;
+  st = skew_tridiag_eigvals_d(h, ev, n, vals, info);
+  if (st) return st;
+  return svdvals_finish(h, n, vals, S);
+}
+
+int skew_tridiag_svd_d(skew_handle_t h, const double* ev, int64_t n, double* S, double* Ur, double* Ui, double* Vr,
+                       double* Vi, int64_t ldu, int* info) {
+  if (!h || n < 1 || !S || !Ur || !Ui || !Vr || !Vi || ldu < n) return SKEW_BAD_ARG;
+  double *vals, *sgn;
+  int* perm;
+  int st = svd_aux(h, n, &vals, &sgn, &perm);
+  if (st) return st;
+  st = skew_tridiag_eigen_d(h, ev, n, vals, Vr, Vi, ldu, info);
+  if (st) return st;
+  CK(launch_svd_rank(vals, (int)n, n, 1, perm, S, n, sgn, h->stream));
+  CK(launch_svd_vectors_d(Vr, Vi, (int)n, ldu, perm, sgn, Ur, Ui, Vr, Vi, h->stream));
+  return SKEW_OK;
+}
+
+int skew_tridiag_svdvals_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n, double* S, int* info) {
+  if (!h || n < 1 || !S) return SKEW_BAD_ARG;
+  double *vals, *sgn;
+  int* perm;
+  int st = svd_aux(h, n, &vals, &sgn, &perm);
+  if (st) return st;
+  st = skew_tridiag_eigvals_z(h, ev, dvim, n, vals, info);
+  if (st) return st;
+  return svdvals_finish(h, n, vals, S);
+}
+
+int skew_tridiag_svd_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n, double* S, double* U,
+                       double* V, int64_t ldu, int* info) {
+  if (!h || n < 1 || !S || !U || !V || ldu < n) return SKEW_BAD_ARG;
+  double *vals, *sgn;
+  int* perm;
+  int st = svd_aux(h, n, &vals, &sgn, &perm);
+  if (st) return st;
+  st = skew_tridiag_eigen_z(h, ev, dvim, n, vals, V, ldu, info);
+  if (st) return st;
+  CK(launch_svd_rank(vals, (int)n, n, 1, perm, S, n, sgn, h->stream));
+  CK(launch_svd_vectors_z(V, (int)n, ldu, perm, sgn, U, V, h->stream));
+  return SKEW_OK;
 }
 
 // ---------------------------------------------------------------------------

@@ -251,6 +251,17 @@ size_t pfz_grid_ws_doubles(int n);
 cudaError_t launch_pfz_grid(zc* A, int64_t lda, int n, int check, double* logpf, double* phase, double* pf,
                             int* info, double* ws, int sms, cudaStream_t st);
 
+// svdvals / svd from the eigenpairs (skew_svd.cu).  Stable rank sort of each problem's
+// values by |v| descending: perm (batch x n, nullable), S (sstride apart, nullable),
+// sgn (batch x n, -1 for negative values, nullable).
+cudaError_t launch_svd_rank(const double* vals, int n, int64_t vstride, int batch, int* perm, double* S,
+                            int64_t sstride, double* sgn, cudaStream_t st);
+// U[:, k] = W[:, perm[k]], V[:, k] = -i sgn[k] U[:, k]; W may share storage with V.
+cudaError_t launch_svd_vectors_d(const double* Wr, const double* Wi, int n, int64_t ld, const int* perm,
+                                 const double* sgn, double* Ur, double* Ui, double* Vr, double* Vi, cudaStream_t st);
+cudaError_t launch_svd_vectors_z(const double* W, int n, int64_t ld, const int* perm, const double* sgn, double* U,
+                                 double* V, cudaStream_t st);
+
 // FP64 DFMA microbenchmark kernel (skew_api.cu).
 cudaError_t launch_dfma_probe(double* out, int blocks, int iters, cudaStream_t st);
 

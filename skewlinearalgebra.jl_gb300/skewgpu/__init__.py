@@ -291,6 +291,67 @@ def eigen(A):
     return 1j * vals.cpu().numpy(), from_device(Vr) + 1j * from_device(Vi)
 
 
+def svdvals(A) -> np.ndarray:
+    """svdvals(A::SkewHermitian) (eigen.jl:110-117): singular values, descending.
+    Real input: |imag(eigvals)|; complex skew-Hermitian: svdvals(Hermitian(i A))."""
+    n = _square_n(A)
+    S = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    if _is_complex(A):
+        W = _skew_hermitian_complex(A)
+        check(_lib.load().skew_svdvals_z(h, _ptr(W), n, n, _ptr(S), _ptr(info)), "svdvals")
+    else:
+        X = _as_skew(A).copy()
+        check(_lib.load().skew_svdvals_d(h, _ptr(X.data), n, n, _ptr(S), _ptr(info)), "svdvals")
+    _info_ok(info, "svdvals")
+    return S.cpu().numpy()[:n]
+
+
+def svd(A):
+    """svd(A::SkewHermitian) (eigen.jl:119-144): (U, S, Vt) with A = U diag(S) Vt, as
+    LinearAlgebra.SVD(U, S, Vt); U and Vt complex.  The eigenvectors are sorted stably
+    by |lambda| descending, S = |lambda| and V = -i U with the columns of negative
+    lambda negated (complex input: the same rule on Hermitian(i A), as LinearAlgebra's
+    svd of a Hermitian matrix)."""
+    n = _square_n(A)
+    S = torch.zeros(max(n, 1), dtype=torch.float64, device="cuda")
+    info = _info_tensor()
+    h = handle().bind()
+    if _is_complex(A):
+        W = _skew_hermitian_complex(A)
+        U = torch.zeros((n, n), dtype=torch.complex128, device="cuda")
+        V = torch.zeros((n, n), dtype=torch.complex128, device="cuda")
+        check(_lib.load().skew_svd_z(h, _ptr(W), n, n, _ptr(S), _ptr(U), _ptr(V), n, _ptr(info)), "svd")
+        _info_ok(info, "svd")
+        Uh, Vh = from_device_complex(U), from_device_complex(V)
+    else:
+        X = _as_skew(A).copy()
+        planes = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for _ in range(4)]
+        check(_lib.load().skew_svd_d(h, _ptr(X.data), n, n, _ptr(S), *[_ptr(t) for t in planes], n, _ptr(info)),
+              "svd")
+        _info_ok(info, "svd")
+        Ur, Ui, Vr, Vi = (from_device(t) for t in planes)
+        Uh, Vh = Ur + 1j * Ui, Vr + 1j * Vi
+    return Uh, S.cpu().numpy()[:n], Vh.conj().T
+
+
+def schur(A):
+    """schur(A::SkewHermitian{Float64}) (skewhermitian.jl:238-243): (T, Z, values) with
+    T = Diagonal(values) as a dense complex matrix and Z the eigenvectors, A = Z T Z^H."""
+    lam, Z = eigen(A)
+    return np.diag(lam), Z, lam
+
+
+def _square_n(A) -> int:
+    if isinstance(A, SkewHermitian):
+        return A.n
+    shape = tuple(A.shape)
+    if len(shape) != 2 or shape[0] != shape[1]:
+        raise ValueError("a square matrix is required")
+    return int(shape[0])
+
+
 def exp(A) -> np.ndarray:
     """exp(A::SkewHermitian{Float64}) (exp.jl:3-35, :48), real n x n."""
     S = _as_skew(A).copy()
@@ -411,6 +472,42 @@ class SkewHermTridiagonal:
               "tridiag eigen")
         _info_ok(info, "tridiag eigen")
         return 1j * vals.cpu().numpy(), from_device(Vr) + 1j * from_device(Vi)
+
+    def svdvals(self) -> np.ndarray:
+        """svdvals!(::SkewHermTridiagonal) (tridiag.jl:526-530): descending."""
+        n = self.n
+        S = torch.zeros(n, dtype=torch.float64, device="cuda")
+        info = _info_tensor()
+        h = handle().bind()
+        if self.complex:
+            check(_lib.load().skew_tridiag_svdvals_z(h, _ptr(self.ev), _ptr(self.dvim), n, _ptr(S), _ptr(info)),
+                  "tridiag svdvals")
+        else:
+            check(_lib.load().skew_tridiag_svdvals_d(h, _ptr(self.ev), n, _ptr(S), _ptr(info)), "tridiag svdvals")
+        _info_ok(info, "tridiag svdvals")
+        return S.cpu().numpy()
+
+    def svd(self):
+        """svd!(::SkewHermTridiagonal) (tridiag.jl:534-555): (U, S, Vt), A = U diag(S) Vt."""
+        n = self.n
+        S = torch.zeros(n, dtype=torch.float64, device="cuda")
+        info = _info_tensor()
+        h = handle().bind()
+        if self.complex:
+            U = torch.zeros((n, n), dtype=torch.complex128, device="cuda")
+            V = torch.zeros((n, n), dtype=torch.complex128, device="cuda")
+            check(_lib.load().skew_tridiag_svd_z(h, _ptr(self.ev), _ptr(self.dvim), n, _ptr(S), _ptr(U), _ptr(V), n,
+                                                 _ptr(info)), "tridiag svd")
+            _info_ok(info, "tridiag svd")
+            Uh, Vh = from_device_complex(U), from_device_complex(V)
+        else:
+            planes = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for _ in range(4)]
+            check(_lib.load().skew_tridiag_svd_d(h, _ptr(self.ev), n, _ptr(S), *[_ptr(t) for t in planes], n,
+                                                 _ptr(info)), "tridiag svd")
+            _info_ok(info, "tridiag svd")
+            Ur, Ui, Vr, Vi = (from_device(t) for t in planes)
+            Uh, Vh = Ur + 1j * Ui, Vr + 1j * Vi
+        return Uh, S.cpu().numpy(), Vh.conj().T
 
     def function(self, name: str) -> np.ndarray:
         n = self.n

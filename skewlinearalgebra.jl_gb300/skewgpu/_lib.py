@@ -70,6 +70,14 @@ SIGNATURES = {
     "skew_batch_func_d": (_int, [_vp, _vp, _int, _vp, _vp]),
     "skew_func_z": (_int, [_vp, _vp, _i64, _i64, _int, _vp, _i64, _vp]),
     "skew_batch_func_z": (_int, [_vp, _vp, _i64, _i64, _int, _vp, _vp]),
+    "skew_svdvals_d": (_int, [_vp, _vp, _i64, _i64, _vp, _vp]),
+    "skew_svd_d": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "skew_svdvals_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp]),
+    "skew_svd_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _i64, _vp]),
+    "skew_tridiag_svdvals_d": (_int, [_vp, _vp, _i64, _vp, _vp]),
+    "skew_tridiag_svd_d": (_int, [_vp, _vp, _i64, _vp, _vp, _vp, _vp, _vp, _i64, _vp]),
+    "skew_tridiag_svdvals_z": (_int, [_vp, _vp, _vp, _i64, _vp, _vp]),
+    "skew_tridiag_svd_z": (_int, [_vp, _vp, _vp, _i64, _vp, _vp, _vp, _i64, _vp]),
     "skew_logabspf_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _int, _vp]),
     "skew_pfaffian_z": (_int, [_vp, _vp, _i64, _i64, _vp, _int, _vp]),
     "skew_batch_logabspf_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
