@@ -898,7 +898,8 @@ struct ZLayout {
 static int zlayout(skew_handle_t h, int64_t n, int64_t B, bool copy, bool vecs, bool func, ZLayout* L) {
   // every segment a multiple of 32 doubles: complex arrays stay 16-byte aligned
   auto seg = [](size_t d) { return (d + 31) & ~(size_t)31; };
-  const size_t zr = B == 1 ? seg(zhess_large_ws_doubles((int)n)) : 0;
+  const size_t zr =
+      B == 1 ? seg(std::max(zhess_large_ws_doubles((int)n), zhess_persist_ws_doubles((int)n))) : 0;
   const size_t zw = copy ? seg(2 * (size_t)B * n * n) : 0;
   const size_t ze = seg(zeigen_ws_doubles((int)n, (int)B));
   const size_t zf = func ? seg(zfunc_ws_doubles((int)n, (int)B)) : 0;
@@ -928,10 +929,17 @@ static int zlayout(skew_handle_t h, int64_t n, int64_t B, bool copy, bool vecs, 
   return SKEW_OK;
 }
 
-// complex reduction in place.  One matrix: one CTA for n <= 128, per-column
-// multi-CTA kernels above.  B > 1 matrices of size n, n^2 apart: one CTA each.
+// complex reduction in place.  One matrix: one CTA for n <= 128, the persistent
+// blocked kernel from zpersist_min_n() (SKEW_ZPERSIST_MIN_N), per-column multi-CTA
+// kernels between (and where the persistent kernel cannot run).  B > 1 matrices of
+// size n, n^2 apart: one CTA each.
+static int64_t zpersist_min_n() {
+  const char* v = getenv("SKEW_ZPERSIST_MIN_N");
+  return (v && *v) ? atoll(v) : 384;
+}
+
 static int zreduce(skew_handle_t h, double* A, int64_t n, int64_t lda, int64_t B, double* tau, double* ev,
-                   double* dvim, double* zws) {
+                   double* dvim, double* zws, int* info = nullptr) {
   if (B > 1 || n <= 128) {
     ZHessParams P;
     P.W = nullptr;
@@ -950,6 +958,12 @@ static int zreduce(skew_handle_t h, double* A, int64_t n, int64_t lda, int64_t B
     P.dvim = dvim;
     CK(launch_zhess_cta(P, (int)B, h->stream));
     return SKEW_OK;
+  }
+  if (n >= zpersist_min_n()) {
+    const cudaError_t e = zhess_persistent(A, lda, (int)n, tau, ev, dvim, zws, h->sms, info, h->stream);
+    if (e == cudaSuccess) return SKEW_OK;
+    if (e != cudaErrorNotSupported) return SKEW_CUDA_ERROR;
+    cudaGetLastError();
   }
   CK(zhess_large(A, lda, (int)n, tau, ev, dvim, zws, h->stream));
   return SKEW_OK;
@@ -971,7 +985,7 @@ int skew_hessenberg_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double
   ZLayout L;
   st = zlayout(h, n, 1, false, false, false, &L);
   if (st) return st;
-  return zreduce(h, A, n, lda, 1, n > 1 ? tau : L.tau, n > 1 ? ev : L.ev, dvim ? dvim : L.dvim, L.zws);
+  return zreduce(h, A, n, lda, 1, n > 1 ? tau : L.tau, n > 1 ? ev : L.ev, dvim ? dvim : L.dvim, L.zws, info);
 }
 
 int skew_eigvals_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info) {
@@ -983,7 +997,7 @@ int skew_eigvals_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* v
   ZLayout L;
   st = zlayout(h, n, 1, false, false, false, &L);
   if (st) return st;
-  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws);
+  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws, info);
   if (st) return st;
   CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, vals_im, nullptr, 0, L.ews, 1, h->stream));
   return SKEW_OK;
@@ -999,7 +1013,7 @@ int skew_eigen_z(skew_handle_t h, double* A, int64_t n, int64_t lda, double* val
   ZLayout L;
   st = zlayout(h, n, 1, false, false, false, &L);
   if (st) return st;
-  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws);
+  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws, info);
   if (st) return st;
   CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, vals_im, V, ldv, L.ews, 1, h->stream));
   return SKEW_OK;
@@ -1015,7 +1029,7 @@ static int zfunc(skew_handle_t h, double* A, int64_t n, int64_t lda, const doubl
   ZLayout L;
   st = zlayout(h, n, 1, false, true, true, &L);
   if (st) return st;
-  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws);
+  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws, info);
   if (st) return st;
   CK(zeigen_from_tridiag(A, lda, (int)n, L.tau, L.ev, L.dvim, L.vals, L.V, n, L.ews, 1, h->stream));
   CK(zfunc_from_eigen(mode, func, (int)n, L.vals, L.V, n, C, n, O, ldo, L.fws, 1, info, h->stream));
@@ -1080,7 +1094,7 @@ int skew_eigvals_interval_z(skew_handle_t h, double* A, int64_t n, int64_t lda, 
   ZLayout L;
   st = zlayout(h, n, 1, false, false, false, &L);
   if (st) return st;
-  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws);
+  st = zreduce(h, A, n, lda, 1, L.tau, L.ev, L.dvim, L.zws, info);
   if (st) return st;
   double* dg = L.ews;
   double* off = dg + ((n + 31) & ~(int64_t)31);

@@ -346,6 +346,12 @@ __global__ void zdiag_im_kernel(const zc* __restrict__ A, int64_t lda, int n, do
   if (k < n) dvim[k] = A[k + (int64_t)k * lda].im;
 }
 
+cudaError_t launch_zdiag_im(const double* A, int64_t lda, int n, double* dvim, cudaStream_t st) {
+  if (!dvim || n <= 0) return cudaSuccess;
+  zdiag_im_kernel<<<(n + 255) / 256, 256, 0, st>>>(reinterpret_cast<const zc*>(A), lda, n, dvim);
+  return cudaGetLastError();
+}
+
 constexpr int ZTAIL = 96;  // trailing columns left to the one-CTA kernel
 
 size_t zhess_large_ws_doubles(int n) {

@@ -130,6 +130,14 @@ struct ZHessParams {
 size_t zhess_cta_smem_bytes(int nmax);
 cudaError_t launch_zhess_cta(const ZHessParams& P, int grid, cudaStream_t st);
 size_t zhess_large_ws_doubles(int n);
+// imag(diag(A)) of a reduced matrix into dvim
+cudaError_t launch_zdiag_im(const double* A, int64_t lda, int n, double* dvim, cudaStream_t st);
+// One cooperative launch for all panels of one large matrix (skew_zblocked.cu), then the
+// tail with the one-CTA kernel.  cudaErrorNotSupported where it cannot run (the caller
+// falls back to zhess_large); info <- SKEW_TIMEOUT if a grid barrier gave up.
+size_t zhess_persist_ws_doubles(int n);
+cudaError_t zhess_persistent(double* A, int64_t lda, int n, double* tau, double* ev, double* dvim, double* ws,
+                             int sms, int* info, cudaStream_t st);
 cudaError_t zhess_large(double* A, int64_t lda, int n, double* tau, double* ev, double* dvim, double* ws,
                         cudaStream_t st);
 // complex eigen from `batch` reduced matrices of size n (arrays per matrix: A lda*n,

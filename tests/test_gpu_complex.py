@@ -55,6 +55,28 @@ def test_hessenberg_complex_vs_oracle(skewgpu, oracle, n):
         np.testing.assert_allclose(Q.conj().T @ A @ Q, Hc.H(), atol=1e-13 * scale * n)
 
 
+@pytest.mark.parametrize("n", [131, 160, 257, 300, 520, 777])
+def test_hessenberg_complex_persistent_vs_oracle(skewgpu, oracle, n, monkeypatch):
+    """The blocked persistent reduction (panels of 32 columns, the complex latrd with
+    the alpha correction, rank-64 trailing updates), forced down to n = 131 with
+    SKEW_ZPERSIST_MIN_N; checked like the per-column path."""
+    monkeypatch.setenv("SKEW_ZPERSIST_MIN_N", "130")
+    A = skewh_random(n, 1600 + n)
+    Hc = skewgpu.hessenberg_complex(A)
+    ev = Hc.ev.cpu().numpy()
+    dvim = Hc.dvim.cpu().numpy()
+    tau = Hc.tau.cpu().numpy()
+    F = skewgpu.from_device_complex(Hc.factors)
+    scale = max(1.0, np.abs(A).max())
+    _, tq, eq, dq = oracle.hessenberg_complex(A, quad=False)
+    np.testing.assert_allclose(ev, eq, atol=1e-11 * scale * np.sqrt(n))
+    np.testing.assert_allclose(dvim, dq, atol=1e-11 * scale * np.sqrt(n))
+    np.testing.assert_allclose(tau, tq, atol=1e-10)
+    Q = formq_complex(F, tau)
+    np.testing.assert_allclose(Q.conj().T @ Q, np.eye(n), atol=1e-13 * n)
+    np.testing.assert_allclose(Q.conj().T @ A @ Q, Hc.H(), atol=1e-13 * scale * n)
+
+
 def test_hessenberg_complex_not_skew(skewgpu):
     A = skewh_random(8, 1)
     A[0, 0] += 0.5  # a real diagonal part: not skew-Hermitian
