@@ -174,6 +174,8 @@ def main():
     ap.add_argument("--no-legs", action="store_true", help="skip the eigvals / n=512 / adjoint legs")
     ap.add_argument("--only-legs", action="store_true", help="run only the eigvals / n=512 / adjoint legs")
     ap.add_argument("--leg", default=None, help="with --only-legs: run only this leg (profiling)")
+    ap.add_argument("--complex-n", type=int, default=4096,
+                    help="with --only-legs: size of the single ComplexF64 leg (profiling cases)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -193,7 +195,7 @@ def main():
                 "pfaffian_adjoint_1024x128": lambda: leg_pfaffian_adjoint(peak, max(1, args.steps)),
                 "exp_adjoint_512_mixed": lambda: leg_exp_adjoint(peak, max(1, min(args.steps, 3))),
                 "exp_adjoint_complex_64x256": lambda: leg_complex_exp_adjoint(peak),
-                "complex_n4096": lambda: leg_complex_large(4096, peak),
+                "complex_n4096": lambda: leg_complex_large(args.complex_n, peak),
                 "complex_pfaffian_2048x128": lambda: leg_complex_pfaffian(peak, cpu=not args.no_cpu)}
         out = {k: f() for k, f in legs.items() if args.leg is None or k == args.leg}
         plan.close()

@@ -4,10 +4,10 @@
 // (:158-166), A22 += V W^H - W V^H on the lower triangle, mirrored as -conj.
 //
 // Per panel column c (panel step i, panel start p):
-//   A  v staged in shared memory.  Warps take items from an atomic counter: the 2i
-//      panel dots u1 = W^H v and u2 = V^H v (one warp per dot over all rows), and
+//   A  v staged in shared memory.  Each warp takes a static share of the items: the
+//      2i panel dots u1 = W^H v and u2 = V^H v (one warp per dot over all rows), and
 //      (32-row, column-chunk) tiles of A22 v whose partial sums go to ypart; each
-//      tile also writes its share of v^H (A22 v) to dpart.
+//      warp also writes its share of v^H (A22 v) to dpart.
 //   B  every CTA sums dpart in a fixed order and forms the alpha correction without
 //      a further reduction: with y = A22 v + V u1 - W u2,
 //        v^H y = v^H (A22 v) + u2^H u1 - u1^H u2,   alpha = |tau|^2 conj(v^H y) / 2,
@@ -42,9 +42,11 @@ constexpr int ZP_NW = ZP_NT / 32;
 constexpr int ZBNB = 32;   // panel width
 constexpr int ZUT = 64;    // trailing-update tile edge
 constexpr int ZKC = 8;     // panel columns per shared-memory stage of the update
-constexpr int ZFIN = 64;   // rows per row block in phase B (4 threads per row)
+constexpr int ZTPR = 16;   // threads per row in phase B
+constexpr int ZFIN = ZP_NT / ZTPR;  // rows per row block in phase B
 constexpr int ZTAILP = 128;  // trailing columns left to the one-CTA kernel
 constexpr long long ZP_POLL = 1LL << 24;
+constexpr int ZP_MAXWARPS = 16384;  // dpart slots: grid x 8 warps at most
 
 struct ZRef {
   zc tau, scale;
@@ -62,8 +64,9 @@ __device__ ZRef zp_refl(zc alpha, double xnorm) {
   }
   const double h = hypot(hypot(alpha.re, alpha.im), xnorm);
   const double beta = (alpha.re > 0.0) ? neg(h) : h;
+  const double rb = 1.0 / beta;
   R.beta = beta;
-  R.tau = zc{1.0 - alpha.re / beta, neg(alpha.im / beta)};
+  R.tau = zc{1.0 - alpha.re * rb, neg(alpha.im * rb)};
   R.scale = zinv(zc{alpha.re - beta, alpha.im});
   return R;
 }
@@ -103,6 +106,7 @@ struct ZPersistParams {
   unsigned* sync; // [0] barrier arrivals, [1] work items
   int* err;
   int maxck;
+  int items_per_warp;  // matvec tiles per warp and column (chunk count)
 };
 
 namespace {
@@ -170,7 +174,14 @@ __device__ ZRef zp_refl_from_column(const ZPersistParams& P, int c, double* red)
     qq = block_sum<ZP_NW>(qq, red);
     xn = mx * sqrt(qq);
   }
-  return zp_refl(ldz(col + c + 1), xn);
+  // one thread forms the reflector (a warp-wide FP64 instruction costs the same
+  // with one lane as with 32), the others read it from shared memory
+  __shared__ ZRef s_R;
+  if (threadIdx.x == 0) s_R = zp_refl(ldz(col + c + 1), xn);
+  __syncthreads();
+  const ZRef R = s_R;
+  __syncthreads();
+  return R;
 }
 
 // One 64 x 64 lower tile t of the trailing update A[q:, q:] += V W^H - W V^H,
@@ -282,6 +293,9 @@ __global__ void __launch_bounds__(ZP_NT, 1) zpersist_kernel(ZPersistParams P) {
   __shared__ zc su[2 * ZBNB];
   __shared__ zc sWrow[ZBNB + 1], sArow[ZBNB + 1];
   __shared__ double s_dot[2 * ZP_NW];
+  __shared__ zc s_alpha, s_y1;
+  __shared__ ZRef s_R;
+  __shared__ int s_scal;
   __shared__ unsigned s_item;
   const int n = P.n;
   const int64_t lda = P.lda;
@@ -302,67 +316,66 @@ __global__ void __launch_bounds__(ZP_NT, 1) zpersist_kernel(ZPersistParams P) {
     for (int i = 0; i < nbp; i++) {
       const int c = p + i, m = n - c - 1;
       const bool zero = zzero(R.tau);
-      // ---- A: stage v, then items from the shared counter
+      // ---- A: stage v, then a static share of the items per warp.  Warps are
+      // numbered CTA-minor (consecutive items on different SMs); matvec tile q goes
+      // to warp q mod nwarps, panel dot d to warp nwarps - 1 - d.  Each warp sums its
+      // share of v^H (A22 v) over its tiles in order (deterministic).
       for (int j = c + 1 + tid; j < n; j += ZP_NT)
         vs[j] = zero ? zc{0.0, 0.0} : (j == c + 1 ? zc{1.0, 0.0} : zmul(ldz(A + j + (int64_t)c * lda), R.scale));
       __syncthreads();
       const int nrt = (m + 31) >> 5;
-      int nck = max(1, min((4 * nwarps + nrt - 1) / nrt, (m + 31) >> 5));
+      int nck = max(1, min((P.items_per_warp * nwarps + nrt - 1) / nrt, (m + 31) >> 5));
       nck = min(nck, P.maxck);
       const int chunk = (m + nck - 1) / nck;
       nck = (m + chunk - 1) / chunk;
       const int ndots = 2 * i;
       const int nmv = nrt * nck;
-      const unsigned nitems = (unsigned)(ndots + nmv);
-      for (;;) {
-        unsigned it = 0;
-        if (lane == 0) it = atomicAdd(P.sync + 1, 1u) - item_base;
-        it = __shfl_sync(0xffffffffu, it, 0);
-        if (it >= nitems) break;
-        if ((int)it < ndots) {  // u1_j = W[:, j]^H v, u2_j = V[:, j]^H v over rows c+1..
-          const int d = (int)it;
-          const int j = d < i ? d : d - i;
-          const zc* col = (d < i) ? (P.W + (size_t)j * n) : (A + (int64_t)(p + j) * lda);
-          zc a0{0.0, 0.0}, a1{0.0, 0.0};
-          int r = c + 1 + lane;
-          for (; r + 32 < n; r += 64) {
-            a0 = zfma(zconj(ldz(col + r)), vs[r], a0);
-            a1 = zfma(zconj(ldz(col + r + 32)), vs[r + 32], a1);
+      const int gw = w * gridDim.x + blockIdx.x;
+      if (nwarps - 1 - gw < ndots) {  // u1_j = W[:, j]^H v, u2_j = V[:, j]^H v over rows c+1..
+        const int d = nwarps - 1 - gw;
+        const int j = d < i ? d : d - i;
+        const zc* col = (d < i) ? (P.W + (size_t)j * n) : (A + (int64_t)(p + j) * lda);
+        zc a0{0.0, 0.0}, a1{0.0, 0.0};
+        int r = c + 1 + lane;
+        for (; r + 32 < n; r += 64) {
+          a0 = zfma(zconj(ldz(col + r)), vs[r], a0);
+          a1 = zfma(zconj(ldz(col + r + 32)), vs[r + 32], a1);
+        }
+        if (r < n) a0 = zfma(zconj(ldz(col + r)), vs[r], a0);
+        const double sr = warp_sum(a0.re + a1.re), si = warp_sum(a0.im + a1.im);
+        if (lane == 0) P.u[d < i ? d : ZBNB + j] = zc{sr, si};
+      }
+      zc dl{0.0, 0.0};  // this lane's share of v^H (A22 v)
+      for (int qq = gw; qq < nmv; qq += nwarps) {  // partial y = A22 v over (32 rows, column chunk)
+        const int rt = qq / nck, ck = qq - rt * nck;
+        const int r = c + 1 + rt * 32 + lane;
+        const int cb = c + 1 + ck * chunk, ce = min(n, cb + chunk);
+        if (r < n) {
+          const zc* row = A + r;
+          zc a0{0.0, 0.0}, a1{0.0, 0.0}, a2{0.0, 0.0}, a3{0.0, 0.0};
+          int j = cb;
+          for (; j + 3 < ce; j += 4) {
+            const zc w0 = ldz(row + (int64_t)j * lda), w1 = ldz(row + (int64_t)(j + 1) * lda),
+                     w2 = ldz(row + (int64_t)(j + 2) * lda), w3 = ldz(row + (int64_t)(j + 3) * lda);
+            a0 = zfma(w0, vs[j], a0);
+            a1 = zfma(w1, vs[j + 1], a1);
+            a2 = zfma(w2, vs[j + 2], a2);
+            a3 = zfma(w3, vs[j + 3], a3);
           }
-          if (r < n) a0 = zfma(zconj(ldz(col + r)), vs[r], a0);
-          const double sr = warp_sum(a0.re + a1.re), si = warp_sum(a0.im + a1.im);
-          if (lane == 0) P.u[d < i ? d : ZBNB + j] = zc{sr, si};
-        } else {  // partial y = A22 v over (32 rows, column chunk), and its share of v^H (A22 v)
-          const int qq = (int)it - ndots;
-          const int rt = qq / nck, ck = qq - rt * nck;
-          const int r = c + 1 + rt * 32 + lane;
-          const int cb = c + 1 + ck * chunk, ce = min(n, cb + chunk);
-          zc acc{0.0, 0.0};
-          if (r < n) {
-            const zc* row = A + r;
-            zc a0{0.0, 0.0}, a1{0.0, 0.0}, a2{0.0, 0.0}, a3{0.0, 0.0};
-            int j = cb;
-            for (; j + 3 < ce; j += 4) {
-              const zc w0 = ldz(row + (int64_t)j * lda), w1 = ldz(row + (int64_t)(j + 1) * lda),
-                       w2 = ldz(row + (int64_t)(j + 2) * lda), w3 = ldz(row + (int64_t)(j + 3) * lda);
-              a0 = zfma(w0, vs[j], a0);
-              a1 = zfma(w1, vs[j + 1], a1);
-              a2 = zfma(w2, vs[j + 2], a2);
-              a3 = zfma(w3, vs[j + 3], a3);
-            }
-            for (; j < ce; j++) a0 = zfma(ldz(row + (int64_t)j * lda), vs[j], a0);
-            acc = zadd(zadd(a0, a1), zadd(a2, a3));
-            stz(P.ypart + (size_t)ck * n + r, acc);
-          }
-          const zc dv = (r < n) ? zcmul(vs[r], acc) : zc{0.0, 0.0};  // conj(v_r) y_r
-          const double dr = warp_sum(dv.re), di = warp_sum(dv.im);
-          if (lane == 0) P.dpart[qq] = zc{dr, di};
+          for (; j < ce; j++) a0 = zfma(ldz(row + (int64_t)j * lda), vs[j], a0);
+          const zc acc = zadd(zadd(a0, a1), zadd(a2, a3));
+          stz(P.ypart + (size_t)ck * n + r, acc);
+          dl = zadd(dl, zcmul(vs[r], acc));  // conj(v_r) y_r
         }
       }
-      item_base += nitems + (unsigned)nwarps;  // every warp took exactly one failing ticket
+      {
+        const double dr = warp_sum(dl.re), di = warp_sum(dl.im);
+        if (lane == 0) P.dpart[gw] = zc{dr, di};
+      }
       if (!zp_gsync(P)) return;
 
-      // ---- B: alpha (every CTA, fixed order), then rows
+      // ---- B head: every CTA loads u, sums the warps' shares of v^H (A22 v) in a
+      // fixed order, and warp 0 gathers row c+1 of V, W and y in the same round trip
       const bool last = (i == nbp - 1);
       for (int d = tid; d < 2 * i; d += ZP_NT) {
         const int slot = d < i ? d : ZBNB + d - i;
@@ -370,8 +383,8 @@ __global__ void __launch_bounds__(ZP_NT, 1) zpersist_kernel(ZPersistParams P) {
       }
       {
         double dr = 0.0, di = 0.0;
-        for (int qq = tid; qq < nmv; qq += ZP_NT) {
-          const zc x = ldz(P.dpart + qq);
+        for (int q2 = tid; q2 < nwarps; q2 += ZP_NT) {
+          const zc x = ldz(P.dpart + q2);
           dr += x.re;
           di += x.im;
         }
@@ -382,50 +395,89 @@ __global__ void __launch_bounds__(ZP_NT, 1) zpersist_kernel(ZPersistParams P) {
           s_dot[ZP_NW + w] = di;
         }
       }
-      __syncthreads();
-      // v^H y = v^H (A22 v) + u2^H u1 - u1^H u2;  alpha = |tau|^2 conj(v^H y) / 2
-      zc vhy{0.0, 0.0};
-      for (int k = 0; k < ZP_NW; k++) {
-        vhy.re += s_dot[k];
-        vhy.im += s_dot[ZP_NW + k];
-      }
-      for (int j = 0; j < i; j++) {
-        const zc u1 = su[j], u2 = su[ZBNB + j];
-        vhy = zadd(vhy, zsub(zcmul(u2, u1), zcmul(u1, u2)));
-      }
-      const double t2 = R.tau.re * R.tau.re + R.tau.im * R.tau.im;
-      const zc alpha = zc{0.5 * t2 * vhy.re, -0.5 * t2 * vhy.im};
-      if (w == 0) {  // row c+1 of W and of V, needed by every row below
+      if (w == 0) {
         const int r0 = c + 1;
-        zc acc{0.0, 0.0};
-        for (int j = lane; j < i; j += 32)
-          acc = zsub(zfma(ldz(A + r0 + (int64_t)(p + j) * lda), su[j], acc), zmul(ldz(P.W + (size_t)j * n + r0), su[ZBNB + j]));
-        for (int q2 = lane; q2 < nck; q2 += 32) acc = zadd(acc, ldz(P.ypart + (size_t)q2 * n + r0));
-        acc.re = warp_sum(acc.re);
-        acc.im = warp_sum(acc.im);
-        if (lane == 0) sWrow[i] = zfma(alpha, vs[r0], zmul(R.tau, acc));
         for (int j = lane; j < i; j += 32) {
           sWrow[j] = ldz(P.W + (size_t)j * n + r0);
           sArow[j] = ldz(A + r0 + (int64_t)(p + j) * lda);
         }
-        if (lane == 0) sArow[i] = vs[r0];
+        zc y1{0.0, 0.0};
+        for (int q2 = lane; q2 < nck; q2 += 32) y1 = zadd(y1, ldz(P.ypart + (size_t)q2 * n + r0));
+        y1.re = warp_sum(y1.re);
+        y1.im = warp_sum(y1.im);
+        if (lane == 0) s_y1 = y1;
       }
       __syncthreads();
+      if (w == 0) {
+        // v^H y = v^H (A22 v) + u2^H u1 - u1^H u2;  alpha = |tau|^2 conj(v^H y) / 2;
+        // y_{c+1} = (A22 v)_{c+1} + sum_j (V[c+1, j] u1_j - W[c+1, j] u2_j)
+        double hr = 0.0, hi = 0.0, er = 0.0, ei = 0.0;
+        for (int j = lane; j < i; j += 32) {
+          const zc u1 = su[j], u2 = su[ZBNB + j];
+          const zc d = zsub(zcmul(u2, u1), zcmul(u1, u2));
+          hr += d.re;
+          hi += d.im;
+          const zc e = zsub(zmul(sArow[j], u1), zmul(sWrow[j], u2));
+          er += e.re;
+          ei += e.im;
+        }
+        hr = warp_sum(hr);
+        hi = warp_sum(hi);
+        er = warp_sum(er);
+        ei = warp_sum(ei);
+        if (lane == 0) {
+          for (int k = 0; k < ZP_NW; k++) {
+            hr += s_dot[k];
+            hi += s_dot[ZP_NW + k];
+          }
+          const double t2 = R.tau.re * R.tau.re + R.tau.im * R.tau.im;
+          const zc alpha = zc{0.5 * t2 * hr, -0.5 * t2 * hi};
+          s_alpha = alpha;
+          const zc y1 = zadd(s_y1, zc{er, ei});
+          sWrow[i] = zfma(alpha, vs[c + 1], zmul(R.tau, y1));
+          sArow[i] = vs[c + 1];
+        }
+      }
+      __syncthreads();
+      const zc alpha = s_alpha;
       const int nfb = (m + ZFIN - 1) / ZFIN;
       for (int fb = blockIdx.x; fb < nfb; fb += gridDim.x) {
-        const int row = c + 1 + fb * ZFIN + (tid >> 2);
-        const int g = tid & 3;
+        const int row = c + 1 + fb * ZFIN + tid / ZTPR;
+        const int g = tid % ZTPR;
         const bool valid = row < n;
+        // this thread's panel terms j = g + ZTPR t: loaded once, used for y and for
+        // the deferred update of column c+1
+        constexpr int NJ = ZBNB / ZTPR;
+        zc aj[NJ], wj[NJ];
+#pragma unroll
+        for (int t = 0; t < NJ; t++) {
+          const int j = g + ZTPR * t;
+          aj[t] = zc{0.0, 0.0};
+          wj[t] = zc{0.0, 0.0};
+          if (valid && j < i) {
+            aj[t] = ldz(A + row + (int64_t)(p + j) * lda);
+            wj[t] = ldz(P.W + (size_t)j * n + row);
+          }
+        }
         zc vr{0.0, 0.0}, acc{0.0, 0.0};
         if (valid) {
           vr = vs[row];
-          for (int j = g; j < i; j += 4)
-            acc = zsub(zfma(ldz(A + row + (int64_t)(p + j) * lda), su[j], acc),
-                       zmul(ldz(P.W + (size_t)j * n + row), su[ZBNB + j]));
-          for (int q2 = g; q2 < nck; q2 += 4) acc = zadd(acc, ldz(P.ypart + (size_t)q2 * n + row));
+          zc y0{0.0, 0.0}, y1{0.0, 0.0};
+          int q2 = g;
+          for (; q2 + ZTPR < nck; q2 += 2 * ZTPR) {
+            y0 = zadd(y0, ldz(P.ypart + (size_t)q2 * n + row));
+            y1 = zadd(y1, ldz(P.ypart + (size_t)(q2 + ZTPR) * n + row));
+          }
+          if (q2 < nck) y0 = zadd(y0, ldz(P.ypart + (size_t)q2 * n + row));
+          acc = zadd(y0, y1);
+#pragma unroll
+          for (int t = 0; t < NJ; t++) {
+            const int j = g + ZTPR * t;
+            if (j < i) acc = zsub(zfma(aj[t], su[j], acc), zmul(wj[t], su[ZBNB + j]));
+          }
         }
 #pragma unroll
-        for (int o = 1; o <= 2; o <<= 1) {
+        for (int o = 1; o < ZTPR; o <<= 1) {
           acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
           acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
         }
@@ -440,14 +492,16 @@ __global__ void __launch_bounds__(ZP_NT, 1) zpersist_kernel(ZPersistParams P) {
         double ssp = 0.0;
         zc uu{0.0, 0.0};
         const bool doupd = valid && !last;
-        if (doupd)
-          for (int j = g; j <= i; j += 4) {
-            const zc arj = (j == i) ? vr : ldz(A + row + (int64_t)(p + j) * lda);
-            const zc wrj = (j == i) ? wri : ldz(P.W + (size_t)j * n + row);
-            uu = zsub(zadd(uu, zmulc(arj, sWrow[j])), zmulc(wrj, sArow[j]));
-          }
+        if (doupd) {
 #pragma unroll
-        for (int o = 1; o <= 2; o <<= 1) {
+          for (int t = 0; t < NJ; t++) {
+            const int j = g + ZTPR * t;
+            if (j < i) uu = zsub(zadd(uu, zmulc(aj[t], sWrow[j])), zmulc(wj[t], sArow[j]));
+          }
+          if (i % ZTPR == g) uu = zsub(zadd(uu, zmulc(vr, sWrow[i])), zmulc(wri, sArow[i]));
+        }
+#pragma unroll
+        for (int o = 1; o < ZTPR; o <<= 1) {
           uu.re += __shfl_xor_sync(0xffffffffu, uu.re, o);
           uu.im += __shfl_xor_sync(0xffffffffu, uu.im, o);
         }
@@ -466,21 +520,23 @@ __global__ void __launch_bounds__(ZP_NT, 1) zpersist_kernel(ZPersistParams P) {
         if (tid == 0) P.sspart[fb] = sb;
       }
       if (!zp_gsync(P)) return;
-      if (!last) {  // reflector c+1, identically in every CTA
+      if (!last) {  // reflector c+1, identically in every CTA (one thread forms it)
         const int c1 = c + 1;
         if (w == 0) {
           double ss = 0.0;
           for (int t = lane; t < nfb; t += 32) ss += __ldcg(P.sspart + t);
           ss = warp_sum(ss);
-          if (lane == 0) red[0] = ss;
+          if (lane == 0) {
+            s_scal = ss_needs_scaling(ss) ? 1 : 0;
+            if (!s_scal) s_R = zp_refl(ldz(A + (c1 + 1) + (int64_t)c1 * lda), sqrt(ss));
+          }
         }
         __syncthreads();
-        const double ss = red[0];
-        __syncthreads();
-        if (ss_needs_scaling(ss))
+        if (s_scal)
           R = zp_refl_from_column(P, c1, red);
         else
-          R = zp_refl(ldz(A + (c1 + 1) + (int64_t)c1 * lda), sqrt(ss));
+          R = s_R;
+        __syncthreads();
         if (lead) {
           P.ev[c1] = R.beta;
           P.tau[c1] = R.tau;
@@ -520,10 +576,9 @@ static int zp_maxck(int n) { return std::max(1, (n + 31) / 32); }
 size_t zhess_persist_ws_doubles(int n) {
   const size_t nn = (size_t)n;
   const size_t maxck = (size_t)zp_maxck(n);
-  const size_t nrt = (nn + 31) / 32 + 1;
   return 2 * nn * ZBNB      // W
          + 2 * maxck * nn   // ypart
-         + 2 * nrt * maxck  // dpart
+         + 2 * ZP_MAXWARPS  // dpart (one per warp)
          + 2 * 2 * ZBNB     // u
          + (nn + ZFIN - 1) / ZFIN + 1  // sspart
          + 8;               // sync words, error flag
@@ -557,6 +612,7 @@ cudaError_t zhess_persistent(double* Ad, int64_t lda, int n, double* taud, doubl
     const char* g = getenv("SKEW_ZPERSIST_CTAS");
     if (g && *g) grid = std::max(1, std::min(sms * occ, atoi(g)));
   }
+  grid = std::min(grid, ZP_MAXWARPS / ZP_NW);
   zc* A = reinterpret_cast<zc*>(Ad);
   zc* tau = reinterpret_cast<zc*>(taud);
   ZPersistParams P;
@@ -566,14 +622,14 @@ cudaError_t zhess_persistent(double* Ad, int64_t lda, int n, double* taud, doubl
   P.pend = n - 1 - ZTAILP;
   P.tau = tau;
   P.ev = ev;
-  const size_t nn = (size_t)n, maxck = (size_t)zp_maxck(n), nrt = (nn + 31) / 32 + 1;
+  const size_t nn = (size_t)n, maxck = (size_t)zp_maxck(n);
   double* wp = wsd;
   P.W = reinterpret_cast<zc*>(wp);
   wp += 2 * nn * ZBNB;
   P.ypart = reinterpret_cast<zc*>(wp);
   wp += 2 * maxck * nn;
   P.dpart = reinterpret_cast<zc*>(wp);
-  wp += 2 * nrt * maxck;
+  wp += 2 * ZP_MAXWARPS;
   P.u = reinterpret_cast<zc*>(wp);
   wp += 2 * 2 * ZBNB;
   P.sspart = wp;
@@ -581,6 +637,11 @@ cudaError_t zhess_persistent(double* Ad, int64_t lda, int n, double* taud, doubl
   P.sync = reinterpret_cast<unsigned*>(wp);  // 2 words
   P.err = reinterpret_cast<int*>(wp + 1);
   P.maxck = (int)maxck;
+  P.items_per_warp = 4;
+  {
+    const char* v = getenv("SKEW_ZPERSIST_ITEMS");  // sweeps: 1..8
+    if (v && *v) P.items_per_warp = std::max(1, std::min(8, atoi(v)));
+  }
   e = cudaMemsetAsync(wp, 0, 2 * sizeof(double), st);
   if (e != cudaSuccess) return e;
   void* args[] = {&P};
