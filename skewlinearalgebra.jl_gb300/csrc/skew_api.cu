@@ -379,7 +379,12 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
     B.end = (int)u;
     B.nmax = std::max<int32_t>(P->n_host[order[t]], 1);
     const size_t smem_full = batch_smem_bytes(B.nmax, true);
-    B.smem_matrix = (smem_full <= 227 * 1024 && B.nmax <= env_int("SKEW_BATCH_SMEM_NMAX", 152)) ? 1 : 0;
+    // Working copies in shared memory up to n = 96 (several CTAs per SM).  Above that a
+    // copy takes most of an SM's shared memory, one CTA per SM stalls at every step's
+    // barriers, and two CTAs per SM on L2-resident global copies are faster (measured
+    // on GB300: 1024 x n = 128 with gradient 12.8 ms against 15.3 ms; the mixed
+    // 16..256 workload +1.5 %).  SKEW_BATCH_SMEM_NMAX overrides (sweeps).
+    B.smem_matrix = (smem_full <= 227 * 1024 && B.nmax <= env_int("SKEW_BATCH_SMEM_NMAX", 96)) ? 1 : 0;
     int occ = batch_occupancy(B.nmax, B.smem_matrix != 0);
     if (!B.smem_matrix) occ = std::max(1, std::min(occ, env_int("SKEW_BATCH_GLOBAL_CTAS_PER_SM", 2)));
     B.grid = (int)std::min<int64_t>((int64_t)h->sms * occ, u - t);
