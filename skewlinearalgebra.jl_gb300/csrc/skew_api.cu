@@ -82,6 +82,17 @@ struct skew_batch_plan_st {
   };
   GraphSlot graphs[6];
   bool graphs_off = false;              // capture failed once (or disabled): launch directly
+  // function paths (exp, cis, the exp adjoint, matrix functions): matrices with
+  // n > fv_thresh take bisection and twisted vectors instead of the QR chain,
+  // by size group; built once per plan and threshold (outside any capture)
+  struct FvGroup {
+    int n, start, count, chunk;
+  };
+  int fv_thresh = -1;
+  std::vector<FvGroup> fv_groups;
+  int32_t* fv_idx = nullptr;  // matrix indices, grouped by size
+  double* fv_ws = nullptr;    // e_g | bp_g | vals_g | vector workspace of one chunk
+  size_t fv_ws_doubles = 0;
   cudaStream_t capture_stream = nullptr;  // graphs are recorded here, launched on the caller's stream
 };
 
@@ -441,6 +452,8 @@ int skew_batch_plan_destroy(skew_batch_plan_t P) {
                  P->e_p_vals, P->e_p_scratch, P->e_p_work, P->e_status, P->e_counter};
   for (void* q : eig)
     if (q) cudaFreeAsync(q, st);
+  if (P->fv_idx) cudaFreeAsync(P->fv_idx, st);
+  if (P->fv_ws) cudaFreeAsync(P->fv_ws, st);
   cudaStreamSynchronize(st);
   delete P;
   return SKEW_OK;
@@ -675,8 +688,78 @@ static int eigen_ws(skew_batch_plan_t P) {
 // A != null: dense matrices (reduction, QR of skewtrieigen_divided!, vectors,
 // back-transformation).  ev_in != null instead: the subdiagonals of
 // SkewHermTridiagonal matrices (skewtrieigen_merged!, no reduction, Q = I).
+// Above this size the batched function paths take bisection and twisted vectors
+// (SKEW_FUNC_CHAIN_NMAX overrides; the eigenvalue order does not matter there).
+// The QR chain runs one matrix per thread, O(n^2) with a long dependency chain:
+// for n = 512 it takes 0.30 s on GB300, where bisection and twisted vectors take
+// a few milliseconds.
+static int func_chain_nmax() { return env_int("SKEW_FUNC_CHAIN_NMAX", 160); }
+
+// Size groups of the matrices above thr, their device index list and the workspace
+// of one chunk (problems per chunk bounded so one chunk's workspace stays within
+// 64 M doubles).
+static int fv_setup(skew_batch_plan_t P, int thr) {
+  if (P->fv_thresh == thr) return SKEW_OK;
+  cudaStream_t st = P->h->stream;
+  if (P->fv_idx) CK(cudaFreeAsync(P->fv_idx, st));
+  if (P->fv_ws) CK(cudaFreeAsync(P->fv_ws, st));
+  P->fv_idx = nullptr;
+  P->fv_ws = nullptr;
+  P->fv_groups.clear();
+  P->fv_ws_doubles = 0;
+  std::vector<int32_t> idx;
+  std::vector<int32_t> bysize(P->count);
+  std::iota(bysize.begin(), bysize.end(), 0);
+  std::stable_sort(bysize.begin(), bysize.end(), [&](int32_t a, int32_t b) { return P->n_host[a] > P->n_host[b]; });
+  for (size_t t = 0; t < bysize.size();) {
+    const int n = P->n_host[bysize[t]];
+    size_t u = t;
+    while (u < bysize.size() && P->n_host[bysize[u]] == n) u++;
+    if (n > thr && n >= 3) {
+      skew_batch_plan_st::FvGroup g;
+      g.n = n;
+      g.start = (int)idx.size();
+      g.count = (int)(u - t);
+      const size_t per = skew_vectors_batch_ws_doubles(n) + 2 * (size_t)n + 8;
+      g.chunk = (int)std::max<size_t>(1, std::min<size_t>((size_t)g.count, (64u << 20) / per));
+      P->fv_ws_doubles = std::max(P->fv_ws_doubles, per * (size_t)g.chunk);
+      for (size_t q = t; q < u; q++) idx.push_back(bysize[q]);
+      P->fv_groups.push_back(g);
+    }
+    t = u;
+  }
+  if (!idx.empty()) {
+    CK(cudaMallocAsync(&P->fv_idx, sizeof(int32_t) * idx.size(), st));
+    CK(cudaMemcpyAsync(P->fv_idx, idx.data(), sizeof(int32_t) * idx.size(), cudaMemcpyHostToDevice, st));
+    CK(cudaMallocAsync(&P->fv_ws, sizeof(double) * P->fv_ws_doubles, st));
+    CK(cudaStreamSynchronize(st));  // idx goes out of scope
+  }
+  P->fv_thresh = thr;
+  return SKEW_OK;
+}
+
+// Bisection and twisted vectors for the groups above the chain threshold.
+static int fv_issue(skew_batch_plan_t P, const EigenBatch& E) {
+  cudaStream_t st = P->h->stream;
+  for (const auto& g : P->fv_groups) {
+    for (int c0 = 0; c0 < g.count; c0 += g.chunk) {
+      const int G = std::min(g.chunk, g.count - c0);
+      const int32_t* ix = P->fv_idx + g.start + c0;
+      double* e_g = P->fv_ws;
+      double* vals_g = e_g + (size_t)G * g.n;
+      double* bp_g = vals_g + (size_t)G * g.n;
+      double* ws = bp_g + (size_t)G * 8;
+      CK(launch_gather_ev(P->d_ev, P->d_ev_off, ix, g.n, G, e_g, st));
+      CK(launch_tridiag_bisect_batch(e_g, g.n, G, bp_g, vals_g, E.vals, ix, st));
+      CK(skew_vectors_batch(e_g, g.n, G, vals_g, bp_g, E.Vr, E.Vi, ix, ws, st));
+    }
+  }
+  return SKEW_OK;
+}
+
 static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const* vals, double* const* Vr,
-                     double* const* Vi, EigenBatch* Eout, const double* const* ev_in = nullptr) {
+                     double* const* Vi, EigenBatch* Eout, const double* const* ev_in = nullptr,
+                     int chain_nmax = 1 << 30) {
   int s = eigen_ws(P);
   if (s) return s;
   cudaStream_t st = P->h->stream;
@@ -712,9 +795,14 @@ static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const*
   E.pwork = P->e_p_work;
   E.func = SKEW_FUNC_EXP;
   E.merged = ev_in ? 1 : 0;
+  E.chain_nmax = (ev_in || chain_nmax >= P->nmax) ? (1 << 30) : chain_nmax;
   const int grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
   CK(launch_eigen_chain(E, st));
   CK(launch_eigen_vectors(E, grid, st));
+  if (E.chain_nmax < P->nmax) {
+    s = fv_issue(P, E);
+    if (s) return s;
+  }
   if (!ev_in) CK(launch_eigen_back(E, grid, P->nmax, st));
   *Eout = E;
   return SKEW_OK;
@@ -749,6 +837,8 @@ static int func_run_graph(skew_batch_plan_t P, const double* const* A, double* c
                           const double* const* cot, int mode, int func, int* status) {
   int s = eigen_ws(P);
   if (s) return s;
+  s = fv_setup(P, func_chain_nmax());
+  if (s) return s;
   const GraphOp op = mode == 0 ? G_EXP : (mode == 1 ? G_CIS : G_EXPVJP);
   return graph_issue(P, op, {A, out, cot, status, reinterpret_cast<const void*>((intptr_t)func), nullptr},
                      [&] { return func_issue(P, A, out, cot, mode, func, status); });
@@ -762,7 +852,9 @@ static int func_run(skew_batch_plan_t P, const double* const* A, double* const* 
 static int func_issue(skew_batch_plan_t P, const double* const* A, double* const* out, const double* const* cot,
                       int mode, int func, int* status) {
   EigenBatch E;
-  int s = eigen_run(P, A, nullptr, nullptr, nullptr, &E);
+  int s = fv_setup(P, func_chain_nmax());
+  if (s) return s;
+  s = eigen_run(P, A, nullptr, nullptr, nullptr, &E, nullptr, func_chain_nmax());
   if (s) return s;
   E.out = out;
   E.cot = cot;

@@ -136,6 +136,10 @@ __global__ void eigen_chain_kernel(EigenBatch E) {
   if (t >= E.count) return;
   const int b = E.order[t];
   const int N = E.n[b];
+  if (N > E.chain_nmax) {  // eigenpairs from bisection and twisted vectors instead
+    E.status[b] = SKEW_OK;
+    return;
+  }
   double* ev = E.ev + E.off_n[b];
   double* evb = E.evb + E.off_n[b];
   double* G = E.G + E.off_n[b];
@@ -363,6 +367,7 @@ __global__ void __launch_bounds__(ENT) eigen_vectors_kernel(EigenBatch E) {
     if (t >= E.count) break;
     const int b = E.order[t];
     const int N = E.n[b];
+    if (N > E.chain_nmax) continue;  // vectors from the twisted path
     double* Vr = E.Vr[b];
     double* Vi = E.Vi[b];
     const int64_t ldv = E.n[b];
@@ -826,6 +831,21 @@ cudaError_t launch_copy_ev(const double* const* ev_in, const int32_t* n, const i
 
 size_t eigen_work_doubles(int n) {
   return (size_t)std::max<int64_t>(4 * (int64_t)n * n, fallback_ws_doubles(n));
+}
+
+__global__ void gather_ev_kernel(const double* __restrict__ ev, const int64_t* __restrict__ off_n,
+                                 const int32_t* __restrict__ idx, int n, double* __restrict__ e_g) {
+  const int mb = blockIdx.y;
+  const double* src = ev + off_n[idx[mb]];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    e_g[(size_t)mb * n + i] = (i + 1 < n) ? src[i] : 0.0;
+}
+
+cudaError_t launch_gather_ev(const double* ev, const int64_t* off_n, const int32_t* idx, int n, int G, double* e_g,
+                             cudaStream_t st) {
+  if (n <= 0 || G <= 0) return cudaSuccess;
+  gather_ev_kernel<<<dim3((n + 255) / 256, G), 256, 0, st>>>(ev, off_n, idx, n, e_g);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_eigen_chain(const EigenBatch& E, cudaStream_t st) {

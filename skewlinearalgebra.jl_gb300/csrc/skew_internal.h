@@ -194,7 +194,23 @@ struct EigenBatch {
   double* const* pwork;      // [count] work + off_w (pointer array for the tiled products)
   int func;                  // skew_func_t of mode 0 (exp and the other matrix functions)
   int merged;                // 1: skewtrieigen_merged! (tridiagonal input; no mem deflation of :355)
+  int chain_nmax;            // matrices with n > chain_nmax skip the QR chain and its vectors
+                             // (their eigenpairs come from bisection and twisted vectors)
 };
+// Eigenpairs of G skew tridiagonals of one size n (subdiagonals e_g, n apart) by
+// bisection (values descending, exact +-pairs, also into vals_out[idx[mb]]) and
+// twisted-factorisation vectors with the banded orthogonal correction, written in
+// the tridiagonal basis to Vr[idx[mb]], Vi[idx[mb]] (n x n, leading dimension n).
+// ws: G x skew_vectors_batch_ws_doubles(n); bp_g: 8 G; vals_g: n G.
+cudaError_t launch_tridiag_bisect_batch(const double* e_g, int n, int G, double* bp_g, double* vals_g,
+                                        double* const* vals_out, const int32_t* idx, cudaStream_t st);
+size_t skew_vectors_batch_ws_doubles(int n);
+cudaError_t skew_vectors_batch(const double* e_g, int n, int G, const double* vals_g, const double* bp_g,
+                               double* const* Vr, double* const* Vi, const int32_t* idx, double* ws,
+                               cudaStream_t st);
+// e_g[mb n + i] = ev[off_n[idx[mb]] + i] (i < n - 1), 0 at i = n - 1
+cudaError_t launch_gather_ev(const double* ev, const int64_t* off_n, const int32_t* idx, int n, int G, double* e_g,
+                             cudaStream_t st);
 // copies n[b] - 1 subdiagonal entries from ev_in[b] to ev + off[b] for every matrix
 cudaError_t launch_copy_ev(const double* const* ev_in, const int32_t* n, const int64_t* off, int count, double* ev,
                            cudaStream_t st);

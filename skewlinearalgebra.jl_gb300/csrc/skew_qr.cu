@@ -317,6 +317,84 @@ cudaError_t launch_tridiag_bisect(const double* ev, int n, double* vals_im, doub
   return cudaGetLastError();
 }
 
+// The same for G problems of one size n (subdiagonals e_g, n apart): per problem the
+// bounds {bound, pivmin} into bp_g (8 apart) and the values (descending, exact
+// +-pairs) into vals_g (n apart) and into vals_out[idx[mb]].
+__global__ void bisect_prep_batch_kernel(const double* __restrict__ e_g, int n, double* __restrict__ bp_g) {
+  __shared__ double red[2][32];
+  const double* e = e_g + (size_t)blockIdx.x * n;
+  double bound = 0.0, emax2 = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    const double l = (i > 0 ? fabs(e[i - 1]) : 0.0), r = (i + 1 < n ? fabs(e[i]) : 0.0);
+    bound = fmax(bound, l + r);
+    if (i + 1 < n) emax2 = fmax(emax2, e[i] * e[i]);
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    bound = fmax(bound, __shfl_xor_sync(0xffffffffu, bound, o));
+    emax2 = fmax(emax2, __shfl_xor_sync(0xffffffffu, emax2, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    red[0][threadIdx.x >> 5] = bound;
+    red[1][threadIdx.x >> 5] = emax2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double b = 0.0, m = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+      b = fmax(b, red[0][w]);
+      m = fmax(m, red[1][w]);
+    }
+    double* bp = bp_g + (size_t)blockIdx.x * 8;
+    bp[0] = b * (1.0 + 1e-14) + 1e-300;
+    bp[1] = 2.2250738585072014e-308 * fmax(1.0, m);
+  }
+}
+
+__global__ void bisect_batch_kernel(const double* __restrict__ e_g, int n, const double* __restrict__ bp_g,
+                                    double* __restrict__ vals_g, double* const* __restrict__ vals_out,
+                                    const int32_t* __restrict__ idx, int p) {
+  const int mb = blockIdx.y;
+  const double* e = e_g + (size_t)mb * n;
+  const double* bp = bp_g + (size_t)mb * 8;
+  double* vals = vals_g + (size_t)mb * n;
+  double* out = vals_out[idx[mb]];
+  const int h = n / 2;
+  const int gid = (blockIdx.x * blockDim.x + threadIdx.x) / p;
+  const int gl = (threadIdx.x & 31) % p;
+  if ((n & 1) && gid == 0 && gl == 0 && blockIdx.x == 0) {
+    vals[h] = 0.0;
+    out[h] = 0.0;
+  }
+  const double bound = bp[0], pivmin = bp[1];
+  const bool active = gid < h;
+  const double x = group_multisect(0.0, bound, n - 1 - (active ? gid : 0), 4.0 * pivmin, p, active,
+                                   [&](double y) { return sturm_count(e, n, y, pivmin); });
+  if (active && gl == 0) {
+    vals[gid] = x;
+    vals[n - 1 - gid] = neg(x);
+    out[gid] = x;
+    out[n - 1 - gid] = neg(x);
+  }
+}
+
+cudaError_t launch_tridiag_bisect_batch(const double* e_g, int n, int G, double* bp_g, double* vals_g,
+                                        double* const* vals_out, const int32_t* idx, cudaStream_t st) {
+  if (n <= 0 || G <= 0) return cudaSuccess;
+  bisect_prep_batch_kernel<<<G, 256, 0, st>>>(e_g, n, bp_g);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 148;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int h = n / 2;
+  // lanes per eigenvalue: the whole batch shares the machine
+  const int p = multisect_lanes(std::max(1, h * G), sms);
+  const long long threads = ((long long)std::max(h, 1) * p + 31) / 32 * 32;
+  const int bs = 128;
+  bisect_batch_kernel<<<dim3((unsigned)((threads + bs - 1) / bs), G), bs, 0, st>>>(e_g, n, bp_g, vals_g, vals_out,
+                                                                                   idx, p);
+  return cudaGetLastError();
+}
+
 // Selected eigenvalues of a symmetric tridiagonal (diagonal dg or zero, off-diagonal
 // e): the ascending eigenvalues lambda_{i0 .. i0+m-1} with
 //   irange (il, iu, 1-based):  i0 = il - 1, m = iu - il + 1;

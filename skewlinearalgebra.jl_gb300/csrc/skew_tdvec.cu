@@ -598,6 +598,85 @@ static size_t strip_smem_bytes() {
   return sizeof(double) * ((size_t)WB * (WB + 1) + (size_t)WB * (SW + 1) + (size_t)RC * (WB + 1) + (size_t)RC * (SW + 1));
 }
 
+// Batched skew-mode write and mirror for G problems of one size (per-problem output
+// pointers Vr[idx[mb]], Vi[idx[mb]], leading dimension n): the same as
+// tdvec_write_skew_kernel and mirror_kernel.
+__global__ void __launch_bounds__(LA_NT) tdvec_write_skew_batch_kernel(TdvecLayout L0, const double* X0,
+                                                                       double* const* Vr_all, double* const* Vi_all,
+                                                                       const int32_t* idx) {
+  __shared__ double out[RC][33];
+  const int mb = blockIdx.z;
+  const TdvecLayout L = at_problem(L0, mb);
+  const double* X = X0 + (size_t)mb * L0.mstride;
+  double* Vr = Vr_all[idx[mb]];
+  double* Vi = Vi_all[idx[mb]];
+  const int k0 = blockIdx.x * 32, i0 = blockIdx.y * RC;
+  const int n = L.n;
+  const int64_t ldv = n;
+  const int64_t KP = L.KP;
+  for (int q = threadIdx.x; q < RC * 32; q += LA_NT) {
+    const int kk = q % 32, rr = q / 32;
+    const int i = i0 + rr, k = k0 + kk;
+    double o = 0.0;
+    if (i < n && k < L.K) {
+      o = X[(int64_t)i * KP + k];
+      if (k < L.h) o *= 0.7071067811865476;
+      if ((i >> 1) & 1) o = neg(o);
+    }
+    out[rr][kk] = o;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < RC * 32; q += LA_NT) {
+    const int kk = q / RC, rr = q - kk * RC;
+    const int i = i0 + rr, k = k0 + kk;
+    if (i >= n || k >= L.K) continue;
+    const int col = (k < L.h) ? n - 1 - k : L.h;
+    const double o = out[rr][kk];
+    if ((i & 1) == 0) {
+      Vr[i + (int64_t)col * ldv] = o;
+      Vi[i + (int64_t)col * ldv] = 0.0;
+    } else {
+      Vr[i + (int64_t)col * ldv] = 0.0;
+      Vi[i + (int64_t)col * ldv] = (k < L.h) ? o : 0.0;
+    }
+  }
+}
+
+__global__ void mirror_batch_kernel(double* const* Vr_all, double* const* Vi_all, const int32_t* idx, int n) {
+  double* Vr = Vr_all[idx[blockIdx.z]];
+  double* Vi = Vi_all[idx[blockIdx.z]];
+  const int h = n / 2;
+  const int k = blockIdx.y;
+  const int64_t ldv = n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (k < h) {
+      const int64_t src = i + (int64_t)(n - 1 - k) * ldv, dst = i + (int64_t)k * ldv;
+      Vr[dst] = Vr[src];
+      Vi[dst] = neg(Vi[src]);
+    } else {
+      Vi[i + (int64_t)h * ldv] = 0.0;  // k == h only launched for odd n
+    }
+  }
+}
+
+size_t skew_vectors_batch_ws_doubles(int n) { return large_eigen_ws_doubles(n); }
+
+cudaError_t skew_vectors_batch(const double* e_g, int n, int G, const double* vals_g, const double* bp_g,
+                               double* const* Vr, double* const* Vi, const int32_t* idx, double* ws,
+                               cudaStream_t st) {
+  if (n < 3 || G <= 0) return cudaErrorInvalidValue;
+  const TdvecLayout L = layout(n, ws);
+  twisted_kernel<<<dim3(L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), 1, G), TW_NT, 0, st>>>(e_g, vals_g, bp_g, L);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  double* X = tdvec_orthogonalize(L, G, st);
+  tdvec_write_skew_batch_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC, G), LA_NT, 0, st>>>(L, X, Vr, Vi, idx);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  mirror_batch_kernel<<<dim3((n + 255) / 256, L.h + (n & 1), G), 256, 0, st>>>(Vr, Vi, idx, n);
+  return cudaGetLastError();
+}
+
 cudaError_t large_eigen_vectors(const double* A, int64_t lda, int n, const double* tau, const double* ev,
                                 const double* vals, const double* bp, double* Vr, double* Vi, int64_t ldv, double* ws,
                                 cudaStream_t st) {

@@ -169,3 +169,47 @@ def test_eigen_stagnation_fallback(skewgpu, oracle):
         np.testing.assert_allclose(V.conj().T @ V, np.eye(ns[b]), atol=1e-11)
         np.testing.assert_allclose(V @ np.diag(1j * v) @ V.conj().T, M, atol=1e-11 * rho)
     plan.close()
+
+
+def test_batch_exp_vjp_twisted_path(skewgpu, oracle, monkeypatch):
+    """Above n = 160 the batched function paths take bisection and twisted vectors
+    instead of the QR chain (the order of the eigenpairs does not matter there).
+    Odd and even sizes, repeated sizes (groups of several problems): exp against the
+    oracle, the adjoint against the oracle's binary128 block exponential for one
+    matrix and against the QR-chain path (SKEW_FUNC_CHAIN_NMAX) for all."""
+    import torch
+
+    sizes = [161, 200, 200, 257, 301, 64]
+    rng = np.random.default_rng(91)
+    mats = []
+    for k, n in enumerate(sizes):
+        A = skew_random(n, 7000 + k, scale=1.0)
+        rho = np.abs(np.linalg.eigvals(A)).max()
+        mats.append(A * (rng.uniform(0.5, 8.0) / rho))
+    cots = [rng.standard_normal((n, n)) for n in sizes]
+
+    def run():
+        plan = skewgpu.BatchPlan(sizes)
+        devs = [skewgpu.to_device(A) for A in mats]
+        cd = [skewgpu.to_device(C) for C in cots]
+        Eo = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in sizes]
+        Go = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in sizes]
+        st = plan.exp(plan.pointer_array(devs), plan.pointer_array(Eo))
+        st2 = plan.exp_vjp(plan.pointer_array(devs), plan.pointer_array(cd), plan.pointer_array(Go))
+        torch.cuda.synchronize()
+        assert (st.cpu().numpy() == 0).all() and (st2.cpu().numpy() == 0).all()
+        out = [skewgpu.from_device(E) for E in Eo], [skewgpu.from_device(G) for G in Go]
+        plan.close()
+        return out
+
+    E1, G1 = run()
+    for b, A in enumerate(mats):
+        Eq = oracle.expm(A)
+        np.testing.assert_allclose(E1[b], Eq, atol=1e-11 * np.sqrt(A.shape[0]) * max(1, np.abs(Eq).max()))
+    Gq = oracle.exp_vjp(mats[0], cots[0])
+    assert np.abs(G1[0] - Gq).max() <= 1e-8 * np.abs(Gq).max()
+    monkeypatch.setenv("SKEW_FUNC_CHAIN_NMAX", "100000")
+    E2, G2 = run()
+    for b in range(len(sizes)):
+        np.testing.assert_allclose(E1[b], E2[b], atol=1e-11 * np.sqrt(sizes[b]) * max(1, np.abs(E2[b]).max()))
+        assert np.abs(G1[b] - G2[b]).max() <= 1e-9 * np.abs(G2[b]).max(), f"n={sizes[b]}"
