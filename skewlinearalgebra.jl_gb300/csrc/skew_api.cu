@@ -692,8 +692,10 @@ static int eigen_ws(skew_batch_plan_t P) {
 // (SKEW_FUNC_CHAIN_NMAX overrides; the eigenvalue order does not matter there).
 // The QR chain runs one matrix per thread, O(n^2) with a long dependency chain:
 // for n = 512 it takes 0.30 s on GB300, where bisection and twisted vectors take
-// a few milliseconds.
-static int func_chain_nmax() { return env_int("SKEW_FUNC_CHAIN_NMAX", 160); }
+// a few milliseconds.  Measured on the 512-matrix exp-adjoint workload (n in
+// {32, ..., 512}): 745 ms per step with 64, 768 with 160, 813 with 256, 1013 with
+// the chain for every size.
+static int func_chain_nmax() { return env_int("SKEW_FUNC_CHAIN_NMAX", 64); }
 
 // Size groups of the matrices above thr, their device index list and the workspace
 // of one chunk (problems per chunk bounded so one chunk's workspace stays within
