@@ -128,16 +128,27 @@ __global__ void __launch_bounds__(ZNT) zhess_cta_kernel(ZHessParams P) {
       __syncthreads();
       if (zero) continue;  // H = I: nothing to update
       zc* A22 = W + (c + 1) + (int64_t)(c + 1) * ld;
-      // p = A22 v  (rows by threads, coalesced down each column)
+      // p = A22 v  (rows by threads, coalesced down each column; eight loads in
+      // flight per thread: the working copy of a batch lives in L2)
       for (int i = threadIdx.x; i < m; i += ZNT) {
-        zc a0{0.0, 0.0}, a1{0.0, 0.0};
+        zc a0{0.0, 0.0}, a1{0.0, 0.0}, a2{0.0, 0.0}, a3{0.0, 0.0};
+        const zc* row = A22 + i;
         int j = 0;
-        for (; j + 1 < m; j += 2) {
-          a0 = zfma(A22[i + (int64_t)j * ld], vs[j], a0);
-          a1 = zfma(A22[i + (int64_t)(j + 1) * ld], vs[j + 1], a1);
+        for (; j + 7 < m; j += 8) {
+          zc x[8];
+#pragma unroll
+          for (int u = 0; u < 8; u++) x[u] = row[(int64_t)(j + u) * ld];
+          a0 = zfma(x[0], vs[j], a0);
+          a1 = zfma(x[1], vs[j + 1], a1);
+          a2 = zfma(x[2], vs[j + 2], a2);
+          a3 = zfma(x[3], vs[j + 3], a3);
+          a0 = zfma(x[4], vs[j + 4], a0);
+          a1 = zfma(x[5], vs[j + 5], a1);
+          a2 = zfma(x[6], vs[j + 6], a2);
+          a3 = zfma(x[7], vs[j + 7], a3);
         }
-        if (j < m) a0 = zfma(A22[i + (int64_t)j * ld], vs[j], a0);
-        ws[i] = zmul(R.tau, zadd(a0, a1));  // W = tau p
+        for (; j < m; j++) a0 = zfma(row[(int64_t)j * ld], vs[j], a0);
+        ws[i] = zmul(R.tau, zadd(zadd(a0, a1), zadd(a2, a3)));  // W = tau p
       }
       __syncthreads();
       // a = tau (W^H v) / 2
@@ -152,19 +163,48 @@ __global__ void __launch_bounds__(ZNT) zhess_cta_kernel(ZHessParams P) {
       const zc a = zmul(R.tau, zc{0.5 * dr, 0.5 * di});
       for (int i = threadIdx.x; i < m; i += ZNT) ws[i] = zfma(a, vs[i], ws[i]);
       __syncthreads();
-      // A22 += v w^H - w v^H on the lower triangle, mirrored
-      for (int64_t q = threadIdx.x; q < (int64_t)m * m; q += ZNT) {
-        const int j = (int)(q / m), i = (int)(q - (int64_t)j * m);
-        if (i < j) continue;
-        const zc vi = vs[i], wi = ws[i], vj = vs[j], wj = ws[j];
-        if (i == j) {
-          const double im2 = 2.0 * (vi.im * wi.re - vi.re * wi.im);  // 2 Im(v conj(w))
-          A22[i + (int64_t)i * ld].im += im2;
-        } else {
-          zc* pij = A22 + i + (int64_t)j * ld;
-          const zc u = zsub(zadd(*pij, zmulc(vi, wj)), zmulc(wi, vj));  // + v_i conj(w_j) - w_i conj(v_j)
-          *pij = u;
-          A22[j + (int64_t)i * ld] = zc{neg(u.re), u.im};  // -conj(u)
+      // A22 += v w^H - w v^H on the lower triangle (diagonal included), mirrored.
+      // The triangle is walked column by column as one list of m (m + 1) / 2 entries
+      // (no division per entry); four entries per thread and iteration, loads first.
+      {
+        int j = 0, r = threadIdx.x;  // entry (j + r, j): column j has m - j entries
+        while (j < m && r >= m - j) {
+          r -= m - j;
+          j++;
+        }
+        while (j < m) {
+          int jj[4], ii[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            jj[u] = j;
+            ii[u] = j + r;
+            if (j < m) {
+              r += ZNT;
+              while (j < m && r >= m - j) {
+                r -= m - j;
+                j++;
+              }
+            }
+          }
+          zc a[4];
+#pragma unroll
+          for (int u = 0; u < 4; u++)
+            if (jj[u] < m) a[u] = A22[ii[u] + (int64_t)jj[u] * ld];
+#pragma unroll
+          for (int u = 0; u < 4; u++) {
+            if (jj[u] >= m) continue;
+            const int i = ii[u], jc = jj[u];
+            const zc vi = vs[i], wi = ws[i];
+            if (i == jc) {
+              a[u].im += 2.0 * (vi.im * wi.re - vi.re * wi.im);  // 2 Im(v conj(w))
+              A22[i + (int64_t)i * ld] = a[u];
+            } else {
+              const zc vj = vs[jc], wj = ws[jc];
+              const zc uu = zsub(zadd(a[u], zmulc(vi, wj)), zmulc(wi, vj));  // + v_i conj(w_j) - w_i conj(v_j)
+              A22[i + (int64_t)jc * ld] = uu;
+              A22[jc + (int64_t)i * ld] = zc{neg(uu.re), uu.im};  // -conj(u)
+            }
+          }
         }
       }
       __syncthreads();
