@@ -31,6 +31,7 @@ namespace skew {
 constexpr int BNB = 64;        // panel width
 constexpr int SYM_ROWS = 256;  // rows per sym CTA (one per thread)
 constexpr int FIN_ROWS = 64;   // rows per fin CTA (4 threads per row)
+constexpr int PF_ROWS = 16;    // persistent kernel, phase B: smallest row block
 constexpr int UPD_T = 64;      // update tile edge
 constexpr int TAIL = 128;      // columns left to the one-CTA kernel
 
@@ -47,7 +48,7 @@ struct BlockedWs {
 size_t blocked_ws_doubles(int n) {
   const int max_chunks = 64;
   const int max_symtiles = (n + SYM_ROWS - 1) / SYM_ROWS;
-  const int max_fintiles = (n + FIN_ROWS - 1) / FIN_ROWS;
+  const int max_fintiles = (n + PF_ROWS - 1) / PF_ROWS;  // covers FIN_ROWS row tiles too
   return (size_t)n * BNB + (size_t)max_chunks * n + (size_t)max_symtiles * 2 * BNB + max_fintiles + 3 * (size_t)n +
          8;
 }
@@ -56,7 +57,7 @@ static BlockedWs carve_ws(double* base, int n) {
   BlockedWs w;
   w.max_chunks = 64;
   w.max_symtiles = (n + SYM_ROWS - 1) / SYM_ROWS;
-  w.max_fintiles = (n + FIN_ROWS - 1) / FIN_ROWS;
+  w.max_fintiles = (n + PF_ROWS - 1) / PF_ROWS;
   double* p = base;
   w.W = p;
   p += (size_t)n * BNB;
@@ -573,6 +574,7 @@ struct PersistParams {
   unsigned* sync;  // [0] barrier count, [1] barrier generation, [2] item counter
   int* err;
   int maxck;
+  int items_per_warp;  // matvec tiles per warp and column (chunk count)
 };
 
 __device__ __forceinline__ double ldg2(const double* p) { return __ldcg(p); }
@@ -648,8 +650,15 @@ __device__ Refl3 refl_from_column(const PersistParams& P, int c, double* red) {
     qq = block_sum<P_NW>(qq, red);
     xn = mx * sqrt(qq);
   }
-  const Reflector R = make_reflector(ldg2(col + c + 1), ss, xn);
-  return Refl3{R.beta, R.tau, R.scale};
+  __shared__ Refl3 s_R;
+  if (threadIdx.x == 0) {
+    const Reflector R = make_reflector(ldg2(col + c + 1), ss, xn);
+    s_R = Refl3{R.beta, R.tau, R.scale};
+  }
+  __syncthreads();
+  const Refl3 R = s_R;
+  __syncthreads();
+  return R;
 }
 
 // One 64 x 64 lower tile of the trailing update (same arithmetic as upd_kernel).
@@ -735,12 +744,88 @@ __device__ void upd_tile(double* __restrict__ A, int64_t lda, int n, int p, int 
   __syncthreads();
 }
 
+// Phase B rows: W[:, i], v into column c, the deferred update of column c+1 and the
+// norm partials of its rows below the subdiagonal.  Blocks of 256 / TPR rows, TPR
+// threads per row; a thread's panel terms j = g + TPR t are loaded once and used
+// both for W and for the column update.
+template <int TPR>
+__device__ void rows_phase(const PersistParams& P, double* A, int64_t lda, int n, int p, int c, int i, int nck,
+                           bool last, const Refl3& R, const double* psm, const double* su, const double* sWrow,
+                           const double* sArow, double* red) {
+  constexpr int ROWS = P_NT / TPR;
+  constexpr int NJ = BNB / TPR;
+  const int tid = threadIdx.x;
+  const int m = n - c - 1;
+  const int nfb = (m + ROWS - 1) / ROWS;
+  for (int fb = blockIdx.x; fb < nfb; fb += gridDim.x) {
+    const int row = c + 1 + fb * ROWS + tid / TPR;
+    const int g = tid % TPR;
+    const bool valid = row < n;
+    double aj[NJ], wj[NJ];
+#pragma unroll
+    for (int t = 0; t < NJ; t++) {
+      const int j = g + TPR * t;
+      aj[t] = 0.0;
+      wj[t] = 0.0;
+      if (valid && j < i) {
+        aj[t] = ldg2(A + row + (int64_t)(p + j) * lda);
+        wj[t] = ldg2(P.W + (size_t)j * n + row);
+      }
+    }
+    double vr = 0.0, acc = 0.0;
+    if (valid) {
+      vr = psm[row];
+      double y0 = 0.0, y1 = 0.0;
+      int q = g;
+      for (; q + TPR < nck; q += 2 * TPR) {
+        y0 += ldg2(P.ypart + (size_t)q * n + row);
+        y1 += ldg2(P.ypart + (size_t)(q + TPR) * n + row);
+      }
+      if (q < nck) y0 += ldg2(P.ypart + (size_t)q * n + row);
+      acc = y0 + y1;
+#pragma unroll
+      for (int t = 0; t < NJ; t++) {
+        const int j = g + TPR * t;
+        if (j < i) acc = fma(aj[t], su[j], fma(-wj[t], su[BNB + j], acc));
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < TPR; o <<= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    double wri = R.tau * acc;
+    if (row == c + 1) wri = sWrow[i];
+    if (valid && g == 0) {
+      P.W[(size_t)i * n + row] = wri;
+      A[row + (int64_t)c * lda] = vr;
+    }
+    double ssp = 0.0, uu = 0.0;
+    const bool doupd = valid && !last && row >= c + 2;
+    if (doupd) {
+#pragma unroll
+      for (int t = 0; t < NJ; t++) {
+        const int j = g + TPR * t;
+        if (j < i) uu = fma(aj[t], sWrow[j], fma(-wj[t], sArow[j], uu));
+      }
+      if (i % TPR == g) uu = fma(vr, sWrow[i], fma(-wri, sArow[i], uu));
+    }
+#pragma unroll
+    for (int o = 1; o < TPR; o <<= 1) uu += __shfl_xor_sync(0xffffffffu, uu, o);
+    if (doupd && g == 0) {
+      const double anew = ldg2(A + row + (int64_t)(c + 1) * lda) + uu;
+      A[row + (int64_t)(c + 1) * lda] = anew;
+      if (row >= c + 3) ssp = anew * anew;
+    }
+    const double sb = block_sum<P_NW>(ssp, red);
+    if (tid == 0) P.sspart[fb] = sb;
+  }
+}
+
 __global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
   extern __shared__ __align__(16) double psm[];  // v stage (n doubles) | update tile buffers
   __shared__ double red[P_NW];
   __shared__ double su[2 * BNB];
   __shared__ double sWrow[BNB + 1], sArow[BNB + 1];
-  __shared__ int s_item;
+  __shared__ int s_item, s_scal;
+  __shared__ Refl3 s_R3;
   const int n = P.n;
   const int64_t lda = P.lda;
   double* A = P.A;
@@ -763,7 +848,7 @@ __global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
         psm[j] = (R.tau == 0.0) ? 0.0 : (j == c + 1 ? 1.0 : ldg2(A + j + (int64_t)c * lda) * R.scale);
       __syncthreads();
       const int nrt = (m + 31) >> 5;
-      int nck = max(1, min((4 * nwarps + nrt - 1) / nrt, (m + 31) >> 5));
+      int nck = max(1, min((P.items_per_warp * nwarps + nrt - 1) / nrt, (m + 31) >> 5));
       nck = min(nck, P.maxck);
       const int chunk = (m + nck - 1) / nck;
       nck = (m + chunk - 1) / chunk;
@@ -836,64 +921,46 @@ __global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
         if (lane == 0) sArow[i] = (R.tau == 0.0) ? 0.0 : 1.0;
       }
       __syncthreads();
-      const int nfb = (m + FIN_ROWS - 1) / FIN_ROWS;
-      for (int fb = blockIdx.x; fb < nfb; fb += gridDim.x) {
-        const int row = c + 1 + fb * FIN_ROWS + (tid >> 2);
-        const int g = tid & 3;
-        const bool valid = row < n;
-        double vr = 0.0, acc = 0.0;
-        if (valid) {
-          vr = psm[row];
-          for (int j = g; j < i; j += 4)
-            acc = fma(ldg2(A + row + (int64_t)(p + j) * lda), su[j],
-                      fma(-ldg2(P.W + (size_t)j * n + row), su[BNB + j], acc));
-          for (int q = g; q < nck; q += 4) acc += ldg2(P.ypart + (size_t)q * n + row);
+      // rows in blocks, TPR threads per row: as many threads per row as keeps every
+      // block in one round of CTAs (16 at small m, fewer at large m)
+      int nfb;
+      {
+        const int G = gridDim.x;
+        if ((m + 15) / 16 <= G) {
+          nfb = (m + 15) / 16;
+          rows_phase<16>(P, A, lda, n, p, c, i, nck, last, R, psm, su, sWrow, sArow, red);
+        } else if ((m + 31) / 32 <= G) {
+          nfb = (m + 31) / 32;
+          rows_phase<8>(P, A, lda, n, p, c, i, nck, last, R, psm, su, sWrow, sArow, red);
+        } else {
+          nfb = (m + 63) / 64;
+          rows_phase<4>(P, A, lda, n, p, c, i, nck, last, R, psm, su, sWrow, sArow, red);
         }
-        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-        double wri = R.tau * acc;
-        if (row == c + 1) wri = sWrow[i];
-        if (valid && g == 0) {
-          P.W[(size_t)i * n + row] = wri;
-          A[row + (int64_t)c * lda] = vr;
-        }
-        double ssp = 0.0, uu = 0.0;
-        const bool doupd = valid && !last && row >= c + 2;
-        if (doupd)
-          for (int j = g; j <= i; j += 4) {
-            const double arj = (j == i) ? vr : ldg2(A + row + (int64_t)(p + j) * lda);
-            const double wrj = (j == i) ? wri : ldg2(P.W + (size_t)j * n + row);
-            uu = fma(arj, sWrow[j], fma(-wrj, sArow[j], uu));
-          }
-        uu += __shfl_xor_sync(0xffffffffu, uu, 1);
-        uu += __shfl_xor_sync(0xffffffffu, uu, 2);
-        if (doupd && g == 0) {
-          const double anew = ldg2(A + row + (int64_t)(c + 1) * lda) + uu;
-          A[row + (int64_t)(c + 1) * lda] = anew;
-          if (row >= c + 3) ssp = anew * anew;
-        }
-        const double sb = block_sum<P_NW>(ssp, red);
-        if (tid == 0) P.sspart[fb] = sb;
       }
       if (!gsync(P)) return;
       if (!last) {
         // reflector c+1, identically in every CTA
         const int c1 = c + 1;
+        // one lane forms it (a warp-wide FP64 instruction costs the pipe the same
+        // with one lane as with 32); the others read it from shared memory
         if (w == 0) {
           double ss = 0.0;
           for (int t = lane; t < nfb; t += 32) ss += ldg2(P.sspart + t);
           ss = warp_sum(ss);
-          if (lane == 0) red[0] = ss;
+          if (lane == 0) {
+            s_scal = ss_needs_scaling(ss) ? 1 : 0;
+            if (!s_scal) {
+              const Reflector Rf = make_reflector(ldg2(A + (c1 + 1) + (int64_t)c1 * lda), ss, -1.0);
+              s_R3 = Refl3{Rf.beta, Rf.tau, Rf.scale};
+            }
+          }
         }
         __syncthreads();
-        const double ss = red[0];
-        __syncthreads();
-        if (ss_needs_scaling(ss)) {
+        if (s_scal)
           R = refl_from_column(P, c1, red);
-        } else {
-          const Reflector Rf = make_reflector(ldg2(A + (c1 + 1) + (int64_t)c1 * lda), ss, -1.0);
-          R = Refl3{Rf.beta, Rf.tau, Rf.scale};
-        }
+        else
+          R = s_R3;
+        __syncthreads();
         if (blockIdx.x == 0 && tid == 0) {
           P.ev[c1] = R.beta;
           P.tau[c1] = R.tau;
@@ -975,6 +1042,11 @@ cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double*
   P.sync = (unsigned*)(extra + 2 * BNB);
   P.err = err_dev;
   P.maxck = ws.max_chunks;
+  P.items_per_warp = 4;
+  {
+    const char* v = getenv("SKEW_PERSIST_ITEMS");  // sweeps: 1..16
+    if (v && *v) P.items_per_warp = std::max(1, std::min(16, atoi(v)));
+  }
   e = cudaMemsetAsync(P.sync, 0, 4 * sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(err_dev, 0, sizeof(int), st);

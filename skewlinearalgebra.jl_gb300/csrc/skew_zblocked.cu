@@ -42,8 +42,7 @@ constexpr int ZP_NW = ZP_NT / 32;
 constexpr int ZBNB = 32;   // panel width
 constexpr int ZUT = 64;    // trailing-update tile edge
 constexpr int ZKC = 8;     // panel columns per shared-memory stage of the update
-constexpr int ZTPR = 16;   // threads per row in phase B
-constexpr int ZFIN = ZP_NT / ZTPR;  // rows per row block in phase B
+constexpr int ZFIN = 16;   // smallest row block of phase B (sizes sspart)
 constexpr int ZTAILP = 128;  // trailing columns left to the one-CTA kernel
 constexpr long long ZP_POLL = 1LL << 24;
 constexpr int ZP_MAXWARPS = 16384;  // dpart slots: grid x 8 warps at most
@@ -286,6 +285,95 @@ __device__ void zp_upd_tile(const ZPersistParams& P, int p, int nbp, int q, int 
 
 }  // namespace
 
+// Phase B rows: blocks of ZP_NT / TPR rows, TPR threads per row (see the kernel).
+template <int TPR>
+__device__ void zp_rows_phase(const ZPersistParams& P, zc* A, int64_t lda, int n, int p, int c, int i, int nck,
+                              bool last, const ZRef& R, const zc alpha, const zc* vs, const zc* su, const zc* sWrow,
+                              const zc* sArow, double* red) {
+  constexpr int ROWS = ZP_NT / TPR;
+  const int tid = threadIdx.x;
+  const int m = n - c - 1;
+  const int nfb = (m + ROWS - 1) / ROWS;
+  for (int fb = blockIdx.x; fb < nfb; fb += gridDim.x) {
+    const int row = c + 1 + fb * ROWS + tid / TPR;
+    const int g = tid % TPR;
+    const bool valid = row < n;
+    // this thread's panel terms j = g + TPR t: loaded once, used for y and for
+    // the deferred update of column c+1
+    constexpr int NJ = ZBNB / TPR;
+    zc aj[NJ], wj[NJ];
+#pragma unroll
+    for (int t = 0; t < NJ; t++) {
+      const int j = g + TPR * t;
+      aj[t] = zc{0.0, 0.0};
+      wj[t] = zc{0.0, 0.0};
+      if (valid && j < i) {
+        aj[t] = ldz(A + row + (int64_t)(p + j) * lda);
+        wj[t] = ldz(P.W + (size_t)j * n + row);
+      }
+    }
+    zc vr{0.0, 0.0}, acc{0.0, 0.0};
+    if (valid) {
+      vr = vs[row];
+      zc y0{0.0, 0.0}, y1{0.0, 0.0};
+      int q2 = g;
+      for (; q2 + TPR < nck; q2 += 2 * TPR) {
+        y0 = zadd(y0, ldz(P.ypart + (size_t)q2 * n + row));
+        y1 = zadd(y1, ldz(P.ypart + (size_t)(q2 + TPR) * n + row));
+      }
+      if (q2 < nck) y0 = zadd(y0, ldz(P.ypart + (size_t)q2 * n + row));
+      acc = zadd(y0, y1);
+#pragma unroll
+      for (int t = 0; t < NJ; t++) {
+        const int j = g + TPR * t;
+        if (j < i) acc = zsub(zfma(aj[t], su[j], acc), zmul(wj[t], su[ZBNB + j]));
+      }
+    }
+#pragma unroll
+    for (int o = 1; o < TPR; o <<= 1) {
+      acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
+      acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
+    }
+    zc wri = zfma(alpha, vr, zmul(R.tau, acc));
+    if (row == c + 1) wri = sWrow[i];
+    if (valid && g == 0) {
+      stz(P.W + (size_t)i * n + row, wri);
+      stz(A + row + (int64_t)c * lda, vr);
+    }
+    // deferred update of column c+1 (rows c+1.., the diagonal included):
+    // A[row, c+1] += sum_{j <= i} V[row, j] conj(W[c+1, j]) - W[row, j] conj(V[c+1, j])
+    double ssp = 0.0;
+    zc uu{0.0, 0.0};
+    const bool doupd = valid && !last;
+    if (doupd) {
+#pragma unroll
+      for (int t = 0; t < NJ; t++) {
+        const int j = g + TPR * t;
+        if (j < i) uu = zsub(zadd(uu, zmulc(aj[t], sWrow[j])), zmulc(wj[t], sArow[j]));
+      }
+      if (i % TPR == g) uu = zsub(zadd(uu, zmulc(vr, sWrow[i])), zmulc(wri, sArow[i]));
+    }
+#pragma unroll
+    for (int o = 1; o < TPR; o <<= 1) {
+      uu.re += __shfl_xor_sync(0xffffffffu, uu.re, o);
+      uu.im += __shfl_xor_sync(0xffffffffu, uu.im, o);
+    }
+    if (doupd && g == 0) {
+      zc* pa = A + row + (int64_t)(c + 1) * lda;
+      zc anew = ldz(pa);
+      if (row == c + 1) {
+        anew.im += uu.im;  // the diagonal receives the imaginary part only
+      } else {
+        anew = zadd(anew, uu);
+      }
+      stz(pa, anew);
+      if (row >= c + 3) ssp = fma(anew.re, anew.re, anew.im * anew.im);
+    }
+    const double sb = block_sum<ZP_NW>(ssp, red);
+    if (tid == 0) P.sspart[fb] = sb;
+  }
+}
+
 __global__ void __launch_bounds__(ZP_NT, 1) zpersist_kernel(ZPersistParams P) {
   extern __shared__ __align__(16) double zpsm_raw[];
   zc* vs = reinterpret_cast<zc*>(zpsm_raw);  // v stage (n complex) | update tile buffers
@@ -440,84 +528,17 @@ __global__ void __launch_bounds__(ZP_NT, 1) zpersist_kernel(ZPersistParams P) {
       }
       __syncthreads();
       const zc alpha = s_alpha;
-      const int nfb = (m + ZFIN - 1) / ZFIN;
-      for (int fb = blockIdx.x; fb < nfb; fb += gridDim.x) {
-        const int row = c + 1 + fb * ZFIN + tid / ZTPR;
-        const int g = tid % ZTPR;
-        const bool valid = row < n;
-        // this thread's panel terms j = g + ZTPR t: loaded once, used for y and for
-        // the deferred update of column c+1
-        constexpr int NJ = ZBNB / ZTPR;
-        zc aj[NJ], wj[NJ];
-#pragma unroll
-        for (int t = 0; t < NJ; t++) {
-          const int j = g + ZTPR * t;
-          aj[t] = zc{0.0, 0.0};
-          wj[t] = zc{0.0, 0.0};
-          if (valid && j < i) {
-            aj[t] = ldz(A + row + (int64_t)(p + j) * lda);
-            wj[t] = ldz(P.W + (size_t)j * n + row);
-          }
-        }
-        zc vr{0.0, 0.0}, acc{0.0, 0.0};
-        if (valid) {
-          vr = vs[row];
-          zc y0{0.0, 0.0}, y1{0.0, 0.0};
-          int q2 = g;
-          for (; q2 + ZTPR < nck; q2 += 2 * ZTPR) {
-            y0 = zadd(y0, ldz(P.ypart + (size_t)q2 * n + row));
-            y1 = zadd(y1, ldz(P.ypart + (size_t)(q2 + ZTPR) * n + row));
-          }
-          if (q2 < nck) y0 = zadd(y0, ldz(P.ypart + (size_t)q2 * n + row));
-          acc = zadd(y0, y1);
-#pragma unroll
-          for (int t = 0; t < NJ; t++) {
-            const int j = g + ZTPR * t;
-            if (j < i) acc = zsub(zfma(aj[t], su[j], acc), zmul(wj[t], su[ZBNB + j]));
-          }
-        }
-#pragma unroll
-        for (int o = 1; o < ZTPR; o <<= 1) {
-          acc.re += __shfl_xor_sync(0xffffffffu, acc.re, o);
-          acc.im += __shfl_xor_sync(0xffffffffu, acc.im, o);
-        }
-        zc wri = zfma(alpha, vr, zmul(R.tau, acc));
-        if (row == c + 1) wri = sWrow[i];
-        if (valid && g == 0) {
-          stz(P.W + (size_t)i * n + row, wri);
-          stz(A + row + (int64_t)c * lda, vr);
-        }
-        // deferred update of column c+1 (rows c+1.., the diagonal included):
-        // A[row, c+1] += sum_{j <= i} V[row, j] conj(W[c+1, j]) - W[row, j] conj(V[c+1, j])
-        double ssp = 0.0;
-        zc uu{0.0, 0.0};
-        const bool doupd = valid && !last;
-        if (doupd) {
-#pragma unroll
-          for (int t = 0; t < NJ; t++) {
-            const int j = g + ZTPR * t;
-            if (j < i) uu = zsub(zadd(uu, zmulc(aj[t], sWrow[j])), zmulc(wj[t], sArow[j]));
-          }
-          if (i % ZTPR == g) uu = zsub(zadd(uu, zmulc(vr, sWrow[i])), zmulc(wri, sArow[i]));
-        }
-#pragma unroll
-        for (int o = 1; o < ZTPR; o <<= 1) {
-          uu.re += __shfl_xor_sync(0xffffffffu, uu.re, o);
-          uu.im += __shfl_xor_sync(0xffffffffu, uu.im, o);
-        }
-        if (doupd && g == 0) {
-          zc* pa = A + row + (int64_t)(c + 1) * lda;
-          zc anew = ldz(pa);
-          if (row == c + 1) {
-            anew.im += uu.im;  // the diagonal receives the imaginary part only
-          } else {
-            anew = zadd(anew, uu);
-          }
-          stz(pa, anew);
-          if (row >= c + 3) ssp = fma(anew.re, anew.re, anew.im * anew.im);
-        }
-        const double sb = block_sum<ZP_NW>(ssp, red);
-        if (tid == 0) P.sspart[fb] = sb;
+      // rows: as many threads per row as keeps every block in one round of CTAs
+      int nfb;
+      if ((m + 15) / 16 <= (int)gridDim.x) {
+        nfb = (m + 15) / 16;
+        zp_rows_phase<16>(P, A, lda, n, p, c, i, nck, last, R, alpha, vs, su, sWrow, sArow, red);
+      } else if ((m + 31) / 32 <= (int)gridDim.x) {
+        nfb = (m + 31) / 32;
+        zp_rows_phase<8>(P, A, lda, n, p, c, i, nck, last, R, alpha, vs, su, sWrow, sArow, red);
+      } else {
+        nfb = (m + 63) / 64;
+        zp_rows_phase<4>(P, A, lda, n, p, c, i, nck, last, R, alpha, vs, su, sWrow, sArow, red);
       }
       if (!zp_gsync(P)) return;
       if (!last) {  // reflector c+1, identically in every CTA (one thread forms it)
