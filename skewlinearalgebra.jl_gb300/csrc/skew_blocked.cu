@@ -1042,7 +1042,9 @@ cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double*
   P.sync = (unsigned*)(extra + 2 * BNB);
   P.err = err_dev;
   P.maxck = ws.max_chunks;
-  P.items_per_warp = 4;
+  // matvec tiles per warp and column: measured on GB300 at n = 8192, 8 gives 932 ms,
+  // 4 945 ms, 2 981 ms (more, smaller tiles shorten the wait for the last ones)
+  P.items_per_warp = 8;
   {
     const char* v = getenv("SKEW_PERSIST_ITEMS");  // sweeps: 1..16
     if (v && *v) P.items_per_warp = std::max(1, std::min(16, atoi(v)));
