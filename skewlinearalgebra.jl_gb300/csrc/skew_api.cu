@@ -703,6 +703,13 @@ static int func_chain_nmax() { return env_int("SKEW_FUNC_CHAIN_NMAX", 64); }
 static int fv_setup(skew_batch_plan_t P, int thr) {
   if (P->fv_thresh == thr) return SKEW_OK;
   cudaStream_t st = P->h->stream;
+  // recorded graphs reference the old workspace: drop them (they re-record)
+  for (auto& g : P->graphs)
+    if (g.valid) {
+      CK(cudaGraphExecDestroy(g.exec));
+      g.valid = false;
+      g.exec = nullptr;
+    }
   if (P->fv_idx) CK(cudaFreeAsync(P->fv_idx, st));
   if (P->fv_ws) CK(cudaFreeAsync(P->fv_ws, st));
   P->fv_idx = nullptr;
