@@ -90,7 +90,7 @@ SKEW_API int skew_logabspf_d(skew_handle_t h, double* A, int64_t n, int64_t lda,
 
 /* rrule(logabspfaffian) forward + pullback seed 1: as skew_logabspf_d, and
  * G = d log|Pf(A)| / dA = 1/2 A^{-T}, formed as Q (1/2 T^{-T}) Q^T from the reflectors.
- * (No reference counterpart: the spec adjoint.) */
+ * (No reference counterpart: the reference defines no rrule for logabspfaffian.) */
 SKEW_API int skew_logabspf_grad_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* sign,
                          double* G, int64_t ldg, int* info);
 
@@ -152,6 +152,17 @@ SKEW_API int skew_batch_plan_destroy(skew_batch_plan_t plan);
  * (leading dimension n[b]).  status[b] is a skew_status_t per matrix. */
 SKEW_API int skew_batch_logabspf_d(skew_batch_plan_t plan, const double* const* A, double* logpf, double* sign,
                           double* const* grad, int* status);
+
+/* The same on host buffers (pfaffian.jl:236-246 called on host matrices, one call
+ * for the batch): A holds the matrices back to back in the order of n[] given to
+ * the plan, each column-major with leading dimension n[b]; grad (or NULL) receives
+ * 1/2 A_b^{-T} in the same layout; logpf, sign, status are host arrays [count].
+ * A and grad must be page-locked (cudaHostAlloc / cudaHostRegister), else
+ * SKEW_BAD_ARG: every CTA reads its matrix from host memory and writes its
+ * gradient back itself, so the transfers overlap the compute.  Returns when the
+ * results are in host memory (synchronises the handle's stream). */
+SKEW_API int skew_batch_logabspf_host_d(skew_batch_plan_t plan, const double* A, double* grad, double* logpf,
+                               double* sign, int* status);
 
 /* eigvals for every matrix: vals_im[b] (device pointers) receives n[b] values. */
 SKEW_API int skew_batch_eigvals_d(skew_batch_plan_t plan, const double* const* A, double* const* vals_im, int* status);

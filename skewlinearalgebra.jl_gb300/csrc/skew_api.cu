@@ -82,6 +82,15 @@ struct skew_batch_plan_st {
   };
   GraphSlot graphs[6];
   bool graphs_off = false;              // capture failed once (or disabled): launch directly
+  // host-buffer logabspfaffian (skew_batch_logabspf_host_d), allocated on first use
+  int64_t hio_total = 0;       // sum n^2
+  int64_t* hio_off = nullptr;  // packed offsets (creation order)
+  double** hio_a = nullptr;    // [count] host-mapped input addresses
+  double** hio_gh = nullptr;   // [count] host-mapped gradient destinations
+  double** hio_g = nullptr;    // [count] device gradient slots
+  double* hio_grad = nullptr;  // sum n^2 doubles
+  double* hio_out = nullptr;   // logpf, sign (2 x count)
+  int* hio_status = nullptr;
   // function paths (exp, cis, the exp adjoint, matrix functions): matrices with
   // n > fv_thresh take bisection and twisted vectors instead of the QR chain,
   // by size group; built once per plan and threshold (outside any capture)
@@ -454,6 +463,9 @@ int skew_batch_plan_destroy(skew_batch_plan_t P) {
     if (q) cudaFreeAsync(q, st);
   if (P->fv_idx) cudaFreeAsync(P->fv_idx, st);
   if (P->fv_ws) cudaFreeAsync(P->fv_ws, st);
+  void* hio[] = {P->hio_off, P->hio_a, P->hio_gh, P->hio_g, P->hio_grad, P->hio_out, P->hio_status};
+  for (void* q : hio)
+    if (q) cudaFreeAsync(q, st);
   cudaStreamSynchronize(st);
   delete P;
   return SKEW_OK;
@@ -461,7 +473,8 @@ int skew_batch_plan_destroy(skew_batch_plan_t P) {
 
 static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logpf, double* sign,
                        double* const* grad, int* status, bool tridiag_only, double* tau_out = nullptr,
-                       double* const* refl_out = nullptr) {
+                       double* const* refl_out = nullptr, bool host_in = false,
+                       double* const* grad_host = nullptr) {
   cudaStream_t st = P->h->stream;
   CK(cudaMemsetAsync(P->d_counters, 0, sizeof(unsigned) * std::max<size_t>(P->buckets.size(), 1), st));
   for (size_t i = 0; i < P->buckets.size(); i++) {
@@ -486,6 +499,8 @@ static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logp
     bp.tau_out = tau_out;
     bp.refl_out = refl_out;
     bp.status = status;
+    bp.host_in = host_in ? 1 : 0;
+    bp.grad_host = grad_host;
     CK(launch_batch_pf(bp, B.grid, st, tridiag_only));
   }
   return SKEW_OK;
@@ -604,6 +619,90 @@ __global__ void fill_ptrs_kernel(double** dst, double* base, const int64_t* off,
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < count) dst[i] = base + off[i];
 }
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// logabspfaffian + gradient on host buffers.  Each CTA reads its matrix from
+// page-locked host memory over the host link and writes its finished gradient
+// back the same way, so the transfers of one matrix overlap the compute of the
+// others instead of running as whole-batch copies before and after the launch.
+// ---------------------------------------------------------------------------
+
+// The device address of a page-locked host buffer [h, h + bytes), or an error
+// when any part of it is pageable or the range is not one mapping.
+static int host_mapped(const void* h, size_t bytes, void** d) {
+  cudaPointerAttributes a0, a1;
+  if (cudaPointerGetAttributes(&a0, h) != cudaSuccess ||
+      cudaPointerGetAttributes(&a1, (const char*)h + bytes - 1) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return SKEW_BAD_ARG;
+  }
+  if (a0.type != cudaMemoryTypeHost || a1.type != cudaMemoryTypeHost || !a0.devicePointer || !a1.devicePointer)
+    return SKEW_BAD_ARG;
+  if ((const char*)a1.devicePointer - (const char*)a0.devicePointer != (ptrdiff_t)(bytes - 1)) return SKEW_BAD_ARG;
+  *d = a0.devicePointer;
+  return SKEW_OK;
+}
+
+static int hio_ws(skew_batch_plan_t P) {
+  if (P->hio_off) return SKEW_OK;
+  cudaStream_t st = P->h->stream;
+  const int64_t count = P->count;
+  std::vector<int64_t> off(count);
+  int64_t sq = 0;
+  for (int64_t b = 0; b < count; b++) {
+    off[b] = sq;
+    sq += (int64_t)P->n_host[b] * P->n_host[b];
+  }
+  bool ok = true;
+  auto alloc = [&](void** p, size_t bytes) { ok &= cudaMallocAsync(p, std::max<size_t>(bytes, 8), st) == cudaSuccess; };
+  alloc((void**)&P->hio_off, sizeof(int64_t) * count);
+  alloc((void**)&P->hio_a, sizeof(double*) * count);
+  alloc((void**)&P->hio_gh, sizeof(double*) * count);
+  alloc((void**)&P->hio_g, sizeof(double*) * count);
+  alloc((void**)&P->hio_grad, sizeof(double) * sq);
+  alloc((void**)&P->hio_out, sizeof(double) * 2 * count);
+  alloc((void**)&P->hio_status, sizeof(int) * count);
+  if (!ok) return SKEW_NO_MEMORY;
+  CK(cudaMemcpyAsync(P->hio_off, off.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, st));
+  fill_ptrs_kernel<<<(int)((count + 255) / 256), 256, 0, st>>>(P->hio_g, P->hio_grad, P->hio_off, (int)count);
+  CK(cudaGetLastError());
+  CK(cudaStreamSynchronize(st));  // `off` goes out of scope
+  P->hio_total = sq;
+  return SKEW_OK;
+}
+
+extern "C" int skew_batch_logabspf_host_d(skew_batch_plan_t P, const double* hA, double* hG, double* h_logpf,
+                                          double* h_sign, int* h_status) {
+  if (!P || (P->count > 0 && (!hA || !h_logpf || !h_sign || !h_status))) return SKEW_BAD_ARG;
+  if (P->count == 0) return SKEW_OK;
+  int s = hio_ws(P);
+  if (s) return s;
+  const int64_t count = P->count;
+  cudaStream_t st = P->h->stream;
+  const int g = (int)((count + 255) / 256);
+  if (P->hio_total > 0) {
+    const size_t bytes = sizeof(double) * (size_t)P->hio_total;
+    void *dA = nullptr, *dG = nullptr;
+    if ((s = host_mapped(hA, bytes, &dA))) return s;
+    if (hG && (s = host_mapped(hG, bytes, &dG))) return s;
+    fill_ptrs_kernel<<<g, 256, 0, st>>>(P->hio_a, (double*)dA, P->hio_off, (int)count);
+    if (dG) fill_ptrs_kernel<<<g, 256, 0, st>>>(P->hio_gh, (double*)dG, P->hio_off, (int)count);
+    CK(cudaGetLastError());
+    s = run_buckets(P, P->hio_a, P->hio_out, P->hio_out + count, dG ? P->hio_g : nullptr, P->hio_status, false,
+                    nullptr, nullptr, true, dG ? P->hio_gh : nullptr);
+  } else {  // every matrix is 0 x 0: nothing to read
+    s = run_buckets(P, P->hio_g, P->hio_out, P->hio_out + count, nullptr, P->hio_status, false);
+  }
+  if (s) return s;
+  CK(cudaMemcpyAsync(h_logpf, P->hio_out, sizeof(double) * count, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h_sign, P->hio_out + count, sizeof(double) * count, cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(h_status, P->hio_status, sizeof(int) * count, cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  return SKEW_OK;
+}
+
+namespace {
 __global__ void set8_kernel(double** dst, double* a, double* b, double* c, double* d, double* e, double* f,
                             double* g, double* h) {
   dst[0] = a;

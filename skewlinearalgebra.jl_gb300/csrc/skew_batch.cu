@@ -17,7 +17,7 @@
 //      step is hidden behind this step's update.
 // Steps 1 and 2 cost m^2 FMAs each (4/3 n^3 flops in total).
 //
-// Gradient (the spec adjoint; the reference has no rrule):
+// Gradient (the adjoint of log|Pf|; the reference has no rrule):
 // d log|Pf(A)|/dA = 1/2 A^{-T} = -1/2 A^{-1} = Q (-1/2 T^{-1}) Q^T with
 // Q = H_0 H_1 ... H_{n-3}.  Starting from M = -1/2 T^{-1}, the reflectors are
 // applied innermost first in blocks of GNB.  A block Q_b = I - V T_b V^T
@@ -126,6 +126,49 @@ __device__ bool copy_in(const double* __restrict__ A, int64_t lda, const MW& W, 
     if (check) bad |= !(a == -A[j + (int64_t)i * lda]);
   }
   return __syncthreads_or(bad) == 0;
+}
+
+// Working copy from page-locked host memory (A contiguous, leading dimension n):
+// eight loads in flight per thread before their stores, so a warp keeps 2 KB of
+// requests on the host link instead of 256 bytes.
+template <int NT, class MW>
+__device__ void copy_in_host(const double* __restrict__ A, const MW& W, int n) {
+  constexpr int U = 8;
+  const int64_t total = (int64_t)n * n;
+  int64_t e0 = threadIdx.x;
+  for (; e0 + (int64_t)(U - 1) * NT < total; e0 += (int64_t)U * NT) {
+    double a[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) a[u] = A[e0 + (int64_t)u * NT];
+#pragma unroll
+    for (int u = 0; u < U; u++) {
+      const int64_t e = e0 + (int64_t)u * NT;
+      const int j = (int)(e / n), i = (int)(e - (int64_t)j * n);
+      W.at(i, j) = a[u];
+    }
+  }
+  for (; e0 < total; e0 += NT) {
+    const int j = (int)(e0 / n), i = (int)(e0 - (int64_t)j * n);
+    W.at(i, j) = A[e0];
+  }
+  __syncthreads();
+}
+
+// The finished gradient (n x n, contiguous, written by this CTA) to its
+// page-locked host destination.
+template <int NT>
+__device__ void copy_out_host(const double* __restrict__ G, double* __restrict__ Gh, int n) {
+  constexpr int U = 4;
+  const int64_t total = (int64_t)n * n;
+  int64_t e0 = threadIdx.x;
+  for (; e0 + (int64_t)(U - 1) * NT < total; e0 += (int64_t)U * NT) {
+    double a[U];
+#pragma unroll
+    for (int u = 0; u < U; u++) a[u] = G[e0 + (int64_t)u * NT];
+#pragma unroll
+    for (int u = 0; u < U; u++) Gh[e0 + (int64_t)u * NT] = a[u];
+  }
+  for (; e0 < total; e0 += NT) Gh[e0] = G[e0];
 }
 
 // ---------------------------------------------------------------------------
@@ -621,12 +664,26 @@ struct Job {
   int* status;
   bool check;
   bool want_pf;
+  bool host_in;  // A in page-locked host memory (batched path: lda == n, never in place)
 };
 
 template <int NT, class MW>
 __device__ void run_job(const Job& J, const MW& W, bool inplace, const Smem& s) {
   const int n = J.n;
-  const bool ok = copy_in<NT>(J.A, J.lda, W, inplace, n, J.check);
+  bool ok = true;
+  if (J.host_in) {
+    copy_in_host<NT>(J.A, W, n);
+    if (J.check) {  // on the working copy: no strided reads over the host link
+      int bad = 0;
+      for (int64_t e = threadIdx.x; e < (int64_t)n * n; e += NT) {
+        const int j = (int)(e / n), i = (int)(e - (int64_t)j * n);
+        bad |= !(W.at(i, j) == -W.at(j, i));
+      }
+      ok = __syncthreads_or(bad) == 0;
+    }
+  } else {
+    ok = copy_in<NT>(J.A, J.lda, W, inplace, n, J.check);
+  }
   const GMat G{J.G, J.ldg};
   if (!ok) {
     if (threadIdx.x == 0) {
@@ -693,7 +750,9 @@ __device__ void run_job(const Job& J, const MW& W, bool inplace, const Smem& s) 
 
 // Persistent batched kernel over order[begin:end) (matrices sorted largest
 // first); CTAs take the next matrix from an atomic counter.
-template <int NT, bool SM>
+// HOST: the inputs are read from, and the gradients written to, page-locked host
+// memory (a separate instantiation, so the device-resident kernels are unchanged).
+template <int NT, bool SM, bool HOST>
 __global__ void __launch_bounds__(NT) batch_kernel(BatchParams P, int tridiag_only) {
   const Smem s = carve(P.nmax);
   const int woff = smem_doubles(P.nmax, NT / 32);
@@ -720,6 +779,7 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchParams P, int tridiag_on
     J.status = tridiag_only ? nullptr : P.status + b;
     J.check = P.check != 0;
     J.want_pf = !tridiag_only;
+    J.host_in = HOST && P.host_in != 0;
     if constexpr (SM) {
       const SMat W{woff, n | 1};
       run_job<NT>(J, W, false, s);
@@ -727,6 +787,9 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchParams P, int tridiag_on
       const GMat W{P.gws + (size_t)blockIdx.x * P.gws_slot, (int64_t)(n | 1)};
       run_job<NT>(J, W, false, s);
     }
+    // run_job ends with a barrier after its last write of G
+    if constexpr (HOST)
+      if (J.G && P.grad_host) copy_out_host<NT>(J.G, P.grad_host[b], n);
   }
 }
 
@@ -748,6 +811,7 @@ __global__ void __launch_bounds__(NT) single_kernel(SingleParams P) {
   J.status = P.info;
   J.check = P.check != 0;
   J.want_pf = P.want_pf != 0;
+  J.host_in = false;
   const GMat W{P.A, P.lda};
   run_job<NT>(J, W, true, s);
 }
@@ -797,26 +861,32 @@ size_t batch_smem_bytes(int nmax, bool smem_matrix) {
 
 // Per-instantiation record of the devices on which the shared-memory limit of
 // batch_kernel<NT, SM> has been raised (shared by the launch and the occupancy query).
-template <int NT, bool SM>
+template <int NT, bool SM, bool HOST>
 std::atomic<uint64_t> g_smem_raised{0};
 
-template <int NT, bool SM>
+template <int NT, bool SM, bool HOST>
 static cudaError_t launch_t(const BatchParams& P, int grid, size_t smem, cudaStream_t st, int tridiag_only) {
-  cudaError_t e = raise_smem_limit_once((const void*)batch_kernel<NT, SM>, g_smem_raised<NT, SM>);
+  cudaError_t e = raise_smem_limit_once((const void*)batch_kernel<NT, SM, HOST>, g_smem_raised<NT, SM, HOST>);
   if (e != cudaSuccess) return e;
-  batch_kernel<NT, SM><<<grid, NT, smem, st>>>(P, tridiag_only);
+  batch_kernel<NT, SM, HOST><<<grid, NT, smem, st>>>(P, tridiag_only);
   return cudaGetLastError();
 }
 
-cudaError_t launch_batch_pf(const BatchParams& P, int grid, cudaStream_t st, bool tridiag_only) {
+template <bool HOST>
+static cudaError_t launch_pf(const BatchParams& P, int grid, cudaStream_t st, bool tridiag_only) {
   const bool sm = P.smem_matrix != 0;
   const size_t smem = batch_smem_bytes(P.nmax, sm);
   const int nt = threads_for(P.nmax, sm);
-  if (sm && nt == 128) return launch_t<128, true>(P, grid, smem, st, tridiag_only);
-  if (sm && nt == 256) return launch_t<256, true>(P, grid, smem, st, tridiag_only);
-  if (sm) return launch_t<512, true>(P, grid, smem, st, tridiag_only);
-  if (nt == NT_LARGE) return launch_t<NT_LARGE, false>(P, grid, smem, st, tridiag_only);
-  return launch_t<NT_GLOBAL, false>(P, grid, smem, st, tridiag_only);
+  if (sm && nt == 128) return launch_t<128, true, HOST>(P, grid, smem, st, tridiag_only);
+  if (sm && nt == 256) return launch_t<256, true, HOST>(P, grid, smem, st, tridiag_only);
+  if (sm) return launch_t<512, true, HOST>(P, grid, smem, st, tridiag_only);
+  if (nt == NT_LARGE) return launch_t<NT_LARGE, false, HOST>(P, grid, smem, st, tridiag_only);
+  return launch_t<NT_GLOBAL, false, HOST>(P, grid, smem, st, tridiag_only);
+}
+
+cudaError_t launch_batch_pf(const BatchParams& P, int grid, cudaStream_t st, bool tridiag_only) {
+  if (P.host_in || P.grad_host) return launch_pf<true>(P, grid, st, tridiag_only);
+  return launch_pf<false>(P, grid, st, tridiag_only);
 }
 
 cudaError_t launch_single(const SingleParams& P, cudaStream_t st) {
@@ -831,11 +901,14 @@ cudaError_t launch_single(const SingleParams& P, cudaStream_t st) {
 
 int batch_threads() { return NT_LARGE; }
 
+// Occupancy of the device-resident instantiation (the host one has the same
+// shared memory and launch bounds).
 template <int NT, bool SM>
 static int occ_t(size_t smem) {
   int occ = 0;
-  cudaError_t e = raise_smem_limit_once((const void*)batch_kernel<NT, SM>, g_smem_raised<NT, SM>);
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<NT, SM>, NT, smem);
+  cudaError_t e = raise_smem_limit_once((const void*)batch_kernel<NT, SM, false>, g_smem_raised<NT, SM, false>);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, batch_kernel<NT, SM, false>, NT, smem);
   if (e != cudaSuccess || occ < 1) {
     cudaGetLastError();
     return 1;

@@ -51,6 +51,9 @@ struct BatchParams {
   double* tau_out;         // packed tau, same offsets, or null
   double* const* refl_out; // [count] n x n buffers receiving the reduced matrix (reflectors) or null
   int* status;             // [count] or null
+  int32_t host_in = 0;     // A[] point into page-locked host memory (read with more loads in flight)
+  double* const* grad_host = nullptr;  // [count] page-locked host destinations: the finished
+                                       // gradient is copied there by the CTA that formed it
 };
 
 struct SingleParams {

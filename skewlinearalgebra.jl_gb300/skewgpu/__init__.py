@@ -802,6 +802,33 @@ class BatchPlan:
                                                 _ptr(status)), "skew_batch_logabspf_d")
         return logpf, sign, status
 
+    def packed_size(self) -> int:
+        """Doubles in the packed layout of the batch (sum of n^2)."""
+        return int((self.sizes * self.sizes).sum())
+
+    def logabspfaffian_host(self, A_host: torch.Tensor, grad_host: Optional[torch.Tensor] = None,
+                            logpf: Optional[torch.Tensor] = None, sign: Optional[torch.Tensor] = None,
+                            status: Optional[torch.Tensor] = None):
+        """log|Pf| (+ gradient) on host buffers (skew_batch_logabspf_host_d).  A_host and
+        grad_host are page-locked float64 CPU tensors holding the matrices back to back
+        (column-major, in plan order); the kernels read and write them directly.
+        Returns host tensors (logpf, sign, status) once the results are in host memory."""
+        total = self.packed_size()
+        for name, t in (("A_host", A_host), ("grad_host", grad_host)):
+            if t is None:
+                continue
+            if t.device.type != "cpu" or t.dtype != torch.float64 or not t.is_contiguous() or t.numel() != total:
+                raise ValueError(f"{name} must be a contiguous float64 CPU tensor of {total} elements")
+            if not t.is_pinned():
+                raise ValueError(f"{name} must be page-locked (pin_memory())")
+        logpf = torch.empty(self.count, dtype=torch.float64) if logpf is None else logpf
+        sign = torch.empty(self.count, dtype=torch.float64) if sign is None else sign
+        status = torch.empty(self.count, dtype=torch.int32) if status is None else status
+        self._h.bind()
+        check(_lib.load().skew_batch_logabspf_host_d(self.plan, _ptr(A_host), _ptr(grad_host), _ptr(logpf),
+                                                     _ptr(sign), _ptr(status)), "skew_batch_logabspf_host_d")
+        return logpf, sign, status
+
     def eigen(self, A_ptrs, val_ptrs, vr_ptrs, vi_ptrs, status=None):
         status = torch.empty(self.count, dtype=torch.int32, device="cuda") if status is None else status
         self._h.bind()

@@ -44,6 +44,7 @@ SIGNATURES = {
     "skew_batch_plan_create": (_int, [_vp, ctypes.POINTER(_i64), _i64, ctypes.POINTER(_vp)]),
     "skew_batch_plan_destroy": (_int, [_vp]),
     "skew_batch_logabspf_d": (_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
+    "skew_batch_logabspf_host_d": (_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "skew_batch_eigvals_d": (_int, [_vp, _vp, _vp, _vp]),
     "skew_batch_eigen_d": (_int, [_vp, _vp, _vp, _vp, _vp, _vp]),
     "skew_batch_exp_d": (_int, [_vp, _vp, _vp, _vp]),

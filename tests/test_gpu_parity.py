@@ -1,6 +1,6 @@
 """GPU parity: libskewgpu (through its C ABI) against the oracle.
 
-Tolerances (the benchmark spec): log|Pf| and eigenvalues within 1e-11 relative of the
+Tolerances: log|Pf| and eigenvalues within 1e-11 relative of the
 binary128 oracle (eigenvalues normwise: max |lambda - lambda*| / max |lambda*|),
 Pfaffian sign exactly equal, gradients within 1e-8 relative (normwise).
 """
