@@ -34,6 +34,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "skewlinearalgebra.jl_gb300"))
 
+# dram__bytes_read.sum + dram__bytes_write.sum over the six batch_kernel launches of one
+# step of the default workload (4096 matrices, even n in [16, 256]), from one ncu capture
+STEP_DRAM_BYTES = 45_180_101_632
 METRIC = "batched log|Pf|+grad matrices/s & n=8192 hessenberg GFLOP/s vs plain GPU, err≤1e-11"
 UNIT = "matrices/s"
 COUNT = 4096
@@ -410,7 +413,10 @@ def main():
                     "staged_copies": {"value": staged_value, "note": "whole-batch cudaMemcpyAsync in and out "
                                       "around skew_batch_logabspf_d on one stream"}},
             "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
-                         "frac": achieved_tflops / fp64_peak, "traffic": None,
+                         "frac": achieved_tflops / fp64_peak, "traffic": STEP_DRAM_BYTES if (count, args.nmin, args.nmax) == (COUNT, NMIN, NMAX) else None,
+                         "traffic_unit": "bytes per step (DRAM read + write, ncu capture of the default "
+                                         "workload; profiles/batch_kernel_dram_traffic_4096_mixed.md)",
+                         "algorithmic_bytes_per_step": int(2 * total * 8),
                          "peak_source": "FP64 DFMA peak measured live by skew_measure_fp64_peak "
                                         "(MEASURED_PEAKS.json has no FP64 figure)",
                          "algorithmic_flops_per_step": flops, "kernel": "batch_pf_kernel"},
