@@ -127,16 +127,19 @@ SKEW_API int skew_eigvals_noalloc_d(double* A, int64_t n, int64_t lda, double* v
 
 /* LA.eigen!(A::SkewHermitian{Float64})  eigen.jl:338-360 (skeweigen! + skewtrieigen_divided!).
  * vals_im[n] in the reference's order; eigenvectors V = Vr + i*Vi (n x n each).  A is
- * destroyed.  Requires lda == ldv == n and n <= 1024 (else SKEW_UNSUPPORTED). */
+ * destroyed.  n <= 1024: lda == ldv == n.  n > 1024 (up to 32768): blocked reduction,
+ * bisection and twisted-factorisation vectors, values sorted descending (the reference's
+ * own fallback formulation, skeweigen.jl:470-489); lda, ldv >= n. */
 SKEW_API int skew_eigen_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,
                  int64_t ldv, int* info);
 
 /* Base.exp(A::SkewHermitian{Float64})  exp.jl:3-35, :48.  E (n x n) = exp(A). A destroyed.
- * Requires lda == lde == n and n <= 1024. */
+ * Requires lda == lde == n.  Above n = 1024 the eigenpairs come from the large-matrix path
+ * of skew_eigen_d (their order does not change the function). */
 SKEW_API int skew_exp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* E, int64_t lde, int* info);
 
 /* Base.cis(A::SkewHermitian{Float64})  exp.jl:99-110, :204.  C = cis(A) = exp(iA), Hermitian,
- * ComplexF64 interleaved (re, im).  A destroyed.  Requires lda == ldc == n and n <= 1024. */
+ * ComplexF64 interleaved (re, im).  A destroyed.  Requires lda == ldc == n (any n, as skew_exp_d). */
 SKEW_API int skew_cis_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* C, int64_t ldc, int* info);
 
 /* ---------------------------------------------------------------------------
@@ -187,7 +190,7 @@ SKEW_API int skew_batch_exp_vjp_d(skew_batch_plan_t plan, const double* const* A
                                   double* const* G, int* status);
 
 /* Single-matrix adjoint of exp (no reference counterpart): G = d<Cbar, exp(A)>/dA.
- * A is destroyed; lda, ldg must equal n (n <= 1024). */
+ * A is destroyed; lda, ldg must equal n (any n, as skew_exp_d). */
 SKEW_API int skew_exp_vjp_d(skew_handle_t h, double* A, int64_t n, int64_t lda, const double* Cbar, double* G,
                             int64_t ldg, int* info);
 
@@ -245,7 +248,7 @@ SKEW_API int skew_batch_exp_vjp_z(skew_handle_t h, const double* A, int64_t n, i
                                   double* G, int* status);
 
 /* Base.cos/sin/sinh/cosh/tan/tanh/cot/coth/log(A::SkewHermitian{Float64})  exp.jl:50-283
- * (and exp): F = f(A) (real n x n, ldf).  A is destroyed; lda == ldf == n, n <= 1024. */
+ * (and exp): F = f(A) (real n x n, ldf).  A is destroyed; lda == ldf == n (any n, as skew_exp_d). */
 SKEW_API int skew_func_d(skew_handle_t h, double* A, int64_t n, int64_t lda, int func, double* F, int64_t ldf,
                          int* info);
 /* The same for every matrix of a batch plan: F[b] (n[b] x n[b], leading dimension n[b]). */
@@ -311,7 +314,8 @@ SKEW_API int skew_tridiag_eigvals_d(skew_handle_t h, const double* ev, int64_t n
  * (ldv == n for n <= 1024); larger n: bisection and twisted vectors, values descending. */
 SKEW_API int skew_tridiag_eigen_d(skew_handle_t h, const double* ev, int64_t n, double* vals_im, double* Vr,
                                   double* Vi, int64_t ldv, int* info);
-/* exp.jl functions of a SkewHermTridiagonal{Float64} (n <= 1024): F = f(T), ldf == n. */
+/* exp.jl functions of a SkewHermTridiagonal{Float64}: F = f(T), ldf == n (above n = 1024 the
+ * eigenpairs come from bisection and twisted vectors, as skew_tridiag_eigen_d). */
 SKEW_API int skew_tridiag_func_d(skew_handle_t h, const double* ev, int64_t n, int func, double* F, int64_t ldf,
                                  int* info);
 /* LA.eigvals! / LA.eigen!(::SkewHermTridiagonal{ComplexF64})  tridiag.jl:462-468, :508-515: ev[n-1]

@@ -1018,12 +1018,18 @@ static int single_plan(skew_handle_t h, int64_t n, skew_batch_plan_t* out) {
   return SKEW_OK;
 }
 
+static int func_large(skew_handle_t h, double* A, const double* ev, int64_t n, double* out, const double* cot,
+                      int mode, int func, int* info);
+
 static int single_func(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, double* Vr, double* Vi,
                        int64_t ldv, double* out, int64_t ldo, const double* cot, int mode, int* info,
                        int func = SKEW_FUNC_EXP) {
   if (!h || n < 1 || !A || lda != n || (ldv && ldv != n) || (ldo && ldo != n)) return n < 1 ? SKEW_BAD_ARG
                                                                                             : SKEW_UNSUPPORTED;
-  if (n > kSingleMax) return SKEW_UNSUPPORTED;
+  if (n > kSingleMax) {
+    if (mode < 0) return SKEW_UNSUPPORTED;  // eigen of large matrices: eigen_large
+    return func_large(h, A, nullptr, n, out, cot, mode, func, info);
+  }
   skew_batch_plan_t P = nullptr;
   int s = single_plan(h, n, &P);
   if (s) return s;
@@ -1063,6 +1069,58 @@ static int eigen_large(skew_handle_t h, double* A, int64_t n, int64_t lda, doubl
   if (st) return st;
   CK(launch_tridiag_bisect(ev, (int)n, vals_im, bp, h->stream));
   CK(large_eigen_vectors(A, lda, (int)n, tau, ev, vals_im, bp, Vr, Vi, ldv, lws, h->stream));
+  return SKEW_OK;
+}
+
+// exp, cis, the other matrix functions and the exp adjoint of one large matrix
+// (n > 1024): the eigenpairs come from eigen_large (dense A, destroyed) or from
+// bisection and twisted vectors of the tridiagonal ev; then the element-wise step
+// and the tiled products of the batched path run on them as a batch of one.  The
+// eigenvalue order (descending here) does not change these functions.
+// Handle aux layout (doubles): [Vr n^2][Vi n^2][work 4 n^2][vals n][8 pointers][n, status].
+static int func_large(skew_handle_t h, double* A, const double* ev, int64_t n, double* out, const double* cot,
+                      int mode, int func, int* info) {
+  if (!h || !out || (mode == 2 && !cot)) return SKEW_BAD_ARG;
+  if (n > (1LL << 15)) return SKEW_UNSUPPORTED;
+  const size_t nn = (size_t)n * (size_t)n;
+  int st = ensure_aux(h, sizeof(double) * (6 * nn + (size_t)n + 8 + 2));
+  if (st) return st;
+  cudaStream_t s = h->stream;
+  double* Vr = (double*)h->aux;
+  double* Vi = Vr + nn;
+  double* work = Vi + nn;
+  double* vals = work + 4 * nn;
+  double** ptrs = (double**)(vals + n);  // [0] Vr, [1] Vi, [2] vals, [3] work, [4] out, [5] cot
+  int32_t* dn = (int32_t*)(ptrs + 8);
+  int* status = (int*)(dn + 1);
+  const int32_t n32 = (int32_t)n;
+  CK(cudaMemcpyAsync(dn, &n32, sizeof(int32_t), cudaMemcpyHostToDevice, s));  // pageable: staged before return
+  CK(cudaMemsetAsync(status, 0, sizeof(int), s));
+  if (A) {
+    st = eigen_large(h, A, n, n, vals, Vr, Vi, n, status);
+  } else {
+    st = skew_tridiag_eigen_d(h, ev, n, vals, Vr, Vi, n, status);
+  }
+  if (st) return st;
+  set8_kernel<<<1, 1, 0, s>>>(ptrs, Vr, Vi, vals, work, out, const_cast<double*>(cot), nullptr, nullptr);
+  CK(cudaGetLastError());
+  EigenBatch E{};
+  E.count = 1;
+  E.nmax = (int32_t)n;
+  E.n = dn;
+  E.status = status;
+  E.vals = ptrs + 2;
+  E.Vr = ptrs;
+  E.Vi = ptrs + 1;
+  E.pwork = ptrs + 3;
+  E.out = ptrs + 4;
+  E.cot = (const double* const*)(ptrs + 5);
+  E.func = func;
+  CK(launch_eigen_func(E, mode, s));
+  if (info) {
+    copy_status_kernel<<<1, 1, 0, s>>>(status, info);
+    CK(cudaGetLastError());
+  }
   return SKEW_OK;
 }
 
@@ -1574,7 +1632,7 @@ int skew_tridiag_eigen_d(skew_handle_t h, const double* ev, int64_t n, double* v
 int skew_tridiag_func_d(skew_handle_t h, const double* ev, int64_t n, int func, double* F, int64_t ldf, int* info) {
   if (!h || n < 1 || (n > 1 && !ev) || !F || ldf != n || func < SKEW_FUNC_EXP || func > SKEW_FUNC_LOG)
     return SKEW_BAD_ARG;
-  if (n > kSingleMax) return SKEW_UNSUPPORTED;
+  if (n > kSingleMax) return func_large(h, nullptr, ev, n, F, nullptr, 0, func, info);
   skew_batch_plan_t P = nullptr;
   int st = single_plan(h, n, &P);
   if (st) return st;
