@@ -591,22 +591,26 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
     __syncthreads();
     // 6. G[i,j] += V_i . Z'_j - Z'_i . V_j for i >= r0, j < i; mirrored.
     //    Items: (row strip of 32, column block of 32) on or below the diagonal.
+    //    Strip si holds rows [n - 32(si+1), n - 32 si) and the columns before its
+    //    last row.  Aligned to the last row, the partial strip is the one next to
+    //    r0, which has the fewest columns: a warp instruction costs the FP64 pipe
+    //    the same with idle lanes, so they belong in the shortest strip.
     {
       const int S = (m + 31) >> 5;
       int total = 0;
-      for (int si = 0; si < S; si++) total += (min(n, r0 + 32 * (si + 1)) - 1 + 31) / 32;
+      for (int si = 0; si < S; si++) total += (n - 32 * si - 1 + 31) / 32;
       for (int item = w; item < total; item += NW) {
         int si = 0, rem = item;
         for (;;) {
-          const int nbk = (min(n, r0 + 32 * (si + 1)) - 1 + 31) / 32;
+          const int nbk = (n - 32 * si - 1 + 31) / 32;
           if (rem < nbk) break;
           rem -= nbk;
           si++;
         }
-        const int i = r0 + 32 * si + lane;
+        const int i = n - 32 * (si + 1) + lane;  // below r0 in the partial strip: idle
         const int jb = rem * 32;
-        const int je = min(jb + 32, min(n, r0 + 32 * (si + 1)) - 1);
-        if (i < n) {
+        const int je = min(jb + 32, n - 32 * si - 1);
+        if (i >= r0) {
           double vi[GNB], zi[GNB];
 #pragma unroll
           for (int l = 0; l < GNB; l++) {
