@@ -302,6 +302,11 @@ SKEW_API int skew_pfaffian_z(skew_handle_t h, double* A, int64_t n, int64_t lda,
  * phase[2 count], pf[2 count] (each nullable, not all), status[count] (nullable). */
 SKEW_API int skew_batch_logabspf_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* logpf,
                                    double* phase, double* pf, int check, int* status);
+/* The same on host buffers: A in page-locked host memory (else SKEW_BAD_ARG), read by
+ * the kernels over the host link; logpf, phase, pf, status are host arrays, filled when
+ * the call returns (it synchronises the handle's stream). */
+SKEW_API int skew_batch_logabspf_host_z(skew_handle_t h, const double* A, int64_t n, int64_t count,
+                                        double* logpf, double* phase, double* pf, int check, int* status);
 
 /* ---------------------------------------------------------------------------
  * SkewHermTridiagonal inputs (tridiag.jl): ev[n-1] the subdiagonal on the device, no

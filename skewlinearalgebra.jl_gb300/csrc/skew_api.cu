@@ -1447,7 +1447,7 @@ int skew_batch_logabspf_z(skew_handle_t h, const double* A, int64_t n, int64_t c
     double* W = (double*)h->ws;
     if (status) CK(cudaMemsetAsync(status, 0, sizeof(int) * count, h->stream));
     for (int64_t b = 0; b < count; b++) {
-      CK(cudaMemcpyAsync(W, A + b * mat, sizeof(double) * mat, cudaMemcpyDeviceToDevice, h->stream));
+      CK(cudaMemcpyAsync(W, A + b * mat, sizeof(double) * mat, cudaMemcpyDefault, h->stream));
       CK(launch_pfz_grid((zc*)W, n, nn, check, logpf ? logpf + b : nullptr, phase ? phase + 2 * b : nullptr,
                          pf ? pf + 2 * b : nullptr, status ? status + b : nullptr, W + mat, h->sms, h->stream));
     }
@@ -1474,6 +1474,39 @@ int skew_batch_logabspf_z(skew_handle_t h, const double* A, int64_t n, int64_t c
     P.gws = (zc*)h->ws;
   }
   CK(launch_pfz_cta(P, (int)grid, h->stream));
+  return SKEW_OK;
+}
+
+// The same on host buffers: A (count x n x n ComplexF64, column-major, back to back)
+// in page-locked host memory, read by the kernels over the host link; the results
+// are copied to the host arrays given (any of logpf, phase, pf, status may be NULL,
+// not all of the first three) and the call returns when they are there.
+int skew_batch_logabspf_host_z(skew_handle_t h, const double* A, int64_t n, int64_t count, double* logpf,
+                               double* phase, double* pf, int check, int* status) {
+  if (!h || n < 0 || count < 0 || (count > 0 && n > 0 && !A)) return SKEW_BAD_ARG;
+  if (!logpf && !phase && !pf) return SKEW_BAD_ARG;
+  if (n > (1LL << 15) || count > INT32_MAX) return SKEW_UNSUPPORTED;
+  if (count == 0) return SKEW_OK;
+  void* dA = nullptr;
+  if (n > 0) {
+    const int st = host_mapped(A, sizeof(double) * 2 * (size_t)n * (size_t)n * (size_t)count, &dA);
+    if (st) return st;
+  }
+  int st = ensure_aux(h, sizeof(double) * 5 * (size_t)count + sizeof(int) * (size_t)count);
+  if (st) return st;
+  double* d_lp = (double*)h->aux;
+  double* d_ph = d_lp + count;
+  double* d_pf = d_ph + 2 * count;
+  int* d_st = (int*)(d_pf + 2 * count);
+  st = skew_batch_logabspf_z(h, (const double*)dA, n, count, logpf ? d_lp : nullptr, phase ? d_ph : nullptr,
+                             pf ? d_pf : nullptr, check, d_st);
+  if (st) return st;
+  cudaStream_t s = h->stream;
+  if (logpf) CK(cudaMemcpyAsync(logpf, d_lp, sizeof(double) * count, cudaMemcpyDeviceToHost, s));
+  if (phase) CK(cudaMemcpyAsync(phase, d_ph, sizeof(double) * 2 * count, cudaMemcpyDeviceToHost, s));
+  if (pf) CK(cudaMemcpyAsync(pf, d_pf, sizeof(double) * 2 * count, cudaMemcpyDeviceToHost, s));
+  if (status) CK(cudaMemcpyAsync(status, d_st, sizeof(int) * count, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
   return SKEW_OK;
 }
 

@@ -268,7 +268,9 @@ __global__ void __launch_bounds__(NT) pfz_cta_kernel(PfzParams P) {
 
   for (int b = blockIdx.x; b < P.count; b += gridDim.x) {
     const zc* A = P.A + (int64_t)b * P.stride;
-    if (P.check) {  // isskewsymmetric(A): A == -transpose(A) elementwise (skewhermitian.jl:101-110)
+    // isskewsymmetric(A): A == -transpose(A) elementwise (skewhermitian.jl:101-110).
+    // Even n > 0 checks after the copy below (every entry of A read once, coalesced).
+    if (P.check && ((n & 1) || n == 0)) {
       int bad = 0;
       for (int64_t e = threadIdx.x; e < (int64_t)n * n; e += NT) {
         const int j = (int)(e / n), i = (int)(e - (int64_t)j * n);
@@ -302,6 +304,21 @@ __global__ void __launch_bounds__(NT) pfz_cta_kernel(PfzParams P) {
           const int i = i0 + 32 * r + lane;
           if (i < n) dst[i] = zc{v[r].x, v[r].y};
         }
+      }
+    }
+    if (P.check) {  // the upper triangle and the diagonal of A against the copied lower triangle
+      __syncthreads();
+      int bad = 0;
+      for (int j = warp; j < n; j += NW) {
+        const zc* col = A + (int64_t)j * P.lda;
+        for (int i = lane; i <= j; i += 32) {
+          const zc a = col[i];
+          bad |= !neg_equal(a, i == j ? a : L[pk(n, j, i)]);
+        }
+      }
+      if (__syncthreads_or(bad)) {
+        if (warp == 0) pf_finish_warp(piv, 0, 0, SKEW_NOT_SKEW, b, P.logpf, P.phase, P.pf, P.status);
+        continue;
       }
     }
     if (threadIdx.x == 0) s_swaps = 0;

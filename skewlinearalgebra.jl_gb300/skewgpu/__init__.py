@@ -752,6 +752,26 @@ def batch_logabspfaffian_complex(mats, check_skew: bool = True):
     return lp.cpu().numpy(), ph.cpu().numpy(), pf.cpu().numpy(), st.cpu().numpy()
 
 
+def batch_logabspfaffian_complex_host(A_host: torch.Tensor, check_skew: bool = True):
+    """batch_logabspfaffian_complex on host memory (skew_batch_logabspf_host_z): ``A_host``
+    is a page-locked complex128 CPU tensor count x n x n holding each matrix column-major;
+    the kernels read it directly.  Returns numpy arrays (log|Pf|, cis(phase), Pf, status)."""
+    if A_host.device.type != "cpu" or A_host.dtype != torch.complex128 or A_host.dim() != 3 \
+            or not A_host.is_contiguous():
+        raise ValueError("A_host must be a contiguous complex128 CPU tensor count x n x n")
+    if not A_host.is_pinned():
+        raise ValueError("A_host must be page-locked (pin_memory())")
+    count, n = A_host.shape[0], A_host.shape[1]
+    lp = torch.zeros(count, dtype=torch.float64)
+    ph = torch.zeros(count, dtype=torch.complex128)
+    pf = torch.zeros(count, dtype=torch.complex128)
+    st = torch.zeros(count, dtype=torch.int32)
+    h = handle().bind()
+    check(_lib.load().skew_batch_logabspf_host_z(h, _ptr(A_host), n, count, _ptr(lp), _ptr(ph), _ptr(pf),
+                                                 int(check_skew), _ptr(st)), "batch_logabspfaffian_complex_host")
+    return lp.numpy(), ph.numpy(), pf.numpy(), st.numpy()
+
+
 def measure_fp64_peak() -> float:
     t = ctypes.c_double()
     check(_lib.load().skew_measure_fp64_peak(handle().bind(), ctypes.byref(t)), "measure_fp64_peak")

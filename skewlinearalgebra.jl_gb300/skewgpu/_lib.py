@@ -82,6 +82,7 @@ SIGNATURES = {
     "skew_logabspf_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _int, _vp]),
     "skew_pfaffian_z": (_int, [_vp, _vp, _i64, _i64, _vp, _int, _vp]),
     "skew_batch_logabspf_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
+    "skew_batch_logabspf_host_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
     "skew_measure_fp64_peak": (_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
 }
 

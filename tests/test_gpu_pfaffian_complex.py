@@ -192,3 +192,36 @@ def test_scaled_entries(skewgpu, oracle):
         ls, ps = skewgpu.logabspfaffian(A * s)
         assert abs(ls - (l0 + n / 2 * np.log(s))) <= 1e-11 * abs(ls)
         assert abs(ps - p0) <= 1e-12
+
+
+@pytest.mark.parametrize("n,count", [(8, 50), (64, 40), (170, 12), (33, 7), (200, 5)])
+def test_batch_host_buffers(skewgpu, n, count):
+    """skew_batch_logabspf_host_z: the same kernels reading page-locked host memory
+    (shared-memory, global-slot and per-matrix grid paths, odd n) give bit-identical
+    results to the device-resident call; a non-skew-symmetric matrix is reported in
+    both (status SKEW_NOT_SKEW); pageable input is refused before any launch."""
+    import ctypes
+
+    import torch
+    from skewgpu import _lib
+
+    mats = [complex_skew(n, 3000 * n + b) for b in range(count)]
+    if count > 3:
+        mats[2] = mats[2].copy()
+        mats[2][0, 1] += 1e-3  # no longer skew-symmetric
+    lp, ph, pf, st = skewgpu.batch_logabspfaffian_complex(mats)
+    host = np.ascontiguousarray(np.stack([m.T for m in mats]))  # column-major storage
+    pinned = torch.from_numpy(host).pin_memory()
+    lph, phh, pfh, sth = skewgpu.batch_logabspfaffian_complex_host(pinned)
+    np.testing.assert_array_equal(sth, st)
+    np.testing.assert_array_equal(lph, lp)
+    np.testing.assert_array_equal(phh, ph)
+    np.testing.assert_array_equal(pfh, pf)
+    if count > 3:
+        assert st[2] == 1
+    with pytest.raises(ValueError):
+        skewgpu.batch_logabspfaffian_complex_host(torch.from_numpy(host))
+    out = np.zeros(count)
+    rc = _lib.load().skew_batch_logabspf_host_z(skewgpu.handle().bind(), ctypes.c_void_p(host.ctypes.data), n,
+                                                count, ctypes.c_void_p(out.ctypes.data), None, None, 1, None)
+    assert rc == _lib.SKEW_BAD_ARG
