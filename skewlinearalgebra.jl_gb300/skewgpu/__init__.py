@@ -844,6 +844,10 @@ class BatchPlan:
         logpf = torch.empty(self.count, dtype=torch.float64) if logpf is None else logpf
         sign = torch.empty(self.count, dtype=torch.float64) if sign is None else sign
         status = torch.empty(self.count, dtype=torch.int32) if status is None else status
+        for name, t, dt in (("logpf", logpf, torch.float64), ("sign", sign, torch.float64),
+                            ("status", status, torch.int32)):
+            if t.device.type != "cpu" or t.dtype != dt or not t.is_contiguous() or t.numel() != self.count:
+                raise ValueError(f"{name} must be a contiguous {dt} CPU tensor of {self.count} elements")
         self._h.bind()
         check(_lib.load().skew_batch_logabspf_host_d(self.plan, _ptr(A_host), _ptr(grad_host), _ptr(logpf),
                                                      _ptr(sign), _ptr(status)), "skew_batch_logabspf_host_d")
