@@ -62,3 +62,56 @@ def test_no_gpu_is_an_error_not_a_crash(lib):
     h = ctypes.c_void_p()
     st = lib.skew_create(ctypes.byref(h))
     assert st == 4  # SKEW_CUDA_ERROR
+
+
+def header_param_types():
+    """name -> list of parameter type strings, from the header's declarations."""
+    txt = open(HEADER).read()
+    txt = re.sub(r"/\*.*?\*/", " ", txt, flags=re.S)
+    out = {}
+    for m in re.finditer(r"SKEW_API\s+[^;(]*?\b(skew_\w+)\s*\(([^)]*)\)\s*;", txt, flags=re.S):
+        params = " ".join(m.group(2).split())
+        if params in ("", "void"):
+            out[m.group(1)] = []
+        else:
+            out[m.group(1)] = [p.strip() for p in params.split(",")]
+    return out
+
+
+def _ctype_kind(t):
+    import ctypes as C
+
+    if t in (C.c_int64,):
+        return "int64"
+    if t in (C.c_int,):
+        return "int"
+    if t in (C.c_double,):
+        return "double"
+    return "ptr"
+
+
+def _decl_kind(p):
+    p = p.strip()
+    if "*" in p or p.split()[0] in ("skew_handle_t", "skew_batch_plan_t", "skew_stream_t"):
+        return "ptr"
+    if p.startswith("int64_t"):
+        return "int64"
+    if p.startswith("int"):
+        return "int"
+    if p.startswith("double"):
+        return "double"
+    return "?"
+
+
+def test_python_signatures_match_header():
+    """Every ctypes signature has the header's arity and argument kinds (pointer,
+    int, int64, double), so a call through the binding passes what the C side reads."""
+    from skewgpu import _lib as L
+
+    decl = header_param_types()
+    assert sorted(decl) == header_functions()
+    for name, (_, args) in L.SIGNATURES.items():
+        want = [_decl_kind(p) for p in decl[name]]
+        got = [_ctype_kind(a) for a in args]
+        assert "?" not in want, (name, decl[name])
+        assert got == want, (name, decl[name], got)
