@@ -115,3 +115,23 @@ def test_python_signatures_match_header():
         got = [_ctype_kind(a) for a in args]
         assert "?" not in want, (name, decl[name])
         assert got == want, (name, decl[name], got)
+
+
+def test_plain_c_caller(lib, tmp_path):
+    """include/skewgpu.h compiles as C99 (-Wall -Wextra -pedantic -Werror) and a C
+    program links against libskewgpu.so and runs: without a GPU skew_create returns a
+    status instead of crashing; with one, a bad argument is rejected on the host."""
+    import shutil
+    import subprocess
+
+    gcc = shutil.which("gcc")
+    if gcc is None:
+        pytest.skip("no gcc")
+    libdir = os.path.dirname(lib._name)
+    exe = str(tmp_path / "caller")
+    src = os.path.join(ROOT, "tests", "c_caller", "caller.c")
+    subprocess.run([gcc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    src, "-L", libdir, "-lskewgpu", "-Wl,-rpath," + libdir, "-o", exe], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "skew_create ->" in r.stdout
