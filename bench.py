@@ -62,6 +62,70 @@ def packed_inputs(sizes, seed=SEED, rank=0):
     return buf, offs
 
 
+def dense_skew_input(n):
+    """The single dense real matrix of size n: A = (B - B^T)/2 with B iid N(0,1),
+    seeded by n (the n = 512 and n = 8192 single-matrix workloads)."""
+    rng = np.random.default_rng(SEED + n)
+    B = rng.standard_normal((n, n))
+    return (B - B.T) / 2
+
+
+def dense_skewh_input(n):
+    """The single dense ComplexF64 skew-Hermitian matrix of size n: A = (C - C^H)/2
+    with the real and imaginary parts of C iid N(0,1), seeded by n."""
+    rng = np.random.default_rng(SEED + 3 * n)
+    C = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    return (C - C.conj().T) / 2, rng
+
+
+def pfaffian_adjoint_inputs(count=1024, n=128):
+    """The batched Pfaffian-adjoint workload: (B - B^T)/2 + 0.5 J with B iid
+    N(0, 1/n) and J the canonical symplectic form, packed column-major back to
+    back, and the loss weights w ~ U(-1, 1)."""
+    rng = np.random.default_rng(SEED + 128)
+    J = np.kron(np.eye(n // 2), np.array([[0.0, 1.0], [-1.0, 0.0]]))
+    buf = np.empty(count * n * n)
+    for b in range(count):
+        B = rng.standard_normal((n, n)) / np.sqrt(n)
+        buf[b * n * n:(b + 1) * n * n] = ((B - B.T) / 2 + 0.5 * J).ravel(order="F")
+    w = rng.uniform(-1.0, 1.0, count)
+    return buf, w
+
+
+def exp_adjoint_inputs(count=512):
+    """The real exp-adjoint workload: n uniform in {32, 64, ..., 512}, each
+    (B - B^T)/2 scaled to a spectral radius ~ U(0.5, 8), cotangents iid N(0,1);
+    returns (sizes, offsets, packed inputs, packed cotangents)."""
+    rng = np.random.default_rng(SEED + 5)
+    sizes = (32 * rng.integers(1, 17, count)).astype(np.int64)
+    offs = np.zeros(count, dtype=np.int64)
+    offs[1:] = np.cumsum(sizes[:-1] ** 2)
+    total = int(offs[-1] + sizes[-1] ** 2)
+    buf = np.empty(total)
+    cot = rng.standard_normal(total)
+    for b, n in enumerate(sizes):
+        B = rng.standard_normal((n, n))
+        A = (B - B.T) / 2
+        rho = np.abs(np.linalg.eigvalsh(1j * A)).max()
+        A *= rng.uniform(0.5, 8.0) / rho
+        buf[offs[b]:offs[b] + n * n] = A.ravel(order="F")
+    return sizes, offs, buf, cot
+
+
+def complex_exp_adjoint_inputs(count=64, n=256):
+    """The complex exp-adjoint workload: ComplexF64 skew-Hermitian (C - C^H)/2
+    scaled to a spectral radius ~ U(0.5, 8), cotangents iid complex N(0,1)."""
+    rng = np.random.default_rng(SEED + 64)
+    mats, cots = [], []
+    for _ in range(count):
+        C = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+        A = (C - C.conj().T) / 2
+        A *= rng.uniform(0.5, 8.0) / np.abs(np.linalg.eigvalsh(1j * A)).max()
+        mats.append(A)
+        cots.append(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    return mats, cots
+
+
 def flops_per_matrix(n):
     """Algorithmic FP64 work: Householder tridiagonalisation 4/3 n^3 plus the
     gradient Q (-1/2 T^{-1}) Q^T by two-sided reflector application 2 n^3."""
@@ -149,11 +213,13 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": sec * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded)",
         "config": {"workload": f"batched_logabspf_grad_{COUNT}x_even_n{NMIN}-{NMAX}", "count": COUNT,
-                   "n_range": [NMIN, NMAX], "sample": sample},
+                   "n_range": [NMIN, NMAX], "entries": "(B-B^T)/2, B~N(0,1/n)", "sample": sample},
         "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port",
-                         "sample": f"first {sample} matrices of the workload per step; Julia is absent on the box, "
-                                   "so the oracle's FP64 restatement of SkewLinearAlgebra.jl (logabspfaffian) "
-                                   "plus an FP64 Gauss-Jordan inverse for the gradient, OpenMP over matrices"},
+                         "sample": (f"all {sample} matrices of the workload per step" if sample >= COUNT else
+                                    f"first {sample} matrices of the workload per step") +
+                                   "; Julia is absent on the box, so the oracle's FP64 restatement of "
+                                   "SkewLinearAlgebra.jl (logabspfaffian) plus an FP64 Gauss-Jordan inverse for the "
+                                   "gradient, OpenMP over matrices, scalar C++ -O3 without BLAS"},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -166,7 +232,7 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
-    ap.add_argument("--cpu-sample", type=int, default=1024)
+    ap.add_argument("--cpu-sample", type=int, default=COUNT)
     ap.add_argument("--plain-sample", type=int, default=256)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--count", type=int, default=COUNT, help="matrices per step (profiling cases)")
@@ -303,7 +369,7 @@ def main():
     staged_sec = replicas.max_over_ranks(e0.elapsed_time(e1) / 1e3, dist, "cuda")
     staged_value = replicas.weak_scaling_throughput(count, world, e2e_steps, staged_sec)
 
-    # roofline of the dominant kernel (batch_pf_kernel: every launch of a step)
+    # roofline of the dominant kernel (batch_kernel: every launch of a step)
     flops = float(flops_per_matrix(sizes).sum())
     achieved_tflops = flops / (ms_dev / args.steps / 1e3) / 1e12
 
@@ -370,8 +436,9 @@ def main():
         nthreads = os.cpu_count() or 1
         cval, (clp, csg, cgrad), _ = cpu_reference(sizes, 1, 0, args.cpu_sample, nthreads, rank)
         cpu = {"value": cval, "unit": UNIT, "cores": nthreads, "kind": "port",
-               "sample": f"first {args.cpu_sample} matrices of the workload, one pass; oracle FP64 restatement of "
-                         "logabspfaffian + FP64 Gauss-Jordan gradient, OpenMP over matrices"}
+               "sample": f"first {args.cpu_sample} of the {count} matrices of the workload, one pass; oracle FP64 "
+                         "restatement of logabspfaffian + FP64 Gauss-Jordan gradient, OpenMP over matrices, "
+                         "scalar C++ -O3 without BLAS"}
         k = args.cpu_sample
         glp = logpf[:k].cpu().numpy()
         gsg = sign[:k].cpu().numpy()
@@ -414,12 +481,12 @@ def main():
                                       "around skew_batch_logabspf_d on one stream"}},
             "roofline": {"bound": "fp64", "achieved": achieved_tflops, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": achieved_tflops / fp64_peak, "traffic": STEP_DRAM_BYTES if (count, args.nmin, args.nmax) == (COUNT, NMIN, NMAX) else None,
-                         "traffic_unit": "bytes per step (DRAM read + write, ncu capture of the default "
-                                         "workload; profiles/batch_kernel_dram_traffic_4096_mixed.md)",
+                         "traffic_unit": "bytes per step (DRAM read + write of the step's batch_kernel "
+                                         "launches, one ncu capture of the default workload)",
                          "algorithmic_bytes_per_step": int(2 * total * 8),
                          "peak_source": "FP64 DFMA peak measured live by skew_measure_fp64_peak "
                                         "(MEASURED_PEAKS.json has no FP64 figure)",
-                         "algorithmic_flops_per_step": flops, "kernel": "batch_pf_kernel"},
+                         "algorithmic_flops_per_step": flops, "kernel": "batch_kernel"},
             "gpu_launches": int(args.steps * len(set(_bucket_ids(sizes)))),
             "clocks": clk,
             "wall_s": wall,
@@ -453,10 +520,7 @@ def bench_hessenberg_large(n, reps, fp64_peak):
 
     import skewgpu
 
-    rng = np.random.default_rng(SEED + 8192)
-    B = rng.standard_normal((n, n))
-    A = (B - B.T) / 2
-    del B
+    A = dense_skew_input(n)
     pristine = skewgpu.to_device(A)
     work = torch.empty_like(pristine)
     tau = torch.empty(n - 1, dtype=torch.float64, device="cuda")
@@ -498,10 +562,8 @@ def leg_eigen_large(n, fp64_peak, reps=1):
 
     import skewgpu
 
-    rng = np.random.default_rng(SEED + n)
-    B = rng.standard_normal((n, n))
-    A = (B - B.T) / 2
-    del B
+    A = dense_skew_input(n)
+    rng = np.random.default_rng(SEED + n + 1)
     pristine = skewgpu.to_device(A)
     work = torch.empty_like(pristine)
     vals = torch.empty(n, dtype=torch.float64, device="cuda")
@@ -533,7 +595,9 @@ def leg_eigen_large(n, fp64_peak, reps=1):
     Ac = torch.complex(At, torch.zeros_like(At))
     res = (Ac @ Vs - Vs * lam).abs().max().item() / vals.abs().max().item()
     orth = (Vs.conj().T @ Vs - torch.eye(16, dtype=Vs.dtype, device="cuda")).abs().max().item()
-    flops = (4.0 / 3.0 + 2.0) * n ** 3  # reduction + back-transformation of n real columns
+    # the work of this algorithm: reduction 4/3 n^3, back-transformation of the n real
+    # columns that carry the -sigma vectors (the +sigma ones are their conjugates) 2 n^3
+    flops = (4.0 / 3.0 + 2.0) * n ** 3
     return {"n": n, "ms": sec * 1e3, "algorithmic_flops": flops, "gflops": flops / sec / 1e9,
             "frac_fp64": flops / sec / 1e12 / fp64_peak, "reps": reps,
             "check_sample": {"pairs": 16, "max_residual_rel": res, "max_orthonormality_err": orth}}
@@ -550,10 +614,7 @@ def leg_complex_large(n, fp64_peak, reps=1):
 
     import skewgpu
 
-    rng = np.random.default_rng(SEED + 3 * n)
-    C = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
-    A = (C - C.conj().T) / 2
-    del C
+    A, rng = dense_skewh_input(n)
     pristine = skewgpu.to_device_complex(A)
     work = torch.empty_like(pristine)
     tau = torch.empty(n - 1, dtype=torch.complex128, device="cuda")
@@ -608,14 +669,7 @@ def leg_complex_exp_adjoint(fp64_peak, count=64, n=256, steps=3):
 
     import skewgpu
 
-    rng = np.random.default_rng(SEED + 64)
-    mats, cots = [], []
-    for _ in range(count):
-        C = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
-        A = (C - C.conj().T) / 2
-        A *= rng.uniform(0.5, 8.0) / np.abs(np.linalg.eigvalsh(1j * A)).max()
-        mats.append(A)
-        cots.append(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    mats, cots = complex_exp_adjoint_inputs(count, n)
     dA = skewgpu._stack_complex(mats)
     dC = skewgpu._stack_complex(cots)
     dG = torch.empty_like(dA)
@@ -638,8 +692,10 @@ def leg_complex_exp_adjoint(fp64_peak, count=64, n=256, steps=3):
     e1.record(stream)
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / 1e3 / steps
-    # reduction 16/3 n^3 + back-transformation 8 n^3 + four complex products 32 n^3 (real flops)
-    flops = count * (16.0 / 3.0 + 8.0 + 32.0) * n ** 3
+    # algorithmic work in real flops: reduction 16/3 n^3, back-transformation of the complex
+    # eigenvectors 8 n^3, the exp assembly V e^L V^H 8 n^3 and the adjoint's three complex
+    # products 24 n^3 (the real count (4/3 + 4 + 4 + 6) n^3 with complex arithmetic)
+    flops = count * (16.0 / 3.0 + 8.0 + 8.0 + 24.0) * n ** 3
     return {"value": count / sec, "unit": "matrices/s", "ms_per_step": sec * 1e3, "count": count, "n": n,
             "steps": steps, "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
             "status_ok": int((st.cpu().numpy() == 0).sum())}
@@ -808,7 +864,9 @@ def leg_plain_n512(fp64_peak, reps=5, cpu=True):
     """One real n=512 matrix, A = (B - B^T)/2 with B iid N(0,1): hessenberg,
     eigvals and logabspfaffian through the single-matrix C-ABI calls (median of
     reps, input restored outside the timed region), next to the oracle's FP64
-    restatement of the reference on one host core."""
+    restatement of the reference on one host core.  eigvals returns the values in
+    the reference's QR deflation order (the QR chain on one GPU thread);
+    eigvals_sorted is eigvals(A, 1:n), the same values sorted by bisection."""
     import ctypes
 
     import torch
@@ -816,9 +874,7 @@ def leg_plain_n512(fp64_peak, reps=5, cpu=True):
     import skewgpu
 
     n = 512
-    rng = np.random.default_rng(SEED + 512)
-    B = rng.standard_normal((n, n))
-    A = (B - B.T) / 2
+    A = dense_skew_input(n)
     pristine = skewgpu.to_device(A)
     work = torch.empty_like(pristine)
     tau = torch.empty(n - 1, dtype=torch.float64, device="cuda")
@@ -832,6 +888,7 @@ def leg_plain_n512(fp64_peak, reps=5, cpu=True):
     P = lambda t, off=0: ctypes.c_void_p(t.data_ptr() + off)  # noqa: E731
     calls = {
         "hessenberg": lambda: L.skew_hessenberg_d(h, P(work), n, n, P(tau), P(ev), P(info)),
+        "eigvals_sorted": lambda: L.skew_eigvals_irange_d(h, P(work), n, n, 1, n, P(vals), P(info)),
         "eigvals": lambda: L.skew_eigvals_d(h, P(work), n, n, P(vals), P(info)),
         "logabspfaffian": lambda: L.skew_logabspf_d(h, P(work), n, n, P(out2), P(out2, 8), 0, P(info)),
     }
@@ -865,7 +922,7 @@ def leg_plain_n512(fp64_peak, reps=5, cpu=True):
         g = out2.cpu().numpy()
         gv = vals.cpu().numpy()
         res["check"] = {"logpf_rel_vs_cpu": float(abs(g[0] - clp) / abs(clp)), "sign_equal": bool(g[1] == csg),
-                        "eigvals_rel_vs_cpu": float(np.abs(np.sort(gv) - np.sort(cv)).max() / np.abs(cv).max())}
+                        "eigvals_rel_vs_cpu_same_order": float(np.abs(gv - cv).max() / np.abs(cv).max())}
     return res
 
 
@@ -877,13 +934,8 @@ def leg_pfaffian_adjoint(fp64_peak, steps, count=1024, n=128):
 
     import skewgpu
 
-    rng = np.random.default_rng(SEED + 128)
-    J = np.kron(np.eye(n // 2), np.array([[0.0, 1.0], [-1.0, 0.0]]))
-    buf = np.empty(count * n * n)
-    for b in range(count):
-        B = rng.standard_normal((n, n)) / np.sqrt(n)
-        buf[b * n * n:(b + 1) * n * n] = ((B - B.T) / 2 + 0.5 * J).ravel(order="F")
-    w = torch.from_numpy(rng.uniform(-1.0, 1.0, count)).to("cuda")
+    buf, w_host = pfaffian_adjoint_inputs(count, n)
+    w = torch.from_numpy(w_host).to("cuda")
     d_in = torch.from_numpy(buf).to("cuda")
     d_g = torch.empty_like(d_in)
     offs = np.arange(count, dtype=np.int64) * n * n
@@ -919,9 +971,16 @@ def leg_pfaffian_adjoint(fp64_peak, steps, count=1024, n=128):
 
 
 def exp_adjoint_flops(n):
-    """Algorithmic FP64 work of one exp adjoint as computed: Householder reduction
-    4/3 n^3, back-transformation of Vr and Vi 4 n^3, and the twelve real n x n
-    products of the Daleckii-Krein assembly 24 n^3 (the QR chain is O(n^2))."""
+    """Algorithmic FP64 work of one exp adjoint: the eigendecomposition, reduction
+    4/3 n^3 and back-transformation of Vr and Vi 4 n^3; the exp assembly 4 n^3; the
+    Daleckii-Krein adjoint 6 n^3 (the QR chain is O(n^2))."""
+    n = np.asarray(n, dtype=np.float64)
+    return (4.0 / 3.0 + 4.0 + 4.0 + 6.0) * n ** 3
+
+
+def exp_adjoint_flops_executed(n):
+    """FP64 work the exp adjoint executes: reduction 4/3 n^3, back-transformation of
+    Vr and Vi 4 n^3, and the twelve real n x n products of the assembly 24 n^3."""
     n = np.asarray(n, dtype=np.float64)
     return (4.0 / 3.0 + 4.0 + 24.0) * n ** 3
 
@@ -934,19 +993,7 @@ def leg_exp_adjoint(fp64_peak, steps, count=512):
 
     import skewgpu
 
-    rng = np.random.default_rng(SEED + 5)
-    sizes = (32 * rng.integers(1, 17, count)).astype(np.int64)
-    offs = np.zeros(count, dtype=np.int64)
-    offs[1:] = np.cumsum(sizes[:-1] ** 2)
-    total = int(offs[-1] + sizes[-1] ** 2)
-    buf = np.empty(total)
-    cot = rng.standard_normal(total)
-    for b, n in enumerate(sizes):
-        B = rng.standard_normal((n, n))
-        A = (B - B.T) / 2
-        rho = np.abs(np.linalg.eigvalsh(1j * A)).max()
-        A *= rng.uniform(0.5, 8.0) / rho
-        buf[offs[b]:offs[b] + n * n] = A.ravel(order="F")
+    sizes, offs, buf, cot = exp_adjoint_inputs(count)
     d_in = torch.from_numpy(buf).to("cuda")
     d_c = torch.from_numpy(cot).to("cuda")
     d_g = torch.empty_like(d_in)
@@ -965,10 +1012,13 @@ def leg_exp_adjoint(fp64_peak, steps, count=512):
     torch.cuda.synchronize()
     sec = e0.elapsed_time(e1) / 1e3 / steps
     flops = float(exp_adjoint_flops(sizes).sum())
+    xflops = float(exp_adjoint_flops_executed(sizes).sum())
     s = st.cpu().numpy()
     plan.close()
     return {"value": count / sec, "unit": "matrices/s", "ms_per_step": sec * 1e3, "steps": steps,
             "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
+            "algorithmic_flops": flops, "algorithmic_flops_per_matrix": "(4/3 + 4 + 4 + 6) n^3",
+            "executed_flops": xflops, "frac_fp64_executed": xflops / sec / 1e12 / fp64_peak,
             "status_ok": int((s == 0).sum()), "status_fallback": int((s == 8).sum()),
             "complex_part": "reported separately as exp_adjoint_complex_64x256"}
 

@@ -74,6 +74,9 @@ def lib():
                                               ctypes.c_int]
         _lib.orc_batch_logabspf_grad_d.argtypes = [_D, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _I64, _D, _D,
                                                    _D, ctypes.c_int]
+        _lib.orc_batch_logabspf_fd.argtypes = [_D, ctypes.POINTER(_I64), ctypes.POINTER(_I64), _I64,
+                                               ctypes.POINTER(_I64), _I64, ctypes.c_double, ctypes.c_int, _D,
+                                               ctypes.c_int]
     return _lib
 
 
@@ -192,7 +195,7 @@ def skewtrieigen(ev):
 
 
 def eigen(A, quad: bool = False):
-    """eigen(::SkewHermitian{Float64}) (eigen.jl:338-360): (vals_im, Vr, Vi, status);
+    """eigen(::SkewHermitian{Float64}) (eigen.jl:75-97): (vals_im, Vr, Vi, status);
     eigenvectors are Vr + i Vi."""
     F = _fmat(A)
     n = F.shape[0]
@@ -296,6 +299,24 @@ def batch_logabspfaffian_grad_packed(buf, offs, ns, nthreads: int = 1):
                                     ns.ctypes.data_as(ctypes.POINTER(_I64)), count, _p(lp), _p(sg), _p(grad),
                                     int(nthreads))
     return lp, sg, grad
+
+
+def batch_logabspfaffian_fd(buf, offs, ns, pairs, h: float = 1e-6, quad: bool = True, nthreads: int = 1):
+    """Central differences of log|Pf| along skew pairs for a packed batch:
+    (f(A + hE) - f(A - hE)) / 2h with E = e_i e_j^T - e_j e_i^T, which equals
+    G_ij - G_ji for the gradient G = 1/2 A^{-T}.  pairs is (count, k, 2), 0-based.
+    quad=True evaluates f and the difference in binary128."""
+    pairs = np.ascontiguousarray(pairs, dtype=np.int64)
+    count, k = pairs.shape[0], pairs.shape[1]
+    buf = np.ascontiguousarray(buf, dtype=np.float64)
+    offs = np.ascontiguousarray(offs, dtype=np.int64)
+    ns = np.ascontiguousarray(ns, dtype=np.int64)
+    fd = np.zeros(count * k)
+    lib().orc_batch_logabspf_fd(_p(buf), offs.ctypes.data_as(ctypes.POINTER(_I64)),
+                                ns.ctypes.data_as(ctypes.POINTER(_I64)), count,
+                                pairs.ctypes.data_as(ctypes.POINTER(_I64)), k, float(h), int(bool(quad)), _p(fd),
+                                int(nthreads))
+    return fd.reshape(count, k)
 
 
 # ---------------------------------------------------------------------------

@@ -385,6 +385,21 @@ template <typename T> static void logabspf(const double* Ain, int64_t n, double*
   *sign = (double)sg;
 }
 
+// log|Pf| of A + h (e_i e_j^T - e_j e_i^T) in the working type T, returned in T, so
+// that a central difference of two such values keeps T's precision (a difference
+// of values already rounded to double would lose about 1e-16 |log|Pf|| / h).
+template <typename T>
+static T logabspf_pair(const double* Ain, int64_t n, int64_t i, int64_t j, T h) {
+  std::vector<T> A((size_t)n * n), tau(n), eta(n);
+  for (int64_t k = 0; k < n * n; k++) A[k] = T(Ain[k]);
+  A[i + j * n] = A[i + j * n] + h;  // column-major A(i, j)
+  A[j + i * n] = A[j + i * n] - h;
+  skewblockedhess<T>(A.data(), n, n, tau.data(), eta.data(), false);
+  T lp = 0;
+  for (int64_t k = 0; k < n - 1; k += 2) lp += M<T>::log(M<T>::abs(eta[k]));
+  return lp;
+}
+
 // ---------------------------------------------------------------------------
 // Complex skew-symmetric Pfaffian by Parlett-Reid elimination with pivoting,
 // pfaffian.jl:98-137 (_pfaffian!, the running product) and :193-233
@@ -823,7 +838,7 @@ template <typename T> static int skewtrieigen_divided(T* ev, int64_t N, T* vals,
   return -1;
 }
 
-// skeweigen!  eigen.jl:338-354 (real).  A (n x n) is consumed.
+// skeweigen!  eigen.jl:75-91 (real).  A (n x n) is consumed.
 template <typename T>
 static int skeweigen(const double* Ain, int64_t n, T* vals, T* Vr, T* Vi, T* ev_out = nullptr) {
   if (n == 1) {  // :340-342
@@ -1053,7 +1068,7 @@ int orc_skewtrieigvals_q(double* ev, int64_t N, double* vals) {
 }
 
 int orc_eigvals_d(const double* A, int64_t n, double* vals) {
-  // skeweigvals!  eigen.jl:312-318
+  // skeweigvals!  eigen.jl:49-55
   if (n == 1) {
     vals[0] = A[0];
     return 0;
@@ -1186,6 +1201,31 @@ void orc_batch_logabspf_grad_d(const double* A, const int64_t* off, const int64_
         for (int64_t i = 0; i < m; i++) grad[off[b] + i + j * m] = 0.5 * X[j + i * m];
     } else {
       for (int64_t k = 0; k < m * m; k++) grad[off[b] + k] = std::numeric_limits<double>::quiet_NaN();
+    }
+  }
+  (void)nthreads;
+}
+
+// Central finite differences of log|Pf| along skew pairs (the check of the
+// rrule gradient: d/dh log|Pf(A + h (e_i e_j^T - e_j e_i^T))| = G_ij - G_ji for
+// G = 1/2 A^{-T}).  pairs holds k (i, j) index pairs per matrix (count * k * 2
+// entries, 0-based); fd[b * k + p] receives the difference quotient with step h.
+// quad != 0 runs the restated reduction and the difference in binary128, so
+// the quotient carries only the O(h^2) truncation error.  OpenMP over pairs.
+void orc_batch_logabspf_fd(const double* A, const int64_t* off, const int64_t* n, int64_t count,
+                           const int64_t* pairs, int64_t k, double h, int quad_prec, double* fd, int nthreads) {
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+#endif
+  for (int64_t t = 0; t < count * k; t++) {
+    const int64_t b = t / k, i = pairs[2 * t], j = pairs[2 * t + 1];
+    if (quad_prec) {
+      const quad hq = (quad)h;
+      const quad d = logabspf_pair<quad>(A + off[b], n[b], i, j, hq) - logabspf_pair<quad>(A + off[b], n[b], i, j, -hq);
+      fd[t] = (double)(d / (2 * hq));
+    } else {
+      const double d = logabspf_pair<double>(A + off[b], n[b], i, j, h) - logabspf_pair<double>(A + off[b], n[b], i, j, -h);
+      fd[t] = d / (2 * h);
     }
   }
   (void)nthreads;

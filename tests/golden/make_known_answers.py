@@ -6,7 +6,7 @@ literals are the golden vectors: they are read here as TEXT from the reference
 checkout and stored as JSON, which the tests load (the reference checkout is
 not needed at test time).
 
-Usage:  python tests/golden/make_known_answers.py [path/to/runtests.jl]
+Usage:  python tests/golden/make_known_answers.py path/to/SkewLinearAlgebra.jl/test/runtests.jl
 """
 from __future__ import annotations
 
@@ -16,7 +16,6 @@ import re
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-DEFAULT_SRC = "/root/reference/test/runtests.jl"
 
 
 def _nums(s: str):
@@ -76,7 +75,9 @@ def extract(src: str) -> dict:
 
 
 def main():
-    src = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_SRC
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_known_answers.py path/to/SkewLinearAlgebra.jl/test/runtests.jl")
+    src = sys.argv[1]
     data = extract(src)
     dst = os.path.join(HERE, "reference_known_answers.json")
     with open(dst, "w") as f:
