@@ -94,11 +94,16 @@ SKEW_API int skew_logabspf_d(skew_handle_t h, double* A, int64_t n, int64_t lda,
 SKEW_API int skew_logabspf_grad_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* sign,
                          double* G, int64_t ldg, int* info);
 
-/* LA.eigvals!(A::SkewHermitian{Float64})  eigen.jl:2-6 -> skeweigvals! :312-318.
- * vals_im[n] = imaginary parts of the eigenvalues (eigenvalue k is i*vals_im[k]),
- * sorted descending: the order the reference returns from its own fallback
- * (skeweigen.jl:134-137); the batched entry point keeps the reference's QR order
- * (skewtrieigvals!, skeweigen.jl:105-156).  A is destroyed. */
+/* LA.eigvals!(A::SkewHermitian{Float64})  eigen.jl:2-6 -> skeweigvals! :49-55.
+ * vals_im[n] = imaginary parts of the eigenvalues (eigenvalue k is i*vals_im[k]).
+ * n <= 1024: in the reference's order, the deflation order of skewtrieigvals!
+ * (skeweigen.jl:105-156), run on one GPU thread after the reduction; info receives
+ * SKEW_OK, SKEW_FALLBACK_USED (the shifts stagnated and the values come from the
+ * reference's fallback, sorted descending, skeweigen.jl:132-137) or
+ * SKEW_NO_CONVERGENCE (skeweigen.jl:154).  n > 1024: sorted descending by bisection
+ * over the whole GPU (the fallback's order).  For the values sorted descending at any
+ * n, at bisection speed, use skew_eigvals_irange_d(1, n), which is eigvals(A, 1:n).
+ * A is destroyed. */
 SKEW_API int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info);
 
 /* LA.eigvals!(A::SkewHermitian{Float64}, irange)  eigen.jl:8-11, :57-64: vals_im[0 .. iu-il] =
@@ -116,16 +121,18 @@ SKEW_API int skew_eigvals_interval_d(skew_handle_t h, double* A, int64_t n, int6
 /* eigvals without any device allocation.  No counterpart in the reference.
  * For callers that cannot call cudaMalloc (a host that owns all device memory
  * through its own pool, or a path where an allocation's synchronisation or
- * failure is not acceptable): same result as skew_eigvals_d, but its scratch
+ * failure is not acceptable): the eigenvalues of skew_eigvals_d, sorted
+ * descending (as eigvals(A, 1:n)), equal to them to rounding; its scratch
  * (n+1 doubles) is a fixed array inside the library instead of the handle's
  * workspace, and the stream is passed directly (no handle).  n <= 1024, else
- * SKEW_UNSUPPORTED.  The first call on each device looks up the array's device
- * address, so make it before any stream capture.  All calls share the array:
- * calls that overlap on the GPU race and must be serialised by the caller. */
+ * SKEW_UNSUPPORTED.  The first call on each device (and again after a device
+ * reset) looks up the array's device address, so make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race and
+ * must be serialised by the caller. */
 SKEW_API int skew_eigvals_noalloc_d(double* A, int64_t n, int64_t lda, double* vals_im, int* info,
                                     skew_stream_t stream);
 
-/* LA.eigen!(A::SkewHermitian{Float64})  eigen.jl:338-360 (skeweigen! + skewtrieigen_divided!).
+/* LA.eigen!(A::SkewHermitian{Float64})  eigen.jl:75-97 (skeweigen! + skewtrieigen_divided!).
  * vals_im[n] in the reference's order; eigenvectors V = Vr + i*Vi (n x n each).  A is
  * destroyed.  n <= 1024: lda == ldv == n.  n > 1024 (up to 32768): blocked reduction,
  * bisection and twisted-factorisation vectors, values sorted descending (the reference's
@@ -170,7 +177,7 @@ SKEW_API int skew_batch_logabspf_host_d(skew_batch_plan_t plan, const double* A,
 /* eigvals for every matrix: vals_im[b] (device pointers) receives n[b] values. */
 SKEW_API int skew_batch_eigvals_d(skew_batch_plan_t plan, const double* const* A, double* const* vals_im, int* status);
 
-/* eigen for every matrix (skeweigen! + skewtrieigen_divided!, eigen.jl:338-360): vals_im[b] (n),
+/* eigen for every matrix (skeweigen! + skewtrieigen_divided!, eigen.jl:75-97): vals_im[b] (n),
  * Vr[b], Vi[b] (n x n, leading dimension n) device pointers; eigenvectors are Vr + i*Vi.
  * status[b]: SKEW_OK, SKEW_FALLBACK_USED (the reference's LAPACK fallback path,
  * skeweigen.jl:364-371, taken on the GPU) or SKEW_NO_CONVERGENCE.  n <= 1024. */
@@ -339,6 +346,48 @@ SKEW_API int skew_tridiag_svdvals_z(skew_handle_t h, const double* ev, const dou
                                     int* info);
 SKEW_API int skew_tridiag_svd_z(skew_handle_t h, const double* ev, const double* dvim, int64_t n, double* S,
                                 double* U, double* V, int64_t ldu, int* info);
+
+/* ---------------------------------------------------------------------------
+ * Tuning: the launch shapes and limits of the kernels, one table per handle.  The
+ * reference fixes its one shape by rule (setnb, hessenberg.jl:133-142, the panel
+ * width from n); here each shape that a measurement decides is a key.  A new handle
+ * starts from the compiled-in defaults (measured on GB300) and then loads the
+ * device's entry (matched by the CUDA device name) from the JSON table that the
+ * environment variable SKEW_TUNING_FILE names, or else from skew_tuning.json beside
+ * libskewgpu.so, written by the autotuner (skewgpu/autotune.py).  Keys
+ * (skew_tuning_key lists them): bucket_edges (list), batch_smem_nmax,
+ * batch_smem_nt_small, batch_smem_nt_large, batch_global_nt,
+ * batch_global_ctas_per_sm, batch_graph, func_chain_nmax, blocked_min_n,
+ * blocked_persistent, persist_ctas, persist_tail, persist_items, zpersist_min_n,
+ * zpersist_ctas, zpersist_items, pfz_cta_max, pfz_nt, pfz_ctas, and the limits
+ * wait_polls (grid-barrier polls before SKEW_TIMEOUT; 0: the default, seconds),
+ * wait_skip_cta (>= 0: that CTA of a cooperative kernel skips its arrivals, so the
+ * bounded waits run out: a test of the timeout path; -1: off) and qr_max_iter (QR
+ * sweeps before SKEW_NO_CONVERGENCE; 0: the reference's 30 n, skeweigen.jl:115).
+ * Batch plans take the bucket keys when they are created.  No reference counterpart.
+ * ------------------------------------------------------------------------- */
+/* One integer key; SKEW_BAD_ARG for an unknown key or a value out of its range. */
+SKEW_API int skew_tuning_set(skew_handle_t h, const char* key, int64_t value);
+/* A list key (bucket_edges: 1..8 ascending sizes). */
+SKEW_API int skew_tuning_set_list(skew_handle_t h, const char* key, const int64_t* values, int count);
+/* values[0 .. *count) <- the key's value(s) (cap: room in values). */
+SKEW_API int skew_tuning_get(skew_handle_t h, const char* key, int64_t* values, int cap, int* count);
+/* Back to the compiled-in defaults. */
+SKEW_API int skew_tuning_reset(skew_handle_t h);
+/* Load the device's entry from a table file; SKEW_UNSUPPORTED if it has none (no change),
+ * SKEW_BAD_ARG if the file cannot be read or a value is out of range (no change). */
+SKEW_API int skew_tuning_load(skew_handle_t h, const char* path);
+/* Where the handle's table came from ("defaults", or the file and device name, then
+ * " +key" for each key set since). */
+SKEW_API const char* skew_tuning_source(skew_handle_t h);
+/* The i-th key name (0-based), NULL past the last. */
+SKEW_API const char* skew_tuning_key(int i);
+/* What a table file holds for a device name, without a handle or a GPU: the key's
+ * value(s) after loading the device's entry over the defaults.  SKEW_OK if the file
+ * has an entry for the device, SKEW_UNSUPPORTED if not (values are the defaults),
+ * SKEW_BAD_ARG if it cannot be read, a value is out of range or the key is unknown. */
+SKEW_API int skew_tuning_file_get(const char* path, const char* device, const char* key, int64_t* values, int cap,
+                                  int* count);
 
 /* Diagnostics: measured FP64 DFMA throughput of the current device in TFLOP/s
  * (runs a short microbenchmark on the handle's stream and synchronizes). */

@@ -10,12 +10,17 @@
 #include <cstring>
 #include <new>
 #include <numeric>
+#include <string>
 #include <vector>
 
 #include "../../include/skewgpu.h"
 #include "skew_internal.h"
 
 using namespace skew;
+
+namespace skew {
+std::string tuning_default_path();
+}
 
 struct skew_handle_st {
   cudaStream_t stream = nullptr;
@@ -27,16 +32,19 @@ struct skew_handle_st {
   size_t aux_bytes = 0;
   struct skew_batch_plan_st* plan1 = nullptr;  // batch-of-one plan for single-matrix eigen/exp/cis
   int64_t plan1_n = 0;
+  Tuning tune;              // launch shapes and limits (compiled defaults, then the device's table)
+  std::string tune_source;  // where tune came from
 };
 
 struct Bucket {
-  int begin, end, nmax, smem_matrix, grid;
+  int begin, end, nmax, smem_matrix, grid, nt;
   int64_t gws_slot;  // doubles per CTA slot (global bucket)
   size_t gws_off;    // offset of the bucket's slots in the plan workspace (doubles)
 };
 
 struct skew_batch_plan_st {
   skew_handle_t h = nullptr;
+  Tuning tune;  // the handle's table when the plan was created (bucket shapes)
   int64_t count = 0;
   std::vector<int32_t> n_host;
   std::vector<Bucket> buckets;
@@ -155,13 +163,96 @@ int skew_create(skew_handle_t* handle) {
   if (!handle) return SKEW_BAD_ARG;
   skew_handle_st* h = new (std::nothrow) skew_handle_st();
   if (!h) return SKEW_NO_MEMORY;
+  cudaDeviceProp prop;
   if (cudaGetDevice(&h->device) != cudaSuccess ||
-      cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess) {
+      cudaDeviceGetAttribute(&h->sms, cudaDevAttrMultiProcessorCount, h->device) != cudaSuccess ||
+      cudaGetDeviceProperties(&prop, h->device) != cudaSuccess) {
     delete h;
     return SKEW_CUDA_ERROR;
   }
+  // the compiled-in defaults, then the table for this device's name, if there is one
+  tuning_defaults(&h->tune);
+  h->tune_source = "defaults";
+  const std::string path = tuning_default_path();
+  bool found = false;
+  if (FILE* f = std::fopen(path.c_str(), "rb")) {
+    std::fclose(f);
+    if (tuning_load_file(&h->tune, path.c_str(), prop.name, &found) != SKEW_OK)
+      h->tune_source = "defaults (unreadable table: " + path + ")";
+    else if (found)
+      h->tune_source = path + " [" + prop.name + "]";
+  }
   *handle = h;
   return SKEW_OK;
+}
+
+int skew_tuning_set(skew_handle_t h, const char* key, int64_t value) {
+  if (!h) return SKEW_BAD_ARG;
+  const long long v = value;
+  const int s = tuning_set(&h->tune, key, &v, 1);
+  if (s == SKEW_OK) h->tune_source += std::string(" +") + key;
+  return s;
+}
+
+int skew_tuning_set_list(skew_handle_t h, const char* key, const int64_t* values, int count) {
+  if (!h || !values || count < 1 || count > kMaxBucketEdges) return SKEW_BAD_ARG;
+  long long v[kMaxBucketEdges];
+  for (int i = 0; i < count; i++) v[i] = values[i];
+  const int s = tuning_set(&h->tune, key, v, count);
+  if (s == SKEW_OK) h->tune_source += std::string(" +") + key;
+  return s;
+}
+
+static int tuning_get_i64(const Tuning* T, const char* key, int64_t* values, int cap, int* count) {
+  if (!values || cap < 1) return SKEW_BAD_ARG;
+  long long v[kMaxBucketEdges];
+  int c = 0;
+  const int s = tuning_get(T, key, v, kMaxBucketEdges, &c);
+  if (s != SKEW_OK) return s;
+  for (int i = 0; i < c && i < cap; i++) values[i] = v[i];
+  if (count) *count = c;
+  return SKEW_OK;
+}
+
+int skew_tuning_get(skew_handle_t h, const char* key, int64_t* values, int cap, int* count) {
+  if (!h) return SKEW_BAD_ARG;
+  return tuning_get_i64(&h->tune, key, values, cap, count);
+}
+
+int skew_tuning_reset(skew_handle_t h) {
+  if (!h) return SKEW_BAD_ARG;
+  tuning_defaults(&h->tune);
+  h->tune_source = "defaults";
+  return SKEW_OK;
+}
+
+int skew_tuning_load(skew_handle_t h, const char* path) {
+  if (!h || !path) return SKEW_BAD_ARG;
+  cudaDeviceProp prop;
+  CK(cudaGetDeviceProperties(&prop, h->device));
+  bool found = false;
+  const int s = tuning_load_file(&h->tune, path, prop.name, &found);
+  if (s != SKEW_OK) return s;
+  if (!found) return SKEW_UNSUPPORTED;  // no entry for this device: nothing changed
+  h->tune_source = std::string(path) + " [" + prop.name + "]";
+  return SKEW_OK;
+}
+
+const char* skew_tuning_source(skew_handle_t h) { return h ? h->tune_source.c_str() : nullptr; }
+
+const char* skew_tuning_key(int i) { return tuning_key_name(i); }
+
+int skew_tuning_file_get(const char* path, const char* device, const char* key, int64_t* values, int cap,
+                         int* count) {
+  if (!path || !device || !key || !values || cap < 1) return SKEW_BAD_ARG;
+  Tuning T;
+  tuning_defaults(&T);
+  bool found = false;
+  int s = tuning_load_file(&T, path, device, &found);
+  if (s != SKEW_OK) return s;
+  s = tuning_get_i64(&T, key, values, cap, count);
+  if (s != SKEW_OK) return s;
+  return found ? SKEW_OK : SKEW_UNSUPPORTED;
 }
 
 int skew_destroy(skew_handle_t h) {
@@ -188,13 +279,10 @@ int skew_set_stream(skew_handle_t h, skew_stream_t s) {
 }
 
 // Largest n handled by the one-CTA single-matrix kernel, and the size above
-// which single-matrix calls use the multi-CTA blocked reduction instead
-// (override with SKEW_BLOCKED_MIN_N).
+// which single-matrix calls use the multi-CTA blocked reduction instead (the
+// tuning key blocked_min_n).
 static const int64_t kSingleMax = 1024;
-static int64_t blocked_min_n() {
-  const char* v = getenv("SKEW_BLOCKED_MIN_N");
-  return (v && *v) ? atoll(v) : 192;
-}
+static int64_t blocked_min_n(skew_handle_t h) { return h->tune.blocked_min_n; }
 
 static int single(skew_handle_t h, double* A, int64_t n, int64_t lda, double* G, int64_t ldg, double* logpf,
                   double* sign, double* ev, double* tau, int* info, int check, int want_pf) {
@@ -232,11 +320,11 @@ static int blocked(skew_handle_t h, double* A, int64_t n, int64_t lda, double* t
     tau = ws + wsd + n;
   }
   // one cooperative launch for all panels when v fits in shared memory; the
-  // multi-launch path otherwise (or with SKEW_BLOCKED_PERSISTENT=0)
-  const char* pv = getenv("SKEW_BLOCKED_PERSISTENT");
-  const bool persistent = n <= 24576 && !(pv && pv[0] == '0');
+  // multi-launch path otherwise (or with the tuning key blocked_persistent = 0)
+  const bool persistent = n <= 24576 && h->tune.blocked_persistent != 0;
   if (persistent) {
-    cudaError_t e = blocked_hessenberg_persistent(A, lda, (int)n, tau, ev, info, ws, h->sms, nullptr, h->stream);
+    cudaError_t e =
+        blocked_hessenberg_persistent(A, lda, (int)n, tau, ev, info, ws, h->sms, nullptr, h->tune, h->stream);
     if (e == cudaSuccess) return SKEW_OK;
     if (e != cudaErrorNotSupported && e != cudaErrorCooperativeLaunchTooLarge) return SKEW_CUDA_ERROR;
     cudaGetLastError();
@@ -247,7 +335,7 @@ static int blocked(skew_handle_t h, double* A, int64_t n, int64_t lda, double* t
 
 int skew_hessenberg_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* tau, double* ev, int* info) {
   if (n > 1 && (!tau || !ev)) return SKEW_BAD_ARG;
-  if (n >= blocked_min_n()) return blocked(h, A, n, lda, tau, ev, info, 0, nullptr);
+  if (n >= blocked_min_n(h)) return blocked(h, A, n, lda, tau, ev, info, 0, nullptr);
   return single(h, A, n, lda, nullptr, 0, nullptr, nullptr, n > 1 ? ev : nullptr, n > 1 ? tau : nullptr, info, 0,
                 0);
 }
@@ -255,7 +343,7 @@ int skew_hessenberg_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double
 int skew_logabspf_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* sign, int check,
                     int* info) {
   if (!logpf || !sign) return SKEW_BAD_ARG;
-  if (n >= blocked_min_n() && (n % 2) == 0) {
+  if (n >= blocked_min_n(h) && (n % 2) == 0) {
     double* extra = nullptr;
     // workspace layout: [blocked ws][ev (n)][tau (n)][not-skew flag]; size it before the check
     const size_t wsd = blocked_ws_doubles((int)n) + persist_ws_extra_doubles();
@@ -277,15 +365,26 @@ int skew_logabspf_grad_d(skew_handle_t h, double* A, int64_t n, int64_t lda, dou
   return single(h, A, n, lda, G, ldg, logpf, sign, nullptr, nullptr, info, 0, 1);
 }
 
-int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info) {
+static int single_plan(skew_handle_t h, int64_t n, skew_batch_plan_t* out);
+static int tridiag_qr_vals(skew_handle_t h, const double* ev, int64_t n, double* vals_im, int* status);
+
+// info <- the QR's status unless the reduction already reported an error.
+__global__ void merge_qr_status_kernel(const int* qr, int* info) {
+  if (*info == SKEW_OK) *info = *qr;
+}
+
+// Eigenvalues sorted descending by bisection on SymTridiagonal(0, ev) after the
+// reduction (the values of skew_eigvals_d without the reference's QR order): the
+// large-matrix path of skew_eigvals_d, and the values under svdvals, which sorts them.
+static int eigvals_bisect_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info) {
   if (!h || n < 0 || (n > 0 && (!A || !vals_im))) return SKEW_BAD_ARG;
   if (n == 0) return SKEW_OK;
-  if (n == 1) {  // skeweigvals! n == 1 returns [A[1,1]] (eigen.jl:314)
+  if (n == 1) {  // skeweigvals! n == 1 returns [A[1,1]] (eigen.jl:51)
     CK(cudaMemcpyAsync(vals_im, A, sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
     if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
     return SKEW_OK;
   }
-  if (n >= blocked_min_n()) {
+  if (n >= blocked_min_n(h)) {
     double* extra = nullptr;
     int st = blocked(h, A, n, lda, nullptr, nullptr, info, 2 * (size_t)n + 2, &extra);
     if (st) return st;
@@ -298,6 +397,36 @@ int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* v
   st = single(h, A, n, lda, nullptr, 0, nullptr, nullptr, ev, nullptr, info, 0, 0);
   if (st) return st;
   CK(launch_tridiag_bisect(ev, (int)n, vals_im, ev + n, h->stream));
+  return SKEW_OK;
+}
+
+int skew_eigvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* vals_im, int* info) {
+  if (!h || n < 0 || (n > 0 && (!A || !vals_im))) return SKEW_BAD_ARG;
+  if (n <= 1 || n > kSingleMax) return eigvals_bisect_d(h, A, n, lda, vals_im, info);
+  // n <= 1024: the reduction, then skewtrieigvals! (skeweigen.jl:105-156) on one lane,
+  // which gives the values in the reference's deflation order (eigen.jl:49-55).
+  skew_batch_plan_t P = nullptr;
+  int st = single_plan(h, n, &P);
+  if (st) return st;
+  double* ev = nullptr;
+  if (n >= blocked_min_n(h)) {
+    double* extra = nullptr;
+    st = blocked(h, A, n, lda, nullptr, nullptr, info, 2 * (size_t)n + 2, &extra);
+    if (st) return st;
+    ev = extra;
+  } else {
+    st = ensure_ws(h, sizeof(double) * (size_t)(n + 2));
+    if (st) return st;
+    ev = (double*)h->ws;
+    st = single(h, A, n, lda, nullptr, 0, nullptr, nullptr, ev, nullptr, info, 0, 0);
+    if (st) return st;
+  }
+  st = tridiag_qr_vals(h, ev, n, vals_im, info ? P->e_status : nullptr);
+  if (st) return st;
+  if (info) {
+    merge_qr_status_kernel<<<1, 1, 0, h->stream>>>(P->e_status, info);
+    CK(cudaGetLastError());
+  }
   return SKEW_OK;
 }
 
@@ -315,7 +444,7 @@ static int eigvals_select_d(skew_handle_t h, double* A, int64_t n, int64_t lda, 
   }
   double* ev = nullptr;
   double* bnd = nullptr;
-  if (n >= blocked_min_n()) {
+  if (n >= blocked_min_n(h)) {
     double* extra = nullptr;
     int st = blocked(h, A, n, lda, nullptr, nullptr, info, 2 * (size_t)n + 8, &extra);
     if (st) return st;
@@ -349,18 +478,16 @@ int skew_eigvals_interval_d(skew_handle_t h, double* A, int64_t n, int64_t lda, 
 // Batched plans
 // ---------------------------------------------------------------------------
 
-// Size buckets: the working copy stays in shared memory up to n = 152 (227 KB
-// with the vectors and gradient scratch); larger matrices work in a per-CTA
-// global slot (L2 resident).
-static const int kBucketEdges[] = {32, 64, 96, 128, 152};
-
-// Tunables (environment overrides for sweeps): largest n whose working copy is
-// kept in shared memory, and resident CTAs per SM for the global-memory bucket
-// (each holds an n x n working copy; 2 per SM keeps 152 * 2 * 0.5 MB in L2).
-static int env_int(const char* name, int dflt) {
-  const char* v = getenv(name);
-  if (!v || !*v) return dflt;
-  return atoi(v);
+// Size buckets (the tuning key bucket_edges; by default 32, 64, 96, 128, 152, and one
+// bucket above the last edge): the working copy may stay in shared memory up to
+// n = 152 (227 KB with the vectors and gradient scratch); larger matrices work in a
+// per-CTA global slot (L2 resident).  The keys batch_smem_nmax and
+// batch_global_ctas_per_sm pick the copy's location and the resident CTAs per SM of
+// the global-memory buckets (each CTA holds an n x n working copy; 2 per SM keeps
+// 152 * 2 * 0.5 MB in L2), batch_smem_nt_* / batch_global_nt the threads per CTA.
+static int bucket_threads(const Tuning& T, int nmax, bool smem_matrix) {
+  if (!smem_matrix) return T.batch_global_nt;
+  return nmax <= 96 ? T.batch_smem_nt_small : T.batch_smem_nt_large;
 }
 
 int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, skew_batch_plan_t* plan) {
@@ -370,6 +497,7 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
   skew_batch_plan_st* P = new (std::nothrow) skew_batch_plan_st();
   if (!P) return SKEW_NO_MEMORY;
   P->h = h;
+  P->tune = h->tune;
   P->count = count;
   P->n_host.resize(count);
   for (int64_t b = 0; b < count; b++) P->n_host[b] = (int32_t)n[b];
@@ -384,9 +512,10 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
   }
   P->ev_total = acc;
   // buckets over the sorted order
-  auto edge_of = [](int nn) {
-    for (int e : kBucketEdges)
-      if (nn <= e) return e;
+  const Tuning& T = P->tune;
+  auto edge_of = [&T](int nn) {
+    for (int i = 0; i < T.nedges; i++)
+      if (nn <= T.bucket_edges[i]) return T.bucket_edges[i];
     return 1 << 30;
   };
   size_t gws_total = 0;
@@ -398,15 +527,16 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
     B.begin = (int)t;
     B.end = (int)u;
     B.nmax = std::max<int32_t>(P->n_host[order[t]], 1);
-    const size_t smem_full = batch_smem_bytes(B.nmax, true);
+    const size_t smem_full = batch_smem_bytes(B.nmax, true, bucket_threads(T, B.nmax, true));
     // Working copies in shared memory up to n = 96 (several CTAs per SM).  Above that a
     // copy takes most of an SM's shared memory, one CTA per SM stalls at every step's
     // barriers, and two CTAs per SM on L2-resident global copies are faster (measured
     // on GB300: 1024 x n = 128 with gradient 12.8 ms against 15.3 ms; the mixed
-    // 16..256 workload +1.5 %).  SKEW_BATCH_SMEM_NMAX overrides (sweeps).
-    B.smem_matrix = (smem_full <= 227 * 1024 && B.nmax <= env_int("SKEW_BATCH_SMEM_NMAX", 96)) ? 1 : 0;
-    int occ = batch_occupancy(B.nmax, B.smem_matrix != 0);
-    if (!B.smem_matrix) occ = std::max(1, std::min(occ, env_int("SKEW_BATCH_GLOBAL_CTAS_PER_SM", 2)));
+    // 16..256 workload +1.5 %).  The tuning key batch_smem_nmax moves the limit.
+    B.smem_matrix = (smem_full <= 227 * 1024 && B.nmax <= T.batch_smem_nmax) ? 1 : 0;
+    B.nt = bucket_threads(T, B.nmax, B.smem_matrix != 0);
+    int occ = batch_occupancy(B.nmax, B.smem_matrix != 0, B.nt);
+    if (!B.smem_matrix) occ = std::max(1, std::min(occ, T.batch_global_ctas_per_sm));
     B.grid = (int)std::min<int64_t>((int64_t)h->sms * occ, u - t);
     B.gws_slot = B.smem_matrix ? 0 : (int64_t)B.nmax * (B.nmax | 1);
     B.gws_off = gws_total;
@@ -487,6 +617,7 @@ static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logp
     bp.end = B.end;
     bp.nmax = B.nmax;
     bp.smem_matrix = B.smem_matrix;
+    bp.nt = B.nt;
     bp.check = 0;
     bp.gws = P->d_gws ? P->d_gws + B.gws_off : nullptr;
     bp.gws_slot = B.gws_slot;
@@ -514,23 +645,15 @@ static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logp
 // call then launches the graph on the handle's stream.  Kernels read the
 // per-matrix pointer arrays at run time, so new contents behind the same arrays
 // need no re-capture.  A stream that the caller is already capturing,
-// SKEW_BATCH_GRAPH=0, or a capture that fails falls back to plain launches of
-// the same kernels on the handle's stream.
+// the tuning key batch_graph = 0, or a capture that fails falls back to plain
+// launches of the same kernels on the handle's stream.
 enum GraphOp { G_LOGPF = 0, G_EIGVALS, G_EIGEN, G_EXP, G_CIS, G_EXPVJP };
-
-static bool graphs_enabled() {
-  static const bool on = [] {
-    const char* e = std::getenv("SKEW_BATCH_GRAPH");
-    return !(e && e[0] == '0');
-  }();
-  return on;
-}
 
 template <class Issue>
 static int graph_issue(skew_batch_plan_t P, GraphOp op, const std::array<const void*, 6>& key, Issue&& issue) {
   cudaStream_t user = P->h->stream;
   cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-  if (P->graphs_off || !graphs_enabled() || cudaStreamIsCapturing(user, &cs) != cudaSuccess ||
+  if (P->graphs_off || !P->tune.batch_graph || cudaStreamIsCapturing(user, &cs) != cudaSuccess ||
       cs != cudaStreamCaptureStatusNone) {
     (void)cudaGetLastError();
     return issue();
@@ -606,6 +729,7 @@ int skew_batch_eigvals_d(skew_batch_plan_t P, const double* const* A, double* co
     tp.status = status;
     tp.fallback = P->d_fallback;
     tp.grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
+    tp.max_iter = P->h->tune.qr_max_iter;
     CK(launch_batch_trieig(tp, P->h->stream));
     return SKEW_OK;
   });
@@ -794,7 +918,7 @@ static int eigen_ws(skew_batch_plan_t P) {
 // a few milliseconds.  Measured on the 512-matrix exp-adjoint workload (n in
 // {32, ..., 512}): 745 ms per step with 64, 768 with 160, 813 with 256, 1013 with
 // the chain for every size.
-static int func_chain_nmax() { return env_int("SKEW_FUNC_CHAIN_NMAX", 64); }
+static int func_chain_nmax(skew_batch_plan_t P) { return P->h->tune.func_chain_nmax; }
 
 // Size groups of the matrices above thr, their device index list and the workspace
 // of one chunk (problems per chunk bounded so one chunk's workspace stays within
@@ -904,6 +1028,7 @@ static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const*
   E.func = SKEW_FUNC_EXP;
   E.merged = ev_in ? 1 : 0;
   E.chain_nmax = (ev_in || chain_nmax >= P->nmax) ? (1 << 30) : chain_nmax;
+  E.max_iter = P->h->tune.qr_max_iter;
   const int grid = (int)std::min<int64_t>(2 * (int64_t)P->h->sms, P->count);
   CK(launch_eigen_chain(E, st));
   CK(launch_eigen_vectors(E, grid, st));
@@ -945,7 +1070,7 @@ static int func_run_graph(skew_batch_plan_t P, const double* const* A, double* c
                           const double* const* cot, int mode, int func, int* status) {
   int s = eigen_ws(P);
   if (s) return s;
-  s = fv_setup(P, func_chain_nmax());
+  s = fv_setup(P, func_chain_nmax(P));
   if (s) return s;
   const GraphOp op = mode == 0 ? G_EXP : (mode == 1 ? G_CIS : G_EXPVJP);
   return graph_issue(P, op, {A, out, cot, status, reinterpret_cast<const void*>((intptr_t)func), nullptr},
@@ -960,9 +1085,9 @@ static int func_run(skew_batch_plan_t P, const double* const* A, double* const* 
 static int func_issue(skew_batch_plan_t P, const double* const* A, double* const* out, const double* const* cot,
                       int mode, int func, int* status) {
   EigenBatch E;
-  int s = fv_setup(P, func_chain_nmax());
+  int s = fv_setup(P, func_chain_nmax(P));
   if (s) return s;
-  s = eigen_run(P, A, nullptr, nullptr, nullptr, &E, nullptr, func_chain_nmax());
+  s = eigen_run(P, A, nullptr, nullptr, nullptr, &E, nullptr, func_chain_nmax(P));
   if (s) return s;
   E.out = out;
   E.cot = cot;
@@ -1057,18 +1182,22 @@ static int eigen_large(skew_handle_t h, double* A, int64_t n, int64_t lda, doubl
                        int64_t ldv, int* info) {
   if (lda < n || ldv < n || n > (1LL << 15)) return n > (1LL << 15) ? SKEW_UNSUPPORTED : SKEW_BAD_ARG;
   const size_t wsd = blocked_ws_doubles((int)n) + persist_ws_extra_doubles();
-  const size_t extra = 2 * (size_t)n + 8 + large_eigen_ws_doubles((int)n);
+  const size_t lwsd = large_eigen_ws_doubles((int)n), auxd = large_eigen_aux_doubles((int)n);
+  const size_t extra = 2 * (size_t)n + 8 + lwsd + auxd + 1;
   int st = ensure_ws(h, sizeof(double) * (wsd + extra));
   if (st) return st;
-  double* base = (double*)h->ws + wsd;  // [ev (n)][tau (n)][bisection scratch (8)][eigenvector workspace]
+  // [ev (n)][tau (n)][bisection scratch (8)][eigenvector workspace][aux][gate]
+  double* base = (double*)h->ws + wsd;
   double* ev = base;
   double* tau = base + n;
   double* bp = base + 2 * n;
   double* lws = base + 2 * n + 8;
+  double* aux = lws + lwsd;
+  int* gate = (int*)(aux + auxd);
   st = blocked(h, A, n, lda, tau, ev, info, extra, nullptr);
   if (st) return st;
   CK(launch_tridiag_bisect(ev, (int)n, vals_im, bp, h->stream));
-  CK(large_eigen_vectors(A, lda, (int)n, tau, ev, vals_im, bp, Vr, Vi, ldv, lws, h->stream));
+  CK(large_eigen_vectors(A, lda, (int)n, tau, ev, vals_im, bp, Vr, Vi, ldv, lws, gate, aux, h->stream));
   return SKEW_OK;
 }
 
@@ -1193,13 +1322,10 @@ static int zlayout(skew_handle_t h, int64_t n, int64_t B, bool copy, bool vecs, 
 }
 
 // complex reduction in place.  One matrix: one CTA for n <= 128, the persistent
-// blocked kernel from zpersist_min_n() (SKEW_ZPERSIST_MIN_N), per-column multi-CTA
+// blocked kernel from the tuning key zpersist_min_n, per-column multi-CTA
 // kernels between (and where the persistent kernel cannot run).  B > 1 matrices of
 // size n, n^2 apart: one CTA each.
-static int64_t zpersist_min_n() {
-  const char* v = getenv("SKEW_ZPERSIST_MIN_N");
-  return (v && *v) ? atoll(v) : 384;
-}
+static int64_t zpersist_min_n(skew_handle_t h) { return h->tune.zpersist_min_n; }
 
 static int zreduce(skew_handle_t h, double* A, int64_t n, int64_t lda, int64_t B, double* tau, double* ev,
                    double* dvim, double* zws, int* info = nullptr) {
@@ -1222,8 +1348,8 @@ static int zreduce(skew_handle_t h, double* A, int64_t n, int64_t lda, int64_t B
     CK(launch_zhess_cta(P, (int)B, h->stream));
     return SKEW_OK;
   }
-  if (n >= zpersist_min_n()) {
-    const cudaError_t e = zhess_persistent(A, lda, (int)n, tau, ev, dvim, zws, h->sms, info, h->stream);
+  if (n >= zpersist_min_n(h)) {
+    const cudaError_t e = zhess_persistent(A, lda, (int)n, tau, ev, dvim, zws, h->sms, info, h->tune, h->stream);
     if (e == cudaSuccess) return SKEW_OK;
     if (e != cudaErrorNotSupported) return SKEW_CUDA_ERROR;
     cudaGetLastError();
@@ -1381,26 +1507,20 @@ int skew_batch_func_z(skew_handle_t h, const double* A, int64_t n, int64_t count
 
 // ---------------------------------------------------------------------------
 // Complex skew-symmetric Pfaffian (pfaffian.jl:98-137, :193-233): one CTA per
-// matrix up to pfz_cta_max(), above that one cooperative grid per matrix.
+// matrix up to the tuning key pfz_cta_max, above that one cooperative grid per matrix.
 // ---------------------------------------------------------------------------
-static int pfz_cta_max() {
-  static int v = -1;
-  if (v < 0) {
-    const char* s = getenv("SKEW_PFZ_CTA_MAX");
-    v = (s && *s) ? std::max(0, std::min(160, atoi(s))) : 160;
-  }
-  return v;
-}
+static int pfz_cta_max(skew_handle_t h) { return h->tune.pfz_cta_max; }
 
 static int pfz_run(skew_handle_t h, double* A, int64_t n, int64_t lda, double* logpf, double* phase, double* pf,
                    int check, int* info) {
   if (!h || n < 0 || (n > 0 && (!A || lda < n))) return SKEW_BAD_ARG;
   if (n > (1LL << 15)) return SKEW_UNSUPPORTED;
-  if (n > pfz_cta_max()) {
+  if (n > pfz_cta_max(h)) {
     int st = ensure_ws(h, sizeof(double) * pfz_grid_ws_doubles((int)n));
     if (st) return st;
     if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
-    CK(launch_pfz_grid((zc*)A, lda, (int)n, check, logpf, phase, pf, info, (double*)h->ws, h->sms, h->stream));
+    CK(launch_pfz_grid((zc*)A, lda, (int)n, check, logpf, phase, pf, info, (double*)h->ws, h->sms, h->tune,
+                       h->stream));
     return SKEW_OK;
   }
   PfzParams P{};
@@ -1415,6 +1535,7 @@ static int pfz_run(skew_handle_t h, double* A, int64_t n, int64_t lda, double* l
   P.phase = phase;
   P.pf = pf;
   P.status = info;
+  P.nt = h->tune.pfz_nt;
   CK(launch_pfz_cta(P, 1, h->stream));
   return SKEW_OK;
 }
@@ -1439,7 +1560,7 @@ int skew_batch_logabspf_z(skew_handle_t h, const double* A, int64_t n, int64_t c
   const int nn = (int)n;
   const bool even = nn % 2 == 0 && nn > 0;
   const bool sm = !even || pfz_smem_fits(nn);
-  if (even && !sm && nn > pfz_cta_max() && count < h->sms) {
+  if (even && !sm && nn > pfz_cta_max(h) && count < h->sms) {
     // few large matrices: one grid per matrix, on a copy (the input is read only)
     const size_t mat = 2 * (size_t)n * n, gw = pfz_grid_ws_doubles(nn);
     int st = ensure_ws(h, sizeof(double) * (mat + gw));
@@ -1449,7 +1570,8 @@ int skew_batch_logabspf_z(skew_handle_t h, const double* A, int64_t n, int64_t c
     for (int64_t b = 0; b < count; b++) {
       CK(cudaMemcpyAsync(W, A + b * mat, sizeof(double) * mat, cudaMemcpyDefault, h->stream));
       CK(launch_pfz_grid((zc*)W, n, nn, check, logpf ? logpf + b : nullptr, phase ? phase + 2 * b : nullptr,
-                         pf ? pf + 2 * b : nullptr, status ? status + b : nullptr, W + mat, h->sms, h->stream));
+                         pf ? pf + 2 * b : nullptr, status ? status + b : nullptr, W + mat, h->sms, h->tune,
+                         h->stream));
     }
     return SKEW_OK;
   }
@@ -1465,7 +1587,8 @@ int skew_batch_logabspf_z(skew_handle_t h, const double* A, int64_t n, int64_t c
   P.phase = phase;
   P.pf = pf;
   P.status = status;
-  const int occ = pfz_cta_occupancy(nn, P.smem_matrix != 0);
+  P.nt = h->tune.pfz_nt;
+  const int occ = pfz_cta_occupancy(nn, P.smem_matrix != 0, P.nt);
   int64_t grid = std::min<int64_t>(count, (int64_t)h->sms * (P.smem_matrix || !even ? occ : std::min(occ, 2)));
   if (even && !P.smem_matrix) {
     P.slot = n * (n - 1) / 2;
@@ -1539,7 +1662,7 @@ int skew_svdvals_d(skew_handle_t h, double* A, int64_t n, int64_t lda, double* S
   int* perm;
   int st = svd_aux(h, n, &vals, &sgn, &perm);
   if (st) return st;
-  st = skew_eigvals_d(h, A, n, lda, vals, info);
+  st = eigvals_bisect_d(h, A, n, lda, vals, info);
   if (st) return st;
   return svdvals_finish(h, n, vals, S);
 }
@@ -1606,6 +1729,13 @@ int skew_tridiag_eigvals_d(skew_handle_t h, const double* ev, int64_t n, double*
     return SKEW_OK;
   }
   // skewtrieigvals! (tridiag.jl:446-450): the QR in the reference's order, batch of one
+  return tridiag_qr_vals(h, ev, n, vals_im, info);
+}
+
+// skewtrieigvals! on one subdiagonal ev (device, n-1 entries, read only) through the
+// handle's batch-of-one plan: vals_im in the reference's order, status <- SKEW_OK,
+// SKEW_FALLBACK_USED or SKEW_NO_CONVERGENCE (status may be NULL).  2 <= n <= 1024.
+static int tridiag_qr_vals(skew_handle_t h, const double* ev, int64_t n, double* vals_im, int* status) {
   skew_batch_plan_t P = nullptr;
   int st = single_plan(h, n, &P);
   if (st) return st;
@@ -1622,9 +1752,10 @@ int skew_tridiag_eigvals_d(skew_handle_t h, const double* ev, int64_t n, double*
   tp.count = 1;
   tp.evwork = P->d_ev;
   tp.vals = arr + 1;
-  tp.status = info;
+  tp.status = status;
   tp.fallback = P->d_fallback;
   tp.grid = 1;
+  tp.max_iter = h->tune.qr_max_iter;
   CK(launch_batch_trieig(tp, h->stream));
   return SKEW_OK;
 }
@@ -1634,13 +1765,15 @@ int skew_tridiag_eigen_d(skew_handle_t h, const double* ev, int64_t n, double* v
   if (!h || n < 1 || (n > 1 && !ev) || !vals_im || !Vr || !Vi || ldv < n) return SKEW_BAD_ARG;
   if (n > kSingleMax) {  // bisection + twisted vectors, Q = I (values sorted descending)
     if (n > (1LL << 15)) return SKEW_UNSUPPORTED;
-    const size_t need = 8 + large_eigen_ws_doubles((int)n);
-    int st = ensure_ws(h, sizeof(double) * need);
+    const size_t lwsd = large_eigen_ws_doubles((int)n), auxd = large_eigen_aux_doubles((int)n);
+    int st = ensure_ws(h, sizeof(double) * (8 + lwsd + auxd + 1));
     if (st) return st;
-    double* bp = (double*)h->ws;
+    double* bp = (double*)h->ws;  // [bisection scratch (8)][eigenvector workspace][aux][gate]
+    double* aux = bp + 8 + lwsd;
     if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
     CK(launch_tridiag_bisect(ev, (int)n, vals_im, bp, h->stream));
-    CK(large_eigen_vectors(nullptr, 0, (int)n, nullptr, ev, vals_im, bp, Vr, Vi, ldv, bp + 8, h->stream));
+    CK(large_eigen_vectors(nullptr, 0, (int)n, nullptr, ev, vals_im, bp, Vr, Vi, ldv, bp + 8, (int*)(aux + auxd),
+                           aux, h->stream));
     return SKEW_OK;
   }
   if (ldv != n) return SKEW_UNSUPPORTED;

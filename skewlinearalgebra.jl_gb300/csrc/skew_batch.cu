@@ -827,37 +827,19 @@ constexpr int NT_SMALL = 128;   // shared-memory buckets up to n = 96
 constexpr int NT_LARGE = 256;   // shared-memory buckets above 96 (one CTA per SM)
 constexpr int NT_GLOBAL = 512;  // optional global-memory variant: one CTA of 16 warps per SM
 
-// Threads per CTA for global-memory working copies: 256 with two CTAs per SM
-// (measured best), or SKEW_BATCH_GLOBAL_NT=512 with one CTA per SM.
-static int global_threads() {
-  static int nt = [] {
-    const char* v = getenv("SKEW_BATCH_GLOBAL_NT");
-    return (v && atoi(v) == 512) ? NT_GLOBAL : 256;
-  }();
-  return nt;
+// Threads per CTA: the bucket's choice (from the handle's tuning table), or the
+// default for the working copy's location: 128 for shared-memory copies up to
+// n = 96, 256 above and for global-memory copies (measured best on GB300).
+static int threads_for(int nmax, bool smem_matrix, int nt) {
+  if (smem_matrix) {
+    if (nt == 128 || nt == 256 || nt == 512) return nt;
+    return nmax <= 96 ? NT_SMALL : NT_LARGE;
+  }
+  return nt == NT_GLOBAL ? NT_GLOBAL : NT_LARGE;
 }
 
-// Shared-memory buckets: SKEW_BATCH_SMEM_NT_SMALL (128 | 256) for n <= 96 and
-// SKEW_BATCH_SMEM_NT_LARGE (256 | 512) above (sweeps).
-static int smem_threads(bool small) {
-  static const int s = [] {
-    const char* v = getenv("SKEW_BATCH_SMEM_NT_SMALL");
-    return (v && atoi(v) == 256) ? 256 : NT_SMALL;
-  }();
-  static const int l = [] {
-    const char* v = getenv("SKEW_BATCH_SMEM_NT_LARGE");
-    return (v && atoi(v) == 512) ? 512 : NT_LARGE;
-  }();
-  return small ? s : l;
-}
-
-static int threads_for(int nmax, bool smem_matrix) {
-  if (!smem_matrix) return global_threads();
-  return smem_threads(nmax <= 96);
-}
-
-size_t batch_smem_bytes(int nmax, bool smem_matrix) {
-  const int nt = threads_for(nmax, smem_matrix);
+size_t batch_smem_bytes(int nmax, bool smem_matrix, int nt_req) {
+  const int nt = threads_for(nmax, smem_matrix, nt_req);
   size_t b = sizeof(double) * (size_t)smem_doubles(nmax, nt / 32);
   if (smem_matrix) b += sizeof(double) * (size_t)nmax * (size_t)(nmax | 1);
   return b;
@@ -879,8 +861,8 @@ static cudaError_t launch_t(const BatchParams& P, int grid, size_t smem, cudaStr
 template <bool HOST>
 static cudaError_t launch_pf(const BatchParams& P, int grid, cudaStream_t st, bool tridiag_only) {
   const bool sm = P.smem_matrix != 0;
-  const size_t smem = batch_smem_bytes(P.nmax, sm);
-  const int nt = threads_for(P.nmax, sm);
+  const size_t smem = batch_smem_bytes(P.nmax, sm, P.nt);
+  const int nt = threads_for(P.nmax, sm, P.nt);
   if (sm && nt == 128) return launch_t<128, true, HOST>(P, grid, smem, st, tridiag_only);
   if (sm && nt == 256) return launch_t<256, true, HOST>(P, grid, smem, st, tridiag_only);
   if (sm) return launch_t<512, true, HOST>(P, grid, smem, st, tridiag_only);
@@ -920,9 +902,9 @@ static int occ_t(size_t smem) {
   return occ;
 }
 
-int batch_occupancy(int nmax, bool smem_matrix) {
-  const size_t smem = batch_smem_bytes(nmax, smem_matrix);
-  const int nt = threads_for(nmax, smem_matrix);
+int batch_occupancy(int nmax, bool smem_matrix, int nt_req) {
+  const size_t smem = batch_smem_bytes(nmax, smem_matrix, nt_req);
+  const int nt = threads_for(nmax, smem_matrix, nt_req);
   if (smem_matrix && nt == 128) return occ_t<128, true>(smem);
   if (smem_matrix && nt == 256) return occ_t<256, true>(smem);
   if (smem_matrix) return occ_t<512, true>(smem);

@@ -559,7 +559,7 @@ cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, doubl
 // ===========================================================================
 constexpr int P_NT = 256;
 constexpr int P_NW = P_NT / 32;
-constexpr long long BAR_POLL_LIMIT = 1LL << 22;  // x ~1 us per poll (L2 read + sleep): ~4 s
+constexpr long long BAR_POLL_LIMIT = 1LL << 22;  // default: x ~1 us per poll (L2 read + sleep): ~4 s
 
 struct PersistParams {
   double* A;
@@ -575,6 +575,8 @@ struct PersistParams {
   int* err;
   int maxck;
   int items_per_warp;  // matvec tiles per warp and column (chunk count)
+  long long poll_limit;  // polls before a grid barrier gives up
+  int skip_cta;          // >= 0: this CTA never arrives (the waits run out: a test of the timeout)
 };
 
 __device__ __forceinline__ double ldg2(const double* p) { return __ldcg(p); }
@@ -588,9 +590,13 @@ __device__ bool gsync(const PersistParams& P) {
     volatile int* err = P.err;
     const unsigned g = *gen;
     __threadfence();
-    const unsigned a = atomicAdd(P.sync, 1u);
     int ok = 1;
-    if (a == gridDim.x - 1) {
+    if ((int)blockIdx.x == P.skip_cta) {
+      // no arrival: the others give up after poll_limit polls; wait (bounded) for that
+      long long it = 0;
+      while (!*err && ++it <= P.poll_limit) __nanosleep(100);
+      ok = 0;
+    } else if (atomicAdd(P.sync, 1u) == gridDim.x - 1) {
       atomicExch(P.sync, 0u);
       __threadfence();
       atomicAdd(P.sync + 1, 1u);
@@ -601,7 +607,7 @@ __device__ bool gsync(const PersistParams& P) {
           ok = 0;
           break;
         }
-        if (++it > BAR_POLL_LIMIT) {
+        if (++it > P.poll_limit) {
           atomicExch(P.err, 1);
           ok = 0;
           break;
@@ -1002,7 +1008,7 @@ __global__ void merge_err_kernel(const int* err, int* info) {
 // Persistent driver; returns cudaErrorNotSupported when the device cannot
 // co-schedule one CTA per SM (the caller then uses the multi-launch path).
 cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double* tau, double* ev, int* info,
-                                          double* wsbase, int sms, int* err_dev, cudaStream_t st) {
+                                          double* wsbase, int sms, int* err_dev, const Tuning& T, cudaStream_t st) {
   BlockedWs ws = carve_ws(wsbase, n);
   double* extra = wsbase + blocked_ws_doubles(n);  // u (2*BNB), 4 sync words, error flag
   int* err_dev_local = (int*)(extra + 2 * BNB + 4);
@@ -1016,18 +1022,14 @@ cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double*
   if (occ < 1) return cudaErrorNotSupported;
   // Two CTAs per SM hide more load latency on large matrices; below that, the two
   // grid barriers per column cost more than the extra CTAs bring.
-  // SKEW_PERSIST_CTAS / SKEW_PERSIST_TAIL override the grid and the columns left
-  // to the one-CTA kernel (sweeps).
+  // The tuning keys persist_ctas / persist_tail replace the grid and the columns
+  // left to the one-CTA kernel.
   // measured on GB300: one CTA per SM is 14-22 % faster for n <= 2048, two per
   // SM break even at n = 4096
   int grid = sms * ((occ >= 2 && n > 3072) ? 2 : 1);
   int tail = TAIL;
-  {
-    const char* g = getenv("SKEW_PERSIST_CTAS");
-    const char* t = getenv("SKEW_PERSIST_TAIL");
-    if (g && *g) grid = std::max(1, std::min(grid, atoi(g)));
-    if (t && *t) tail = std::max(32, std::min(TAIL, atoi(t)));
-  }
+  if (T.persist_ctas > 0) grid = std::max(1, std::min(sms * occ, T.persist_ctas));
+  if (T.persist_tail > 0) tail = std::max(32, std::min(TAIL, T.persist_tail));
   PersistParams P;
   P.A = A;
   P.lda = lda;
@@ -1044,11 +1046,9 @@ cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double*
   P.maxck = ws.max_chunks;
   // matvec tiles per warp and column: measured on GB300 at n = 8192, 8 gives 932 ms,
   // 4 945 ms, 2 981 ms (more, smaller tiles shorten the wait for the last ones)
-  P.items_per_warp = 8;
-  {
-    const char* v = getenv("SKEW_PERSIST_ITEMS");  // sweeps: 1..16
-    if (v && *v) P.items_per_warp = std::max(1, std::min(16, atoi(v)));
-  }
+  P.items_per_warp = std::max(1, std::min(16, T.persist_items));
+  P.poll_limit = T.wait_polls > 0 ? T.wait_polls : BAR_POLL_LIMIT;
+  P.skip_cta = T.wait_skip_cta;
   e = cudaMemsetAsync(P.sync, 0, 4 * sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(err_dev, 0, sizeof(int), st);

@@ -16,7 +16,7 @@
 //           tridiagonal SymTridiagonal(0, ev) come from a cyclic Jacobi solver
 //           in the same CTA and are laid out as skewtrieigen_backup! does
 //           (:470-489).
-//   back    V <- Q V for both parts (eigen.jl:348-352) by compact-WY blocks of 8
+//   back    V <- Q V for both parts (eigen.jl:85-89) by compact-WY blocks of 8
 //           reflectors: Y = V_b^T X, Z = T_b Y, X -= V_b Z.
 //   exp     E = Qr P^T + Qi R^T with P = Qr C + Qi S, R = Qi C - Qr S
 //           (C, S = cos, sin of the eigenvalues; exp.jl:3-35 reassociated).
@@ -104,10 +104,16 @@ __device__ int implicitstep_log(double* ev, int n, int start, double* log, int64
   const double shift = __dmul_rn(ev[n - 1], ev[n - 1]);
   const double tol = 10.0 * 2.220446049250313e-16;
   const int first = start;
+  // ev[i-2], ev[i-1], ev[i] of step i are what step i-1 wrote: carried in
+  // registers; ev[i+1] (untouched this sweep) is loaded one step ahead.  Every
+  // store of the reference's step is still made.
+  double pa = 0.0;            // ev[i-2] as left by the previous step
+  double b = ev[first - 1];   // ev[i-1]
+  double g = ev[first];       // ev[i]
+  double z = (first < n - 1) ? ev[first + 1] : 0.0;
   for (int i = first; i <= n - 1; i++) {
-    const double a = (i > start ? ev[i - 2] : 0.0);
-    const double b = ev[i - 1];
-    const double g = ev[i];
+    const double zn = (i + 2 <= n - 1) ? ev[i + 2] : 0.0;
+    const double a = (i > start ? pa : 0.0);
     double c, s;
     if (i > start) {
       givens_e(a, bulge, c, s);
@@ -117,13 +123,19 @@ __device__ int implicitstep_log(double* ev, int n, int start, double* log, int64
       givens_e(x1, x2, c, s);
     }
     if (i > 1) ev[i - 2] = __dadd_rn(__dmul_rn(c, a), __dmul_rn(s, bulge));
-    ev[i - 1] = __dsub_rn(__dmul_rn(c, b), __dmul_rn(s, g));
-    ev[i] = __dadd_rn(__dmul_rn(s, b), __dmul_rn(c, g));
+    const double nb = __dsub_rn(__dmul_rn(c, b), __dmul_rn(s, g));
+    const double ng = __dadd_rn(__dmul_rn(s, b), __dmul_rn(c, g));
+    ev[i - 1] = nb;
+    ev[i] = ng;
     if (i < n - 1) {
-      const double z = ev[i + 1];
-      ev[i + 1] = __dmul_rn(z, c);
+      const double nz = __dmul_rn(z, c);
+      ev[i + 1] = nz;
       bulge = __dmul_rn(s, z);
-      if (fabs(bulge) < tol && fabs(ev[i - 1]) < tol) start = i + 1;
+      if (fabs(bulge) < tol && fabs(nb) < tol) start = i + 1;
+      pa = nb;
+      b = ng;
+      g = nz;
+      z = zn;
     }
     log[len++] = c;
     log[len++] = s;
@@ -157,7 +169,7 @@ __global__ void eigen_chain_kernel(EigenBatch E) {
       reducetozero_g(ev, G, n);
     }
     const double tol = 10.0 * 2.220446049250313e-16;
-    const int max_iter = 30 * n;
+    const int max_iter = E.max_iter > 0 ? E.max_iter : 30 * n;
     int iter = 0, count_static = 0, start = 1;
     double mem = 1.0;
     while (n > 2 && iter < max_iter) {

@@ -31,6 +31,45 @@ inline cudaError_t raise_smem_limit_once(const void* kernel, std::atomic<uint64_
   return cudaSuccess;
 }
 
+// Launch shapes and limits of the kernels, one table per handle (skew_tuning.cu):
+// compiled-in defaults measured on GB300, replaced per device by a table the
+// autotuner writes, or key by key through skew_tuning_set.
+constexpr int kMaxBucketEdges = 8;
+struct Tuning {
+  // batched plans (fixed when a plan is created)
+  int bucket_edges[kMaxBucketEdges];  // a bucket holds the matrices with n <= edge (ascending)
+  int nedges;
+  int batch_smem_nmax;           // working copy in shared memory up to this n (and if it fits)
+  int batch_smem_nt_small;       // threads per CTA of shared-memory buckets with nmax <= 96
+  int batch_smem_nt_large;       // ... above 96
+  int batch_global_nt;           // threads per CTA of global-memory buckets
+  int batch_global_ctas_per_sm;  // resident CTAs per SM for global-memory buckets
+  int batch_graph;               // 1: batched calls record and replay CUDA graphs
+  int func_chain_nmax;           // function paths: the QR chain up to this n, bisection above
+  // one large real matrix
+  int blocked_min_n;             // the blocked multi-CTA reduction from this n
+  int blocked_persistent;        // 1: one cooperative launch for all panels
+  int persist_ctas;              // grid of the persistent reduction (0: chosen by n)
+  int persist_tail;              // columns left to the one-CTA kernel (0: the default)
+  int persist_items;             // matvec tiles per warp and column
+  // ComplexF64
+  int zpersist_min_n;            // the persistent complex reduction from this n
+  int zpersist_ctas;             // its grid (0: one CTA per SM)
+  int zpersist_items;            // its matvec tiles per warp and column
+  int pfz_cta_max;               // complex Pfaffian: one CTA per matrix up to this n, a grid above
+  int pfz_nt;                    // threads per CTA of the one-CTA Pfaffian (0: chosen by n)
+  int pfz_ctas;                  // grid of the cooperative Pfaffian (0: chosen by n)
+  // bounded waits and iteration limits
+  long long wait_polls;          // grid-barrier polls before SKEW_TIMEOUT (0: the kernel's default)
+  int wait_skip_cta;             // >= 0: this CTA skips its arrivals, so the barrier waits run out
+  int qr_max_iter;               // > 0: QR sweeps before SKEW_NO_CONVERGENCE (0: 30 n, the reference's)
+};
+void tuning_defaults(Tuning* T);
+int tuning_set(Tuning* T, const char* key, const long long* values, int count);
+int tuning_get(const Tuning* T, const char* key, long long* values, int cap, int* count);
+const char* tuning_key_name(int i);
+int tuning_load_file(Tuning* T, const char* path, const char* device, bool* found);
+
 // Batched one-CTA-per-matrix launches (skew_batch.cu).
 struct BatchParams {
   const double* const* A;  // [count] device pointers, original order
@@ -51,6 +90,7 @@ struct BatchParams {
   double* tau_out;         // packed tau, same offsets, or null
   double* const* refl_out; // [count] n x n buffers receiving the reduced matrix (reflectors) or null
   int* status;             // [count] or null
+  int32_t nt = 0;          // threads per CTA (0: the default for the copy's location)
   int32_t host_in = 0;     // A[] point into page-locked host memory (read with more loads in flight)
   double* const* grad_host = nullptr;  // [count] page-locked host destinations: the finished
                                        // gradient is copied there by the CTA that formed it
@@ -71,11 +111,11 @@ struct SingleParams {
   int want_pf;
 };
 
-size_t batch_smem_bytes(int nmax, bool smem_matrix);
+size_t batch_smem_bytes(int nmax, bool smem_matrix, int nt);
 cudaError_t launch_batch_pf(const BatchParams& P, int grid, cudaStream_t st, bool tridiag_only);
 cudaError_t launch_single(const SingleParams& P, cudaStream_t st);
 int batch_threads();
-int batch_occupancy(int nmax, bool smem_matrix);  // resident CTAs per SM
+int batch_occupancy(int nmax, bool smem_matrix, int nt);  // resident CTAs per SM
 
 // Skew tridiagonal eigenvalues (skew_qr.cu).
 struct TrieigParams {
@@ -90,6 +130,7 @@ struct TrieigParams {
   unsigned* fallback;      // [2 + 2 count]: number of stagnated matrices, work counter,
                            // then their indices and active sizes (solved by a second kernel)
   int grid;                // CTAs of the fallback kernel
+  int max_iter = 0;        // QR sweeps before SKEW_NO_CONVERGENCE (0: 30 n, skeweigen.jl:115)
 };
 cudaError_t launch_batch_trieig(const TrieigParams& P, cudaStream_t st);
 
@@ -140,7 +181,7 @@ cudaError_t launch_zdiag_im(const double* A, int64_t lda, int n, double* dvim, c
 // falls back to zhess_large); info <- SKEW_TIMEOUT if a grid barrier gave up.
 size_t zhess_persist_ws_doubles(int n);
 cudaError_t zhess_persistent(double* A, int64_t lda, int n, double* tau, double* ev, double* dvim, double* ws,
-                             int sms, int* info, cudaStream_t st);
+                             int sms, int* info, const Tuning& T, cudaStream_t st);
 cudaError_t zhess_large(double* A, int64_t lda, int n, double* tau, double* ev, double* dvim, double* ws,
                         cudaStream_t st);
 // complex eigen from `batch` reduced matrices of size n (arrays per matrix: A lda*n,
@@ -164,9 +205,13 @@ cudaError_t zfunc_from_eigen(int mode, int func, int n, const double* vals_im, c
 size_t large_eigen_ws_doubles(int n);
 cudaError_t symtri_vectors(const double* dg, const double* e, int n, const double* mu, const double* bp, double* Y,
                            double* ws, int batch, cudaStream_t st);
+// gate: a device int of scratch; aux: large_eigen_aux_doubles(n) doubles of scratch.
+// A tridiagonal that splits exactly into more odd-size blocks than n mod 2 (several
+// zero eigenvalues) is solved in full mode, as the reference's fallback does.
+size_t large_eigen_aux_doubles(int n);
 cudaError_t large_eigen_vectors(const double* A, int64_t lda, int n, const double* tau, const double* ev,
                                 const double* vals, const double* bp, double* Vr, double* Vi, int64_t ldv, double* ws,
-                                cudaStream_t st);
+                                int* gate, double* aux, cudaStream_t st);
 
 // Eigenvectors / exp / cis / exp adjoint for batches of real skew matrices (skew_eigen.cu).
 // Leading dimensions of every per-matrix n x n buffer are n.
@@ -199,6 +244,7 @@ struct EigenBatch {
   int merged;                // 1: skewtrieigen_merged! (tridiagonal input; no mem deflation of :355)
   int chain_nmax;            // matrices with n > chain_nmax skip the QR chain and its vectors
                              // (their eigenpairs come from bisection and twisted vectors)
+  int max_iter = 0;          // QR sweeps before SKEW_NO_CONVERGENCE (0: 30 n, skeweigen.jl:340)
 };
 // Eigenpairs of G skew tridiagonals of one size n (subdiagonals e_g, n apart) by
 // bisection (values descending, exact +-pairs, also into vals_out[idx[mb]]) and
@@ -233,7 +279,7 @@ cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, doubl
 size_t persist_ws_extra_doubles();
 // One cooperative launch for all panels (grid barriers with bounded waits); then the tail.
 cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double* tau, double* ev, int* info,
-                                          double* ws, int sms, int* err_dev, cudaStream_t st);
+                                          double* ws, int sms, int* err_dev, const Tuning& T, cudaStream_t st);
 cudaError_t launch_pf_from_tridiag(const double* ev, const double* tau, int n, double* logpf, double* sign, int* info,
                                    const double* notskew, cudaStream_t st);
 cudaError_t launch_check_skew(const double* A, int64_t lda, int n, double* flag, int sms, cudaStream_t st);
@@ -251,6 +297,7 @@ struct PfzParams {
   double* phase;  // [2 count] cis(phase) (nullable)
   double* pf;     // [2 count] the product (nullable)
   int* status;    // [count] (nullable)
+  int nt;         // threads per CTA of the shared-memory kernel (0: chosen by n)
 };
 struct PfzGridParams {
   zc* A;  // in place on the strictly lower triangle
@@ -268,15 +315,17 @@ struct PfzGridParams {
   double* phase;
   double* pf;
   int* info;
+  long long poll_limit;  // polls before a grid barrier gives up
+  int skip_cta;          // >= 0: this CTA never arrives (a test of the timeout path)
 };
 size_t pfz_cta_smem(int n, bool smem_matrix);
 bool pfz_smem_fits(int n);
-int pfz_cta_occupancy(int n, bool smem_matrix);
+int pfz_cta_occupancy(int n, bool smem_matrix, int nt);
 cudaError_t launch_pfz_cta(const PfzParams& P, int grid, cudaStream_t st);
 size_t pfz_grid_ws_doubles(int n);
 // n >= 1 (odd n: Pf = 0); check != 0 tests A == -transpose(A) first (info = SKEW_NOT_SKEW).
 cudaError_t launch_pfz_grid(zc* A, int64_t lda, int n, int check, double* logpf, double* phase, double* pf,
-                            int* info, double* ws, int sms, cudaStream_t st);
+                            int* info, double* ws, int sms, const Tuning& T, cudaStream_t st);
 
 // svdvals / svd from the eigenpairs (skew_svd.cu).  Stable rank sort of each problem's
 // values by |v| descending: perm (batch x n, nullable), S (sstride apart, nullable),

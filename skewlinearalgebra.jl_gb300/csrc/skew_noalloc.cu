@@ -16,15 +16,20 @@
 //     library until the process exits.
 //   * The device address of the array is looked up with cudaGetSymbolAddress
 //     on the first call made on each device (with that device current); make
-//     that first call before any stream capture.
+//     that first call before any stream capture.  The address is kept per
+//     device and per CUDA context: after a device reset (a new primary
+//     context), the next call looks it up again.
 //   * All calls share the one array.  Each call writes every entry it reads
 //     before reading it, so nothing has to start at zero, but calls that
 //     overlap on the GPU (different streams, or threads) race on it and give
 //     wrong results: serialise them.
+//   * Values come out sorted descending (bisection on the tridiagonal form),
+//     the order of the reference's own fallback and of eigvals(A, 1:n); they
+//     are the eigenvalues skew_eigvals_d returns in the QR's order.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <atomic>
+#include <mutex>
 
 #include "../../include/skewgpu.h"
 #include "skew_internal.h"
@@ -36,19 +41,58 @@ namespace {
 static __device__ __align__(256) double g_eigvals_scratch[SKEW_NOALLOC_EIGVALS_NMAX + 2];
 
 constexpr int kMaxDevices = 64;
-std::atomic<double*> g_scratch_addr[kMaxDevices];
 
-// Device address of g_eigvals_scratch on the current device (looked up once).
+// Cached device address of g_eigvals_scratch per device, with the id of the CUDA
+// context it belongs to (a device reset destroys the context and the module with it).
+struct ScratchSlot {
+  double* addr = nullptr;
+  unsigned long long ctx = 0;
+};
+ScratchSlot g_slot[kMaxDevices];
+std::mutex g_slot_mu;
+
+// Id of the calling thread's current CUDA context (unique for the process's
+// lifetime), or 0 if there is none; through the driver entry points the runtime
+// hands out, so the library does not link the driver library itself.
+unsigned long long current_context_id() {
+  typedef int (*GetCurrentFn)(void**);
+  typedef int (*GetIdFn)(void*, unsigned long long*);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = (GetCurrentFn)f;
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = (GetIdFn)f;
+  });
+  void* ctx = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+  return id;
+}
+
+// Device address of g_eigvals_scratch on the current device and context.
 int scratch_address(double** out) {
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return SKEW_CUDA_ERROR;
   if (dev < 0 || dev >= kMaxDevices) return SKEW_UNSUPPORTED;
-  double* p = g_scratch_addr[dev].load(std::memory_order_acquire);
-  if (!p) {
+  std::lock_guard<std::mutex> lock(g_slot_mu);
+  ScratchSlot& slot = g_slot[dev];
+  const unsigned long long ctx = current_context_id();
+  if (!slot.addr || ctx == 0 || ctx != slot.ctx) {
+    double* p = nullptr;
+    // also makes the device's primary context current if no context is yet
     if (cudaGetSymbolAddress((void**)&p, g_eigvals_scratch) != cudaSuccess || !p) return SKEW_CUDA_ERROR;
-    g_scratch_addr[dev].store(p, std::memory_order_release);
+    slot.addr = p;
+    slot.ctx = current_context_id();
   }
-  *out = p;
+  *out = slot.addr;
   return SKEW_OK;
 }
 
@@ -60,7 +104,7 @@ extern "C" SKEW_API int skew_eigvals_noalloc_d(double* A, int64_t n, int64_t lda
   if (n > SKEW_NOALLOC_EIGVALS_NMAX) return SKEW_UNSUPPORTED;
   cudaStream_t st = (cudaStream_t)stream;
   if (n == 0) return SKEW_OK;
-  if (n == 1) {  // skeweigvals! returns [A[1,1]] for n == 1 (eigen.jl:314)
+  if (n == 1) {  // skeweigvals! returns [A[1,1]] for n == 1 (eigen.jl:51)
     if (cudaMemcpyAsync(vals_im, A, sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
       return SKEW_CUDA_ERROR;
     if (info && cudaMemsetAsync(info, 0, sizeof(int), st) != cudaSuccess) return SKEW_CUDA_ERROR;

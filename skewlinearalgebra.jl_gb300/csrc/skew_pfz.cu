@@ -448,7 +448,7 @@ namespace {
 constexpr int GZ_NT = 512;
 constexpr int GZ_NW = GZ_NT / 32;
 constexpr int GZ_TC = 16;  // columns per tile (rows per tile: 32, one per lane)
-constexpr long long GZ_POLL_LIMIT = 1LL << 24;
+constexpr long long GZ_POLL_LIMIT = 1LL << 24;  // default polls before a grid barrier gives up
 
 __device__ __forceinline__ zc ldz(const zc* p) {
   const double2 v = __ldcg((const double2*)p);
@@ -460,10 +460,17 @@ __device__ __forceinline__ void stz(zc* p, zc x) { __stcg((double2*)p, make_doub
 // counter reaches (b + 1) * gridDim.x, so each CTA makes one atomic and then
 // polls with acquire loads (no reset and no second word).  Bounded: false if
 // it gave up (error recorded) or another CTA did.
-__device__ bool pfz_gsync(unsigned* sync, int* err) {
+// poll_limit bounds the wait; the CTA skip_cta (>= 0) never arrives, so the others'
+// waits run out (a test of the timeout path) while it waits, bounded, for that.
+__device__ bool pfz_gsync(unsigned* sync, int* err, long long poll_limit, int skip_cta) {
   __shared__ int s_ok;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && (int)blockIdx.x == skip_cta) {
+    volatile int* verr = err;
+    long long it = 0;
+    while (!*verr && ++it <= poll_limit) __nanosleep(32);
+    s_ok = 0;
+  } else if (threadIdx.x == 0) {
     volatile int* verr = err;
     __threadfence();
     const unsigned old = atomicAdd(sync, 1u);
@@ -479,7 +486,7 @@ __device__ bool pfz_gsync(unsigned* sync, int* err) {
           ok = 0;
           break;
         }
-        if (it > GZ_POLL_LIMIT) {
+        if (it > poll_limit) {
           atomicExch(err, 1);
           ok = 0;
           break;
@@ -534,7 +541,7 @@ __global__ void __launch_bounds__(GZ_NT) pfz_grid_kernel(PfzGridParams P) {
     }
   }
   int status = SKEW_OK, swaps = 0;
-  if (!pfz_gsync(P.sync, P.err)) return;
+  if (!pfz_gsync(P.sync, P.err, P.poll_limit, P.skip_cta)) return;
   for (int k = 0; k < n - 1; k += 2) {
     const int p = k + 1, q = p + 1, m = n - q;
     // ---- phase T: the pivot (every CTA reduces the partials), tau and c ----
@@ -592,7 +599,7 @@ __global__ void __launch_bounds__(GZ_NT) pfz_grid_kernel(PfzGridParams P) {
       stz(P.tau + i, t);
       stz(P.cc + i, c);
     }
-    if (!pfz_gsync(P.sync, P.err)) return;
+    if (!pfz_gsync(P.sync, P.err, P.poll_limit, P.skip_cta)) return;
     // ---- phase U: 32 x 16 tiles of the trailing lower triangle ----
     const int nrb = (m + 31) / 32, ncb = (m + GZ_TC - 1) / GZ_TC;
     zc* tcw = s_tc[warp];
@@ -652,7 +659,7 @@ __global__ void __launch_bounds__(GZ_NT) pfz_grid_kernel(PfzGridParams P) {
       }
     }
     nparts = nrb;
-    if (!pfz_gsync(P.sync, P.err)) return;
+    if (!pfz_gsync(P.sync, P.err, P.poll_limit, P.skip_cta)) return;
   }
 #undef AZ
   if (blockIdx.x == 0 && warp == 0) {
@@ -671,15 +678,10 @@ size_t pfz_cta_smem(int n, bool smem_matrix) {
   return b;
 }
 
-static int pfz_threads(int n, bool smem_matrix) {
+// forced: the tuning key pfz_nt (64/128/256/512 for the shared-memory kernel), or 0
+static int pfz_threads(int n, bool smem_matrix, int forced) {
   if (!smem_matrix) return 512;
-  static int forced = -1;  // SKEW_PFZ_NT: 64/128/256/512 for the shared-memory kernel (sweeps)
-  if (forced < 0) {
-    const char* e = getenv("SKEW_PFZ_NT");
-    const int v = (e && *e) ? atoi(e) : 0;
-    forced = (v == 64 || v == 128 || v == 256 || v == 512) ? v : 0;
-  }
-  if (forced) return forced;
+  if (forced == 64 || forced == 128 || forced == 256 || forced == 512) return forced;
   // measured on GB300 (batches of 1024-4096): 128 threads best at n = 64, 256 at
   // n = 96 (+10 % over 128), 512 at n = 128-160 (+3-5 % over 256)
   if (n <= 48) return 64;
@@ -717,10 +719,10 @@ bool pfz_smem_fits(int n) {
   return pfz_cta_smem(n, true) + 1024 <= (size_t)optin;  // + the kernel's static shared memory
 }
 
-int pfz_cta_occupancy(int n, bool smem_matrix) {
+int pfz_cta_occupancy(int n, bool smem_matrix, int nt) {
   const size_t smem = pfz_cta_smem(n, smem_matrix);
   if (!smem_matrix) return pfz_occ_t<512, false>(smem);
-  switch (pfz_threads(n, true)) {
+  switch (pfz_threads(n, true, nt)) {
     case 64: return pfz_occ_t<64, true>(smem);
     case 128: return pfz_occ_t<128, true>(smem);
     case 256: return pfz_occ_t<256, true>(smem);
@@ -732,7 +734,7 @@ cudaError_t launch_pfz_cta(const PfzParams& P, int grid, cudaStream_t st) {
   const bool sm = P.smem_matrix != 0;
   const size_t smem = pfz_cta_smem(P.n, sm);
   if (!sm) return pfz_launch_t<512, false>(P, grid, smem, st);
-  switch (pfz_threads(P.n, true)) {
+  switch (pfz_threads(P.n, true, P.nt)) {
     case 64: return pfz_launch_t<64, true>(P, grid, smem, st);
     case 128: return pfz_launch_t<128, true>(P, grid, smem, st);
     case 256: return pfz_launch_t<256, true>(P, grid, smem, st);
@@ -767,8 +769,10 @@ size_t pfz_grid_ws_doubles(int n) {
 }
 
 cudaError_t launch_pfz_grid(zc* A, int64_t lda, int n, int check, double* logpf, double* phase, double* pf,
-                            int* info, double* ws, int sms, cudaStream_t st) {
+                            int* info, double* ws, int sms, const Tuning& T, cudaStream_t st) {
   PfzGridParams P;
+  P.poll_limit = T.wait_polls > 0 ? T.wait_polls : GZ_POLL_LIMIT;
+  P.skip_cta = T.wait_skip_cta;
   P.A = A;
   P.lda = lda;
   P.n = n;
@@ -802,10 +806,7 @@ cudaError_t launch_pfz_grid(zc* A, int64_t lda, int n, int check, double* logpf,
   // fewer CTAs for smaller matrices: the two grid barriers per step cost more
   // with more CTAs, and the trailing block holds less work
   int grid = std::min(sms, std::max(16, n / 8));
-  {
-    const char* g = getenv("SKEW_PFZ_CTAS");
-    if (g && *g) grid = std::max(1, std::min(sms * occ, atoi(g)));
-  }
+  if (T.pfz_ctas > 0) grid = std::max(1, std::min(sms * occ, T.pfz_ctas));
   void* args[] = {&P};
   e = cudaLaunchCooperativeKernel((const void*)pfz_grid_kernel, dim3(grid), dim3(GZ_NT), args, 0, st);
   if (e != cudaSuccess) return e;

@@ -69,14 +69,22 @@ __device__ void reducetozero_dev(double* ev, int n) {
 }
 
 // implicitstep_novec (skeweigen.jl:73-103); n = active size - 1, start 1-based.
+// The chain is serial: step i needs the rotation of step i-1.  The three entries
+// a step reads besides ev[i+1] are the ones the previous step just wrote, so they
+// are carried in registers instead of going through memory, and ev[i+1], which no
+// step of this sweep has touched yet, is loaded one step ahead.  Every store of
+// the reference's step is still made, in the same order, so ev holds the same
+// values at every step and after an early return.
 __device__ int implicitstep_dev(double* ev, int n, int start) {
   double bulge = 0.0;
   const double shift = __dmul_rn(ev[n - 1], ev[n - 1]);
   const double tol = 2.220446049250313e-16;  // eps(Float64)
+  double a = 0.0;              // ev[i-2] (zero at i == start, as the reference's alpha)
+  double b = ev[start - 1];    // ev[i-1]
+  double g = ev[start];        // ev[i]
+  double z = (start < n - 1) ? ev[start + 1] : 0.0;  // ev[i+1], untouched this sweep
   for (int i = start; i <= n - 1; i++) {
-    const double a = (i > start ? ev[i - 2] : 0.0);
-    const double b = ev[i - 1];
-    const double g = ev[i];
+    const double zn = (i + 2 <= n - 1) ? ev[i + 2] : 0.0;  // next step's ev[i+1]
     double c, s;
     if (i > start) {
       givens(a, bulge, c, s);
@@ -86,13 +94,19 @@ __device__ int implicitstep_dev(double* ev, int n, int start) {
       givens(x1, x2, c, s);
     }
     if (i > 1) ev[i - 2] = __dadd_rn(__dmul_rn(c, a), __dmul_rn(s, bulge));
-    ev[i - 1] = __dsub_rn(__dmul_rn(c, b), __dmul_rn(s, g));
-    ev[i] = __dadd_rn(__dmul_rn(s, b), __dmul_rn(c, g));
+    const double nb = __dsub_rn(__dmul_rn(c, b), __dmul_rn(s, g));
+    const double ng = __dadd_rn(__dmul_rn(s, b), __dmul_rn(c, g));
+    ev[i - 1] = nb;
+    ev[i] = ng;
     if (i < n - 1) {
-      const double z = ev[i + 1];
-      ev[i + 1] = __dmul_rn(z, c);
+      const double nz = __dmul_rn(z, c);
+      ev[i + 1] = nz;
       bulge = __dmul_rn(s, z);
-      if (fabs(bulge) < tol && fabs(ev[i - 1]) < tol) return i + 1;
+      if (fabs(bulge) < tol && fabs(nb) < tol) return i + 1;
+      a = nb;
+      b = ng;
+      g = nz;
+      z = zn;
     }
   }
   return start;
@@ -119,7 +133,7 @@ __device__ int sturm_count(const double* e, int n, double x, double pivmin) {
 // vals[N] receives the imaginary parts in the reference's order.  On stagnation
 // the active size n is returned in *fb_n (vals[0..n) and ev[0..n-1) are then
 // left to the fallback kernel).
-__device__ int skewtrieigvals_dev(double* ev, int N, double* vals, int* fb_n) {
+__device__ int skewtrieigvals_dev(double* ev, int N, double* vals, int* fb_n, int max_iter_cap) {
   int n = N;
   for (int i = 0; i < N; i++) vals[i] = 0.0;
   if (n & 1) {
@@ -127,7 +141,7 @@ __device__ int skewtrieigvals_dev(double* ev, int N, double* vals, int* fb_n) {
     reducetozero_dev(ev, n);
   }
   const double tol = 10.0 * 2.220446049250313e-16;
-  const int max_iter = 30 * n;
+  const int max_iter = max_iter_cap > 0 ? max_iter_cap : 30 * n;
   int iter = 0, count_static = 0, start = 1;
   double mem = 1.0;
   while (n > 2 && iter < max_iter) {
@@ -175,7 +189,7 @@ __global__ void batch_trieig_kernel(TrieigParams P) {
   if (P.evwork != P.ev_all)
     for (int i = 0; i + 1 < N; i++) ev[i] = P.ev_all[P.ev_off[b] + i];
   int fb_n = 0;
-  const int st = (N >= 1) ? skewtrieigvals_dev(ev, N, P.vals[b], &fb_n) : SKEW_OK;
+  const int st = (N >= 1) ? skewtrieigvals_dev(ev, N, P.vals[b], &fb_n, P.max_iter) : SKEW_OK;
   if (st == SKEW_FALLBACK_USED) {
     const unsigned k = atomicAdd(P.fallback, 1u);
     P.fallback[2 + k] = (unsigned)b;

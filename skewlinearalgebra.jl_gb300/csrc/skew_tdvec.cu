@@ -60,7 +60,16 @@ struct TdvecLayout {
   double* bandU;    // KP x (LW + 1) raw dots over even rows
   double* bandV;    // KP x (LW + 1) raw dots over odd rows
   double* T;        // npan x WB x WB
+  // gate != null: every kernel of the pipeline returns at once unless *gate ==
+  // gate_on (two pipelines are queued and the device picks one, no host sync)
+  const int* gate;
+  int gate_on;
 };
+
+// problem mb of the launch (blockIdx.z of the batched kernels, 0 for one matrix)
+__device__ __forceinline__ bool gated_off(const TdvecLayout& L, int mb = 0) {
+  return L.gate && L.gate[mb] != L.gate_on;
+}
 
 size_t large_eigen_ws_doubles(int n);
 
@@ -82,6 +91,8 @@ static TdvecLayout layout(int n, double* ws, bool full = false, const double* dg
   L.bandU = L.nrm2 + L.KP;
   L.bandV = L.bandU + (size_t)L.KP * (LW + 1);
   L.T = L.bandV + (size_t)L.KP * (LW + 1);
+  L.gate = nullptr;
+  L.gate_on = 0;
   return L;
 }
 
@@ -112,6 +123,7 @@ __device__ __forceinline__ TdvecLayout at_problem(TdvecLayout L, int mb) {
 __global__ void __launch_bounds__(TW_NT) twisted_kernel(const double* __restrict__ e, const double* __restrict__ vals,
                                                         const double* __restrict__ bp, TdvecLayout L0) {
   const int mb = blockIdx.z;
+  if (gated_off(L0, mb)) return;
   const TdvecLayout L = at_problem(L0, mb);
   e += (size_t)mb * L.n;
   vals += (size_t)mb * L.n;
@@ -146,6 +158,7 @@ __global__ void __launch_bounds__(TW_NT) twisted_kernel(const double* __restrict
 // unit length, s_k = sqrt(2)/|z_k| (sigma > 0) or 1/|z_k| (the zero-eigenvalue
 // vector, even rows only); full mode: s_k = 1/|z_k|.  X may be L.dp.
 __global__ void tdvec_normalize_kernel(TdvecLayout L0, double* X0) {
+  if (gated_off(L0, blockIdx.z)) return;
   const TdvecLayout L = at_problem(L0, blockIdx.z);
   double* X = X0 + (size_t)blockIdx.z * L0.mstride;
   const int64_t KP = L.KP;
@@ -173,6 +186,7 @@ constexpr int BD_PAIRS = 32 * (LW + 1);
 constexpr int BD_PER = (BD_PAIRS + BD_NT - 1) / BD_NT;
 
 __global__ void __launch_bounds__(BD_NT) band_dots_kernel(TdvecLayout L0, const double* X0) {
+  if (gated_off(L0, blockIdx.z)) return;
   const TdvecLayout L = at_problem(L0, blockIdx.z);
   const double* X = X0 + (size_t)blockIdx.z * L0.mstride;
   __shared__ double zs[RC][BD_COLS + 1];
@@ -226,6 +240,7 @@ constexpr int LA_NT = 256;
 constexpr int LA_COLS = 32 + 2 * LW;
 
 __global__ void __launch_bounds__(LA_NT) band_apply_kernel(TdvecLayout L0, const double* X0, double* Y0) {
+  if (gated_off(L0, blockIdx.z)) return;
   const TdvecLayout L = at_problem(L0, blockIdx.z);
   const double* X = X0 + (size_t)blockIdx.z * L0.mstride;
   double* Y = Y0 + (size_t)blockIdx.z * L0.mstride;
@@ -278,6 +293,7 @@ __global__ void __launch_bounds__(LA_NT) band_apply_kernel(TdvecLayout L0, const
 __global__ void __launch_bounds__(LA_NT) tdvec_write_skew_kernel(TdvecLayout L, const double* __restrict__ X,
                                                                  double* __restrict__ Vr, double* __restrict__ Vi,
                                                                  int64_t ldv) {
+  if (gated_off(L)) return;
   __shared__ double out[RC][33];
   const int k0 = blockIdx.x * 32, i0 = blockIdx.y * RC;
   const int n = L.n;
@@ -382,6 +398,7 @@ constexpr int WT_RC = 16;  // rows per staged chunk of the factor kernel
 // receive T as the recurrence produces it (a diagonal G entry is never needed).
 __global__ void __launch_bounds__(WT_NT) wy_factor_kernel(const double* __restrict__ A, int64_t lda,
                                                           const double* __restrict__ tau, TdvecLayout L) {
+  if (gated_off(L)) return;
   __shared__ double Vs[WT_RC][WB + 1];
   __shared__ double M[WB][WB + 1];
   const int b = blockIdx.x;
@@ -461,6 +478,7 @@ struct StripParams {
 };
 
 __global__ void __launch_bounds__(BT_NT) back_strip_kernel(StripParams P) {
+  if (gated_off(P.L)) return;
   extern __shared__ __align__(16) double bsm[];
   double(*Ts)[WB + 1] = reinterpret_cast<double(*)[WB + 1]>(bsm);                   // WB x (WB+1)
   double(*Ws)[SW + 1] = reinterpret_cast<double(*)[SW + 1]>(bsm + WB * (WB + 1));  // WB x (SW+1)
@@ -580,7 +598,9 @@ __global__ void __launch_bounds__(BT_NT) back_strip_kernel(StripParams P) {
 }
 
 // 6. +sigma columns: Vr[:, k] = Vr[:, n-1-k], Vi[:, k] = -Vi[:, n-1-k]; odd n: Vi[:, h] = 0
-__global__ void mirror_kernel(double* __restrict__ Vr, double* __restrict__ Vi, int64_t ldv, int n) {
+__global__ void mirror_kernel(double* __restrict__ Vr, double* __restrict__ Vi, int64_t ldv, int n,
+                              const int* __restrict__ gate) {
+  if (gate && *gate != 0) return;  // the skew-mode pipeline only
   const int h = n / 2;
   const int k = blockIdx.y;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -604,6 +624,7 @@ static size_t strip_smem_bytes() {
 __global__ void __launch_bounds__(LA_NT) tdvec_write_skew_batch_kernel(TdvecLayout L0, const double* X0,
                                                                        double* const* Vr_all, double* const* Vi_all,
                                                                        const int32_t* idx) {
+  if (gated_off(L0, blockIdx.z)) return;
   __shared__ double out[RC][33];
   const int mb = blockIdx.z;
   const TdvecLayout L = at_problem(L0, mb);
@@ -642,7 +663,9 @@ __global__ void __launch_bounds__(LA_NT) tdvec_write_skew_batch_kernel(TdvecLayo
   }
 }
 
-__global__ void mirror_batch_kernel(double* const* Vr_all, double* const* Vi_all, const int32_t* idx, int n) {
+__global__ void mirror_batch_kernel(double* const* Vr_all, double* const* Vi_all, const int32_t* idx, int n,
+                                    const int* __restrict__ gate) {
+  if (gate && gate[blockIdx.z] != 0) return;  // the skew-mode pipeline only
   double* Vr = Vr_all[idx[blockIdx.z]];
   double* Vi = Vi_all[idx[blockIdx.z]];
   const int h = n / 2;
@@ -659,60 +682,245 @@ __global__ void mirror_batch_kernel(double* const* Vr_all, double* const* Vi_all
   }
 }
 
-size_t skew_vectors_batch_ws_doubles(int n) { return large_eigen_ws_doubles(n); }
+// ---------------------------------------------------------------------------
+// Several zero eigenvalues.  Where ev has exact zeros, the tridiagonal is a direct
+// sum of blocks and each odd-size block brings one zero eigenvalue.  More zero
+// eigenvalues than n mod 2 do not fit the +-sigma pairing of the skew mode, so the
+// whole problem is then solved in full mode, as the reference's fallback
+// skewtrieigen_backup! (skeweigen.jl:470-489) solves it: every eigenpair of
+// SymTridiagonal(0, ev), each column laid out on its own.
+// ---------------------------------------------------------------------------
+constexpr int OB_NT = 1024;
 
-cudaError_t skew_vectors_batch(const double* e_g, int n, int G, const double* vals_g, const double* bp_g,
-                               double* const* Vr, double* const* Vi, const int32_t* idx, double* ws,
-                               cudaStream_t st) {
-  if (n < 3 || G <= 0) return cudaErrorInvalidValue;
-  const TdvecLayout L = layout(n, ws);
-  twisted_kernel<<<dim3(L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), 1, G), TW_NT, 0, st>>>(e_g, vals_g, bp_g, L);
+// gate <- 1 when the exact splits of ev leave more odd-size blocks than n mod 2, else
+// 0; for full mode also mu[j] = -vals[j] (ascending) and bpf = (bound, pivmin, -bound).
+// One CTA per problem (blockIdx.x; ev, vals, mu n apart, bp, bpf 8 apart): each thread
+// summarises a contiguous chunk of ev (first and last zero and the odd gaps between its
+// zeros), thread 0 joins the chunks in order.
+__global__ void __launch_bounds__(OB_NT) odd_blocks_kernel(const double* __restrict__ ev, int n,
+                                                           const double* __restrict__ vals,
+                                                           const double* __restrict__ bp, int* __restrict__ gate,
+                                                           double* __restrict__ mu, double* __restrict__ bpf) {
+  __shared__ int first[OB_NT], last[OB_NT], odd[OB_NT];
+  const int mb = blockIdx.x;
+  ev += (size_t)mb * n;
+  vals += (size_t)mb * n;
+  mu += (size_t)mb * n;
+  bp += (size_t)mb * 8;
+  bpf += (size_t)mb * 8;
+  gate += mb;
+  const int m = n - 1;  // entries of ev; a zero at ev[i] ends a block at row i
+  const int chunk = (m + OB_NT - 1) / OB_NT;
+  const int t = threadIdx.x;
+  int f = -1, l = -1, c = 0;
+  for (int i = t * chunk; i < min(m, (t + 1) * chunk); i++) {
+    if (ev[i] == 0.0) {
+      if (l >= 0) c += (i - l) & 1;
+      else f = i;
+      l = i;
+    }
+  }
+  first[t] = f;
+  last[t] = l;
+  odd[t] = c;
+  for (int j = t; j < n; j += OB_NT) mu[j] = -vals[j];
+  __syncthreads();
+  if (t == 0) {
+    int prev = -1, count = 0;  // previous zero position (-1: the start of row 0)
+    for (int q = 0; q < OB_NT; q++) {
+      if (first[q] < 0) continue;
+      count += ((first[q] - prev) & 1) + odd[q];
+      prev = last[q];
+    }
+    count += ((n - 1 - prev) & 1);  // the last block
+    *gate = (count > (n & 1)) ? 1 : 0;
+    bpf[0] = bp[0];
+    bpf[1] = bp[1];
+    bpf[2] = -bp[0];
+  }
+}
+
+// full mode into the fallback's layout (skeweigen.jl:476-487): column j holds the
+// eigenvector w_j of SymTridiagonal(0, ev) for mu_j = -vals_j, real on even 0-based
+// rows and imaginary on odd rows, with the sign (-1)^(i/2) of row pair i/2
+__global__ void __launch_bounds__(LA_NT) tdvec_write_fallback_kernel(TdvecLayout L, const double* __restrict__ X,
+                                                                     double* __restrict__ Vr,
+                                                                     double* __restrict__ Vi, int64_t ldv) {
+  if (gated_off(L)) return;
+  __shared__ double out[RC][33];
+  const int k0 = blockIdx.x * 32, i0 = blockIdx.y * RC;
+  const int n = L.n;
+  const int64_t KP = L.KP;
+  for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
+    const int kk = idx % 32, rr = idx / 32;
+    const int i = i0 + rr, k = k0 + kk;
+    double o = 0.0;
+    if (i < n && k < L.K) {
+      o = X[(int64_t)i * KP + k];
+      if ((i >> 1) & 1) o = neg(o);
+    }
+    out[rr][kk] = o;
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < RC * 32; idx += LA_NT) {
+    const int kk = idx / RC, rr = idx - kk * RC;
+    const int i = i0 + rr, k = k0 + kk;
+    if (i >= n || k >= L.K) continue;
+    const double o = out[rr][kk];
+    const int64_t at = i + (int64_t)k * ldv;
+    Vr[at] = (i & 1) ? 0.0 : o;
+    Vi[at] = (i & 1) ? o : 0.0;
+  }
+}
+
+// the same for problem blockIdx.z of a batch: Vr[idx[mb]], Vi[idx[mb]] (n x n, ld n)
+__global__ void __launch_bounds__(LA_NT) tdvec_write_fallback_batch_kernel(TdvecLayout L0, const double* X0,
+                                                                           double* const* Vr_all,
+                                                                           double* const* Vi_all,
+                                                                           const int32_t* idx) {
+  const int mb = blockIdx.z;
+  if (gated_off(L0, mb)) return;
+  __shared__ double out[RC][33];
+  const TdvecLayout L = at_problem(L0, mb);
+  const double* X = X0 + (size_t)mb * L0.mstride;
+  double* Vr = Vr_all[idx[mb]];
+  double* Vi = Vi_all[idx[mb]];
+  const int k0 = blockIdx.x * 32, i0 = blockIdx.y * RC;
+  const int n = L.n;
+  const int64_t KP = L.KP;
+  for (int q = threadIdx.x; q < RC * 32; q += LA_NT) {
+    const int kk = q % 32, rr = q / 32;
+    const int i = i0 + rr, k = k0 + kk;
+    double o = 0.0;
+    if (i < n && k < L.K) {
+      o = X[(int64_t)i * KP + k];
+      if ((i >> 1) & 1) o = neg(o);
+    }
+    out[rr][kk] = o;
+  }
+  __syncthreads();
+  for (int q = threadIdx.x; q < RC * 32; q += LA_NT) {
+    const int kk = q / RC, rr = q - kk * RC;
+    const int i = i0 + rr, k = k0 + kk;
+    if (i >= n || k >= L.K) continue;
+    const double o = out[rr][kk];
+    const int64_t at = i + (int64_t)k * n;
+    Vr[at] = (i & 1) ? 0.0 : o;
+    Vi[at] = (i & 1) ? o : 0.0;
+  }
+}
+
+static cudaError_t back_transform(const double* A, int64_t lda, const double* tau, const TdvecLayout& L, double* Vr,
+                                  double* Vi, int64_t ldv, int cr0, int ci0, cudaStream_t st) {
+  const int n = L.n;
+  wy_factor_kernel<<<L.npan, WT_NT, 0, st>>>(A, lda, tau, L);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
-  double* X = tdvec_orthogonalize(L, G, st);
-  tdvec_write_skew_batch_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC, G), LA_NT, 0, st>>>(L, X, Vr, Vi, idx);
-  e = cudaGetLastError();
+  StripParams P;
+  P.A = A;
+  P.lda = lda;
+  P.tau = tau;
+  P.L = L;
+  P.Xr = Vr;
+  P.Xi = Vi;
+  P.ldv = ldv;
+  P.cr0 = cr0;
+  P.ci0 = ci0;
+  P.nstr_r = (n - cr0 + SW - 1) / SW;
+  const int nstr_i = (n - ci0 + SW - 1) / SW;
+  static std::atomic<uint64_t> raised{0};
+  e = raise_smem_limit_once((const void*)back_strip_kernel, raised);
   if (e != cudaSuccess) return e;
-  mirror_batch_kernel<<<dim3((n + 255) / 256, L.h + (n & 1), G), 256, 0, st>>>(Vr, Vi, idx, n);
+  back_strip_kernel<<<P.nstr_r + nstr_i, BT_NT, strip_smem_bytes(), st>>>(P);
   return cudaGetLastError();
 }
 
+size_t large_eigen_aux_doubles(int n) { return (size_t)n + 8; }
+
+// gate (device int) and aux (large_eigen_aux_doubles(n)) are scratch of the caller.
 cudaError_t large_eigen_vectors(const double* A, int64_t lda, int n, const double* tau, const double* ev,
                                 const double* vals, const double* bp, double* Vr, double* Vi, int64_t ldv, double* ws,
-                                cudaStream_t st) {
+                                int* gate, double* aux, cudaStream_t st) {
   if (n < 3) return cudaErrorInvalidValue;
-  const TdvecLayout L = layout(n, ws);
-  twisted_kernel<<<L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), TW_NT, 0, st>>>(ev, vals, bp, L);
+  double* mu = aux;
+  double* bpf = aux + n;
+  odd_blocks_kernel<<<1, OB_NT, 0, st>>>(ev, n, vals, bp, gate, mu, bpf);
   cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // skew mode (gate == 0): -sigma vectors, back-transformed, +sigma mirrored
+  TdvecLayout L = layout(n, ws);
+  L.gate = gate;
+  L.gate_on = 0;
+  twisted_kernel<<<L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), TW_NT, 0, st>>>(ev, vals, bp, L);
+  e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   double* X = tdvec_orthogonalize(L, 1, st);
   tdvec_write_skew_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC), LA_NT, 0, st>>>(L, X, Vr, Vi, ldv);
   e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   if (A) {  // A == null: a tridiagonal input, Q = I
-    wy_factor_kernel<<<L.npan, WT_NT, 0, st>>>(A, lda, tau, L);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-    StripParams P;
-    P.A = A;
-    P.lda = lda;
-    P.tau = tau;
-    P.L = L;
-    P.Xr = Vr;
-    P.Xi = Vi;
-    P.ldv = ldv;
-    P.cr0 = L.h;                // -sigma columns and the zero vector
-    P.ci0 = L.h + (n & 1);      // -sigma columns
-    P.nstr_r = (n - P.cr0 + SW - 1) / SW;
-    const int nstr_i = (n - P.ci0 + SW - 1) / SW;
-    static std::atomic<uint64_t> raised{0};
-    e = raise_smem_limit_once((const void*)back_strip_kernel, raised);
-    if (e != cudaSuccess) return e;
-    back_strip_kernel<<<P.nstr_r + nstr_i, BT_NT, strip_smem_bytes(), st>>>(P);
-    e = cudaGetLastError();
+    // -sigma columns and the zero vector of Vr, -sigma columns of Vi
+    e = back_transform(A, lda, tau, L, Vr, Vi, ldv, L.h, L.h + (n & 1), st);
     if (e != cudaSuccess) return e;
   }
-  mirror_kernel<<<dim3((n + 255) / 256, L.h + (n & 1)), 256, 0, st>>>(Vr, Vi, ldv, n);
+  mirror_kernel<<<dim3((n + 255) / 256, L.h + (n & 1)), 256, 0, st>>>(Vr, Vi, ldv, n, gate);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // full mode (gate == 1): every eigenpair, each column back-transformed
+  TdvecLayout F = layout(n, ws, true, nullptr);
+  F.gate = gate;
+  F.gate_on = 1;
+  twisted_kernel<<<F.KP / TW_NT + (F.KP % TW_NT ? 1 : 0), TW_NT, 0, st>>>(ev, mu, bpf, F);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  X = tdvec_orthogonalize(F, 1, st);
+  tdvec_write_fallback_kernel<<<dim3(F.KP / 32, (n + RC - 1) / RC), LA_NT, 0, st>>>(F, X, Vr, Vi, ldv);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  if (A) return back_transform(A, lda, tau, F, Vr, Vi, ldv, 0, 0, st);
+  return cudaSuccess;
+}
+
+
+// Batched skew-mode vectors for G problems of one size.  ws holds each problem's
+// workspace (large_eigen_ws_doubles(n), mstride apart), then per problem the
+// full-mode inputs mu (n), bpf (8) and the gate (as in large_eigen_vectors).
+size_t skew_vectors_batch_ws_doubles(int n) { return large_eigen_ws_doubles(n) + (size_t)n + 16; }
+
+cudaError_t skew_vectors_batch(const double* e_g, int n, int G, const double* vals_g, const double* bp_g,
+                               double* const* Vr, double* const* Vi, const int32_t* idx, double* ws,
+                               cudaStream_t st) {
+  if (n < 3 || G <= 0) return cudaErrorInvalidValue;
+  double* aux = ws + (size_t)G * large_eigen_ws_doubles(n);
+  double* mu = aux;
+  double* bpf = aux + (size_t)G * n;
+  int* gate = (int*)(bpf + (size_t)G * 8);
+  odd_blocks_kernel<<<G, OB_NT, 0, st>>>(e_g, n, vals_g, bp_g, gate, mu, bpf);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // skew mode (gate 0): the -sigma vectors, then the +sigma mirror
+  TdvecLayout L = layout(n, ws);
+  L.gate = gate;
+  L.gate_on = 0;
+  twisted_kernel<<<dim3(L.KP / TW_NT + (L.KP % TW_NT ? 1 : 0), 1, G), TW_NT, 0, st>>>(e_g, vals_g, bp_g, L);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  double* X = tdvec_orthogonalize(L, G, st);
+  tdvec_write_skew_batch_kernel<<<dim3(L.KP / 32, (n + RC - 1) / RC, G), LA_NT, 0, st>>>(L, X, Vr, Vi, idx);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  mirror_batch_kernel<<<dim3((n + 255) / 256, L.h + (n & 1), G), 256, 0, st>>>(Vr, Vi, idx, n, gate);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  // full mode (gate 1): every eigenpair in the fallback's layout
+  TdvecLayout F = layout(n, ws, true, nullptr);
+  F.gate = gate;
+  F.gate_on = 1;
+  twisted_kernel<<<dim3(F.KP / TW_NT + (F.KP % TW_NT ? 1 : 0), 1, G), TW_NT, 0, st>>>(e_g, mu, bpf, F);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return e;
+  X = tdvec_orthogonalize(F, G, st);
+  tdvec_write_fallback_batch_kernel<<<dim3(F.KP / 32, (n + RC - 1) / RC, G), LA_NT, 0, st>>>(F, X, Vr, Vi, idx);
   return cudaGetLastError();
 }
 

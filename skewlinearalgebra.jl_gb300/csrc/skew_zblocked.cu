@@ -44,7 +44,7 @@ constexpr int ZUT = 64;    // trailing-update tile edge
 constexpr int ZKC = 8;     // panel columns per shared-memory stage of the update
 constexpr int ZFIN = 16;   // smallest row block of phase B (sizes sspart)
 constexpr int ZTAILP = 128;  // trailing columns left to the one-CTA kernel
-constexpr long long ZP_POLL = 1LL << 24;
+constexpr long long ZP_POLL = 1LL << 24;  // default polls before a grid barrier gives up
 constexpr int ZP_MAXWARPS = 16384;  // dpart slots: grid x 8 warps at most
 
 struct ZRef {
@@ -106,6 +106,8 @@ struct ZPersistParams {
   int* err;
   int maxck;
   int items_per_warp;  // matvec tiles per warp and column (chunk count)
+  long long poll_limit;  // polls before a grid barrier gives up
+  int skip_cta;          // >= 0: this CTA never arrives (a test of the timeout path)
 };
 
 namespace {
@@ -113,7 +115,13 @@ namespace {
 __device__ bool zp_gsync(const ZPersistParams& P) {
   __shared__ int s_ok;
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (threadIdx.x == 0 && (int)blockIdx.x == P.skip_cta) {
+    // no arrival: the others give up after poll_limit polls; wait (bounded) for that
+    volatile int* verr = P.err;
+    long long it = 0;
+    while (!*verr && ++it <= P.poll_limit) __nanosleep(32);
+    s_ok = 0;
+  } else if (threadIdx.x == 0) {
     volatile int* verr = P.err;
     __threadfence();
     const unsigned old = atomicAdd(P.sync, 1u);
@@ -129,7 +137,7 @@ __device__ bool zp_gsync(const ZPersistParams& P) {
           ok = 0;
           break;
         }
-        if (it > ZP_POLL) {
+        if (it > P.poll_limit) {
           atomicExch(P.err, 1);
           ok = 0;
           break;
@@ -614,7 +622,7 @@ __global__ void zp_merge_err_kernel(const int* err, int* info) {
 // co-schedule the grid or n is outside the staged range (the caller then uses the
 // per-column path).
 cudaError_t zhess_persistent(double* Ad, int64_t lda, int n, double* taud, double* ev, double* dvim, double* wsd,
-                             int sms, int* info, cudaStream_t st) {
+                             int sms, int* info, const Tuning& tune, cudaStream_t st) {
   const size_t smem = std::max((size_t)n * sizeof(zc), (size_t)ZUT * (ZUT + 1) * sizeof(zc));
   int dev = 0, optin = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -629,10 +637,7 @@ cudaError_t zhess_persistent(double* Ad, int64_t lda, int n, double* taud, doubl
   if (e != cudaSuccess) return e;
   if (occ < 1) return cudaErrorNotSupported;
   int grid = sms;
-  {
-    const char* g = getenv("SKEW_ZPERSIST_CTAS");
-    if (g && *g) grid = std::max(1, std::min(sms * occ, atoi(g)));
-  }
+  if (tune.zpersist_ctas > 0) grid = std::max(1, std::min(sms * occ, tune.zpersist_ctas));
   grid = std::min(grid, ZP_MAXWARPS / ZP_NW);
   zc* A = reinterpret_cast<zc*>(Ad);
   zc* tau = reinterpret_cast<zc*>(taud);
@@ -658,11 +663,9 @@ cudaError_t zhess_persistent(double* Ad, int64_t lda, int n, double* taud, doubl
   P.sync = reinterpret_cast<unsigned*>(wp);  // 2 words
   P.err = reinterpret_cast<int*>(wp + 1);
   P.maxck = (int)maxck;
-  P.items_per_warp = 4;
-  {
-    const char* v = getenv("SKEW_ZPERSIST_ITEMS");  // sweeps: 1..8
-    if (v && *v) P.items_per_warp = std::max(1, std::min(8, atoi(v)));
-  }
+  P.items_per_warp = std::max(1, std::min(8, tune.zpersist_items));
+  P.poll_limit = tune.wait_polls > 0 ? tune.wait_polls : ZP_POLL;
+  P.skip_cta = tune.wait_skip_cta;
   e = cudaMemsetAsync(wp, 0, 2 * sizeof(double), st);
   if (e != cudaSuccess) return e;
   void* args[] = {&P};

@@ -26,6 +26,7 @@ libskewgpu's kernels, and there is no CPU fallback.
 from __future__ import annotations
 
 import ctypes
+import os
 from dataclasses import dataclass
 from typing import List, Optional, Sequence, Tuple
 
@@ -68,6 +69,68 @@ def handle(device: Optional[int] = None) -> _Handle:
         with torch.cuda.device(d):
             _handles[d] = _Handle()
     return _handles[d]
+
+
+# ---------------------------------------------------------------------------
+# Tuning table of the current device's handle (skew_tuning_* in skewgpu.h)
+# ---------------------------------------------------------------------------
+def tuning_keys() -> list:
+    """Names of the tuning keys."""
+    out, i = [], 0
+    while True:
+        k = _lib.load().skew_tuning_key(i)
+        if not k:
+            return out
+        out.append(k.decode())
+        i += 1
+
+
+def tuning_get(key: str):
+    """The key's value (a list for bucket_edges)."""
+    vals = (ctypes.c_int64 * 16)()
+    cnt = ctypes.c_int(0)
+    check(_lib.load().skew_tuning_get(handle().h, key.encode(), vals, 16, ctypes.byref(cnt)), f"tuning_get {key}")
+    return list(vals[: cnt.value]) if key == "bucket_edges" else int(vals[0])
+
+
+def tuning_set(key: str, value) -> None:
+    """Set one key (an int, or a list for bucket_edges); raises SkewError if out of range."""
+    if isinstance(value, (list, tuple)):
+        arr = (ctypes.c_int64 * len(value))(*[int(v) for v in value])
+        check(_lib.load().skew_tuning_set_list(handle().h, key.encode(), arr, len(value)), f"tuning_set {key}")
+    else:
+        check(_lib.load().skew_tuning_set(handle().h, key.encode(), int(value)), f"tuning_set {key}")
+
+
+def tuning_reset() -> None:
+    check(_lib.load().skew_tuning_reset(handle().h), "tuning_reset")
+
+
+def tuning_load(path: str) -> None:
+    check(_lib.load().skew_tuning_load(handle().h, os.fspath(path).encode()), "tuning_load")
+
+
+def tuning_source() -> str:
+    return _lib.load().skew_tuning_source(handle().h).decode()
+
+
+class tuned:
+    """Context manager: set tuning keys on the current device's handle, restore them on exit."""
+
+    def __init__(self, **keys):
+        self.keys = keys
+        self.saved = {}
+
+    def __enter__(self):
+        for k, v in self.keys.items():
+            self.saved[k] = tuning_get(k)
+            tuning_set(k, v)
+        return self
+
+    def __exit__(self, *exc):
+        for k, v in self.saved.items():
+            tuning_set(k, v)
+        return False
 
 
 def _ptr(t: Optional[torch.Tensor]) -> ctypes.c_void_p:
@@ -225,13 +288,16 @@ def logabspfaffian_rrule(A):
 
 
 def eigvals(A) -> np.ndarray:
-    """eigvals(A::SkewHermitian{Float64}) -> complex numpy vector (0 + i*vals)."""
+    """eigvals(A::SkewHermitian{Float64}) (eigen.jl:2-6) -> complex numpy vector
+    (0 + i*vals): for n <= 1024 in the reference's QR deflation order, above that
+    sorted descending.  Raises where the reference's QR raises (skeweigen.jl:154)."""
     S = _as_skew(A).copy()
     n = S.n
     vals = torch.zeros(n, dtype=torch.float64, device="cuda")
     info = _info_tensor()
     h = handle().bind()
     check(_lib.load().skew_eigvals_d(h, _ptr(S.data), n, n, _ptr(vals), _ptr(info)), "eigvals")
+    _info_ok(info, "eigvals")
     return 1j * vals.cpu().numpy()
 
 
@@ -277,7 +343,7 @@ def _info_ok(info: torch.Tensor, where: str) -> int:
 
 
 def eigen(A):
-    """eigen(A::SkewHermitian{Float64}) (eigen.jl:338-360): (values, vectors) as numpy
+    """eigen(A::SkewHermitian{Float64}) (eigen.jl:75-97): (values, vectors) as numpy
     complex arrays; values in the reference's order, vectors = Vr + i Vi."""
     S = _as_skew(A).copy()
     n = S.n

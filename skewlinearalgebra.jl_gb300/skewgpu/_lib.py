@@ -84,6 +84,15 @@ SIGNATURES = {
     "skew_batch_logabspf_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
     "skew_batch_logabspf_host_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
     "skew_measure_fp64_peak": (_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    "skew_tuning_set": (_int, [_vp, ctypes.c_char_p, ctypes.c_int64]),
+    "skew_tuning_set_list": (_int, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _int]),
+    "skew_tuning_get": (_int, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _int, ctypes.POINTER(_int)]),
+    "skew_tuning_reset": (_int, [_vp]),
+    "skew_tuning_load": (_int, [_vp, ctypes.c_char_p]),
+    "skew_tuning_source": (ctypes.c_char_p, [_vp]),
+    "skew_tuning_key": (ctypes.c_char_p, [_int]),
+    "skew_tuning_file_get": (_int, [ctypes.c_char_p, ctypes.c_char_p, ctypes.c_char_p,
+                                    ctypes.POINTER(ctypes.c_int64), _int, ctypes.POINTER(_int)]),
 }
 
 _lib = None

@@ -1,0 +1,263 @@
+"""Autotuner: measures the library's own calls at candidate values of each tuning
+key on the current GPU and writes the best values into the tuning table that
+libskewgpu.so loads at handle creation (skew_tuning.json beside the library, or
+the file SKEW_TUNING_FILE names), under this device's name.
+
+    python -m skewgpu.autotune [--out PATH] [--quick]
+
+The reference fixes its one shape by rule (setnb, hessenberg.jl:133-142: the panel
+width from n).  Here each key is decided by timing, one key at a time over its
+candidates with the other keys held at their current best (coordinate descent),
+on seeded synthetic workloads shaped like the benchmark configurations:
+
+* batched log|Pf| + gradient over uneven sizes (even n in [16, 256], entries of
+  (B - B^T)/2 with B ~ N(0, 1/n)): bucket_edges, batch_smem_nmax,
+  batch_smem_nt_small, batch_smem_nt_large, batch_global_nt,
+  batch_global_ctas_per_sm;
+* single real matrices: blocked_min_n (the size from which the multi-CTA blocked
+  reduction beats the one-CTA kernel), persist_items and persist_ctas (n = 4096);
+* single complex matrices: zpersist_min_n and zpersist_items;
+* batched exp adjoint over n in {32, 64, ..., 512}: func_chain_nmax.
+
+Every measurement is recorded in the table next to the chosen values.  Timing:
+CUDA events on the current stream, median of several calls after warm-up.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import datetime
+import json
+import os
+import time
+from typing import Callable, Dict, List, Sequence
+
+import numpy as np
+import torch
+
+import skewgpu
+from skewgpu import _lib
+
+DEFAULT_TABLE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "skew_tuning.json")
+
+
+def _time(fn: Callable[[], None], reps: int = 5, warm: int = 2) -> float:
+    """Median seconds of fn() over reps calls (CUDA events, after warm calls)."""
+    for _ in range(warm):
+        fn()
+    torch.cuda.synchronize()
+    out = []
+    for _ in range(reps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        fn()
+        e1.record()
+        torch.cuda.synchronize()
+        out.append(e0.elapsed_time(e1) / 1e3)
+    return float(np.median(out))
+
+
+def _packed(sizes: Sequence[int], seed: int) -> torch.Tensor:
+    rng = np.random.default_rng(seed)
+    parts = []
+    for n in sizes:
+        B = rng.standard_normal((n, n)) / np.sqrt(n)
+        parts.append(((B - B.T) / 2).ravel(order="F"))
+    return torch.from_numpy(np.concatenate(parts)).cuda()
+
+
+def _ptrs(base: torch.Tensor, sizes: Sequence[int]) -> torch.Tensor:
+    offs = np.zeros(len(sizes), dtype=np.int64)
+    offs[1:] = np.cumsum(np.asarray(sizes[:-1], dtype=np.int64) ** 2)
+    return torch.tensor((base.data_ptr() + 8 * offs).tolist(), dtype=torch.int64, device="cuda")
+
+
+class Tuner:
+    def __init__(self, quick: bool = False):
+        self.quick = quick
+        self.log: Dict[str, List] = {}
+
+    def sweep(self, key: str, candidates: Sequence, measure: Callable[[], float]) -> None:
+        """Time measure() at each candidate value of key; keep the fastest."""
+        base = skewgpu.tuning_get(key)
+        results = []
+        for c in candidates:
+            try:
+                skewgpu.tuning_set(key, c)
+                t = measure()
+            except Exception as e:  # a candidate the device cannot run (e.g. shared memory)
+                results.append([c, None, str(e)])
+                continue
+            results.append([c, t])
+        ok = [r for r in results if r[1] is not None]
+        best = min(ok, key=lambda r: r[1])[0] if ok else base
+        skewgpu.tuning_set(key, best)
+        self.log[key] = results
+        print(f"  {key}: " + ", ".join(f"{r[0]}={r[1] * 1e3:.3f} ms" if r[1] is not None else f"{r[0]}=fail"
+                                       for r in results) + f"  -> {best}", flush=True)
+
+    # -- batched uneven log|Pf| + gradient --------------------------------------
+    def batched(self) -> None:
+        count = 1024 if self.quick else 4096
+        rng = np.random.default_rng(7)
+        sizes = (2 * rng.integers(8, 129, count)).astype(np.int64)
+        A = _packed(sizes, 11)
+        G = torch.empty_like(A)
+        a_ptrs, g_ptrs = _ptrs(A, sizes), _ptrs(G, sizes)
+
+        def measure() -> float:
+            plan = skewgpu.BatchPlan(sizes)  # plans take the bucket keys at creation
+            try:
+                return _time(lambda: plan.logabspfaffian(a_ptrs, g_ptrs), reps=3 if self.quick else 5)
+            finally:
+                plan.close()
+
+        self.sweep("bucket_edges", [[32, 64, 96, 128, 152], [32, 64, 96, 128, 152, 192],
+                                    [24, 48, 72, 96, 128, 152], [32, 64, 96, 128, 152, 192, 224],
+                                    [16, 32, 48, 64, 96, 128, 152, 200]], measure)
+        self.sweep("batch_smem_nmax", [64, 96, 128, 152], measure)
+        self.sweep("batch_smem_nt_small", [128, 256], measure)
+        self.sweep("batch_smem_nt_large", [256, 512], measure)
+        self.sweep("batch_global_nt", [256, 512], measure)
+        self.sweep("batch_global_ctas_per_sm", [1, 2, 3], measure)
+
+    # -- single real matrices -------------------------------------------------------
+    def single_real(self) -> None:
+        L = _lib.load()
+        h = skewgpu.handle().bind()
+
+        def hess_time(n: int) -> float:
+            rng = np.random.default_rng(n)
+            B = rng.standard_normal((n, n))
+            src = skewgpu.to_device((B - B.T) / 2)
+            work = torch.empty_like(src)
+            tau = torch.empty(n, dtype=torch.float64, device="cuda")
+            ev = torch.empty(n, dtype=torch.float64, device="cuda")
+            info = torch.zeros(1, dtype=torch.int32, device="cuda")
+            P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+            def call():
+                work.copy_(src)
+                _lib.check(L.skew_hessenberg_d(h, P(work), n, n, P(tau), P(ev), P(info)), "hessenberg")
+
+            copy = _time(lambda: work.copy_(src), reps=3)
+            return _time(call, reps=3) - copy
+
+        # the crossover from the one-CTA kernel to the blocked reduction
+        rows = []
+        best = None
+        for n in (96, 128, 160, 192, 224, 256, 320, 384):
+            skewgpu.tuning_set("blocked_min_n", 1025)
+            t1 = hess_time(n)
+            skewgpu.tuning_set("blocked_min_n", 16)
+            tb = hess_time(n)
+            rows.append([n, t1, tb])
+            if best is None and tb < t1:
+                best = n
+        skewgpu.tuning_set("blocked_min_n", best if best is not None else 1025)
+        self.log["blocked_min_n"] = rows
+        print(f"  blocked_min_n: " + ", ".join(f"n={r[0]}: one CTA {r[1] * 1e3:.2f} / blocked {r[2] * 1e3:.2f} ms"
+                                               for r in rows) + f"  -> {skewgpu.tuning_get('blocked_min_n')}",
+              flush=True)
+        n = 2048 if self.quick else 4096
+        self.sweep("persist_items", [2, 4, 8, 16], lambda: hess_time(n))
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        self.sweep("persist_ctas", [0, sms, 2 * sms], lambda: hess_time(n))
+
+    # -- single complex matrices ------------------------------------------------------
+    def single_complex(self) -> None:
+        L = _lib.load()
+        h = skewgpu.handle().bind()
+
+        def zhess_time(n: int) -> float:
+            rng = np.random.default_rng(n + 1)
+            C = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+            src = skewgpu.to_device_complex((C - C.conj().T) / 2)
+            work = torch.empty_like(src)
+            tau = torch.empty(n, dtype=torch.complex128, device="cuda")
+            ev = torch.empty(n, dtype=torch.float64, device="cuda")
+            dv = torch.empty(n, dtype=torch.float64, device="cuda")
+            info = torch.zeros(1, dtype=torch.int32, device="cuda")
+            P = lambda t: ctypes.c_void_p(t.data_ptr())  # noqa: E731
+
+            def call():
+                work.copy_(src)
+                _lib.check(L.skew_hessenberg_z(h, P(work), n, n, P(tau), P(ev), P(dv), P(info)), "hessenberg_z")
+
+            copy = _time(lambda: work.copy_(src), reps=3)
+            return _time(call, reps=3) - copy
+
+        rows = []
+        best = None
+        for n in (256, 320, 384, 448, 512, 768):
+            skewgpu.tuning_set("zpersist_min_n", 1 << 15)
+            t1 = zhess_time(n)
+            skewgpu.tuning_set("zpersist_min_n", 129)
+            tp = zhess_time(n)
+            rows.append([n, t1, tp])
+            if best is None and tp < t1:
+                best = n
+        skewgpu.tuning_set("zpersist_min_n", best if best is not None else 1 << 15)
+        self.log["zpersist_min_n"] = rows
+        print(f"  zpersist_min_n: " + ", ".join(f"n={r[0]}: columns {r[1] * 1e3:.2f} / persistent {r[2] * 1e3:.2f} ms"
+                                                for r in rows) + f"  -> {skewgpu.tuning_get('zpersist_min_n')}",
+              flush=True)
+        self.sweep("zpersist_items", [2, 4, 8], lambda: zhess_time(1024 if self.quick else 2048))
+
+    # -- batched exp adjoint --------------------------------------------------------------
+    def functions(self) -> None:
+        count = 64 if self.quick else 128
+        rng = np.random.default_rng(5)
+        sizes = (32 * rng.integers(1, 17, count)).astype(np.int64)
+        A = _packed(sizes, 13)
+        C = torch.randn_like(A)
+        G = torch.empty_like(A)
+        a, c, g = _ptrs(A, sizes), _ptrs(C, sizes), _ptrs(G, sizes)
+
+        def measure() -> float:
+            plan = skewgpu.BatchPlan(sizes)
+            try:
+                return _time(lambda: plan.exp_vjp(a, c, g), reps=3, warm=1)
+            finally:
+                plan.close()
+
+        self.sweep("func_chain_nmax", [32, 64, 128], measure)
+
+    def run(self) -> Dict:
+        torch.cuda.set_device(0)
+        skewgpu.tuning_reset()
+        t0 = time.time()
+        for part in (self.batched, self.single_real, self.single_complex, self.functions):
+            print(f"{part.__name__}:", flush=True)
+            part()
+        entry = {k: skewgpu.tuning_get(k) for k in skewgpu.tuning_keys()
+                 if k not in ("wait_polls", "wait_skip_cta", "qr_max_iter")}
+        entry["measurements"] = {"unit": "seconds per call", "rows": self.log,
+                                 "when": datetime.datetime.now(datetime.timezone.utc).isoformat(timespec="seconds"),
+                                 "elapsed_s": round(time.time() - t0, 1), "quick": self.quick}
+        return entry
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--out", default=DEFAULT_TABLE, help="table to write (the device's entry is replaced)")
+    ap.add_argument("--quick", action="store_true", help="smaller workloads (a rough table in about a minute)")
+    args = ap.parse_args(argv)
+    name = torch.cuda.get_device_name(0)
+    entry = Tuner(args.quick).run()
+    table = {"devices": {}}
+    if os.path.exists(args.out):
+        with open(args.out) as f:
+            table = json.load(f)
+    table.setdefault("devices", {})[name] = entry
+    table["tool"] = "skewgpu.autotune"
+    tmp = args.out + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(table, f, indent=1)
+    os.replace(tmp, args.out)
+    print(f"wrote {args.out} [{name}]", flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())

@@ -56,13 +56,13 @@ def test_hessenberg_complex_vs_oracle(skewgpu, oracle, n):
 
 
 @pytest.mark.parametrize("n", [131, 160, 257, 300, 520, 777])
-def test_hessenberg_complex_persistent_vs_oracle(skewgpu, oracle, n, monkeypatch):
+def test_hessenberg_complex_persistent_vs_oracle(skewgpu, oracle, n):
     """The blocked persistent reduction (panels of 32 columns, the complex latrd with
     the alpha correction, rank-64 trailing updates), forced down to n = 131 with
-    SKEW_ZPERSIST_MIN_N; checked like the per-column path."""
-    monkeypatch.setenv("SKEW_ZPERSIST_MIN_N", "130")
+    the tuning key zpersist_min_n; checked like the per-column path."""
     A = skewh_random(n, 1600 + n)
-    Hc = skewgpu.hessenberg_complex(A)
+    with skewgpu.tuned(zpersist_min_n=130):
+        Hc = skewgpu.hessenberg_complex(A)
     ev = Hc.ev.cpu().numpy()
     dvim = Hc.dvim.cpu().numpy()
     tau = Hc.tau.cpu().numpy()

@@ -171,12 +171,12 @@ def test_eigen_stagnation_fallback(skewgpu, oracle):
     plan.close()
 
 
-def test_batch_exp_vjp_twisted_path(skewgpu, oracle, monkeypatch):
-    """Above n = 160 the batched function paths take bisection and twisted vectors
+def test_batch_exp_vjp_twisted_path(skewgpu, oracle):
+    """Above n = 64 the batched function paths take bisection and twisted vectors
     instead of the QR chain (the order of the eigenpairs does not matter there).
     Odd and even sizes, repeated sizes (groups of several problems): exp against the
     oracle, the adjoint against the oracle's binary128 block exponential for one
-    matrix and against the QR-chain path (SKEW_FUNC_CHAIN_NMAX) for all."""
+    matrix and against the QR-chain path (the tuning key func_chain_nmax) for all."""
     import torch
 
     sizes = [161, 200, 200, 257, 301, 64]
@@ -208,8 +208,47 @@ def test_batch_exp_vjp_twisted_path(skewgpu, oracle, monkeypatch):
         np.testing.assert_allclose(E1[b], Eq, atol=1e-11 * np.sqrt(A.shape[0]) * max(1, np.abs(Eq).max()))
     Gq = oracle.exp_vjp(mats[0], cots[0])
     assert np.abs(G1[0] - Gq).max() <= 1e-8 * np.abs(Gq).max()
-    monkeypatch.setenv("SKEW_FUNC_CHAIN_NMAX", "100000")
-    E2, G2 = run()
+    with skewgpu.tuned(func_chain_nmax=100000):
+        E2, G2 = run()
     for b in range(len(sizes)):
         np.testing.assert_allclose(E1[b], E2[b], atol=1e-11 * np.sqrt(sizes[b]) * max(1, np.abs(E2[b]).max()))
         assert np.abs(G1[b] - G2[b]).max() <= 1e-9 * np.abs(G2[b]).max(), f"n={sizes[b]}"
+
+
+def test_functions_several_odd_blocks(skewgpu):
+    """exp and the exp adjoint of singular block-diagonal inputs whose tridiagonal
+    splits exactly into several odd blocks (one zero eigenvalue each), through the
+    batched function path above n = 64 (bisection and twisted vectors) and the
+    single-matrix call, against scipy's expm and expm_frechet."""
+    import scipy.linalg as sl
+    import torch
+
+    def blockdiag(sizes, seed):
+        n = sum(sizes)
+        A = np.zeros((n, n))
+        o = 0
+        for k, m in enumerate(sizes):
+            A[o:o + m, o:o + m] = skew_random(m, seed + k, scale=2.0 / np.sqrt(m))
+            o += m
+        return A
+
+    mats = [blockdiag((67, 67, 66), 10), blockdiag((101, 99, 101), 20), blockdiag((33, 31, 35, 29, 2), 30)]
+    sizes = [m.shape[0] for m in mats]
+    rng = np.random.default_rng(8)
+    cots = [rng.standard_normal((n, n)) for n in sizes]
+    plan = skewgpu.BatchPlan(sizes)
+    devs = [skewgpu.to_device(A) for A in mats]
+    cd = [skewgpu.to_device(C) for C in cots]
+    Eo = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in sizes]
+    Go = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in sizes]
+    st = plan.exp(plan.pointer_array(devs), plan.pointer_array(Eo)).cpu().numpy()
+    st2 = plan.exp_vjp(plan.pointer_array(devs), plan.pointer_array(cd), plan.pointer_array(Go)).cpu().numpy()
+    torch.cuda.synchronize()
+    plan.close()
+    assert (st == 0).all() and (st2 == 0).all()
+    for b, A in enumerate(mats):
+        n = sizes[b]
+        np.testing.assert_allclose(skewgpu.from_device(Eo[b]), sl.expm(A), atol=1e-11 * np.sqrt(n))
+        _, Lf = sl.expm_frechet(A.T, cots[b])
+        assert np.abs(skewgpu.from_device(Go[b]) - Lf).max() <= 1e-8 * np.abs(Lf).max(), n
+        np.testing.assert_allclose(skewgpu.exp(A), sl.expm(A), atol=1e-11 * np.sqrt(n))

@@ -87,3 +87,78 @@ def test_large_eigen_identical_blocks(skewgpu, oracle):
     A[:560, :560] = B
     A[560:, 560:] = B
     _check(skewgpu, oracle, A)
+
+
+def _check_full_mode(skewgpu, A, tol=1e-11, otol=1e-12):
+    """Several zero eigenvalues (the fallback's layout): values against LAPACK
+    (sorted descending), reconstruction, orthonormality and residuals."""
+    n = A.shape[0]
+    lam, V = skewgpu.eigen(A)
+    vals = lam.imag
+    assert np.all(np.diff(vals) <= 0.0), "values must be sorted descending"
+    rho = np.abs(vals).max()
+    ref = np.sort(-np.linalg.eigvalsh(1j * A))[::-1]
+    np.testing.assert_allclose(vals, ref, atol=tol * rho)
+    G = V.conj().T @ V
+    assert np.abs(G - np.eye(n)).max() <= otol, f"orthonormality {np.abs(G - np.eye(n)).max()}"
+    R = V @ np.diag(lam) @ V.conj().T - A
+    assert np.abs(R).max() <= tol * rho, f"reconstruction {np.abs(R).max() / rho}"
+    assert np.abs(A @ V - V * lam).max() <= tol * rho
+    return lam, V
+
+
+@pytest.mark.parametrize("sizes", [(367, 401, 333), (501, 299, 301, 8), (551, 551)])
+def test_large_eigen_several_odd_blocks(skewgpu, sizes):
+    """A block-diagonal input whose tridiagonal splits exactly into several blocks of
+    odd size: one zero eigenvalue per odd block.  More zero eigenvalues than n mod 2
+    do not come in +-sigma pairs, so the path solves the whole tridiagonal in full
+    mode, as the reference's fallback does (skeweigen.jl:470-489); every zero
+    eigenvalue must get its own null vector."""
+    n = sum(sizes)
+    A = np.zeros((n, n))
+    o = 0
+    for k, m in enumerate(sizes):
+        A[o:o + m, o:o + m] = skew_random(m, 400 + k)
+        o += m
+    zeros = sum(m % 2 for m in sizes)
+    lam, V = _check_full_mode(skewgpu, A)
+    assert np.sum(np.abs(lam.imag) <= 1e-12 * np.abs(lam).max()) == zeros
+
+
+def test_large_tridiagonal_several_odd_blocks(skewgpu):
+    """The same through the SkewHermTridiagonal entry point (no reduction, Q = I):
+    ev with exact zeros leaving three odd blocks."""
+    rng = np.random.default_rng(9)
+    n = 1203
+    ev = rng.standard_normal(n - 1)
+    # exact zeros split the rows into blocks of 11, 2, 388, 400, 1, 299, 50 and 52:
+    # three odd blocks, three zero eigenvalues
+    for i in (10, 12, 400, 800, 801, 1100, 1150):
+        ev[i] = 0.0
+    T = skewgpu.SkewHermTridiagonal(ev)
+    lam, V = T.eigen()
+    Td = np.zeros((n, n))
+    Td[np.arange(1, n), np.arange(n - 1)] = ev
+    Td[np.arange(n - 1), np.arange(1, n)] = -ev
+    rho = np.abs(lam).max()
+    ref = np.sort(-np.linalg.eigvalsh(1j * Td))[::-1]
+    np.testing.assert_allclose(lam.imag, ref, atol=1e-11 * rho)
+    assert np.abs(V.conj().T @ V - np.eye(n)).max() <= 1e-12
+    assert np.abs(V @ np.diag(lam) @ V.conj().T - Td).max() <= 1e-11 * rho
+    assert np.sum(np.abs(lam.imag) <= 1e-12 * rho) == 3
+
+
+def test_large_exp_several_odd_blocks(skewgpu):
+    """exp of a singular block-diagonal input with three odd blocks above n = 1024
+    (its eigenpairs come from the same path) against scipy's expm."""
+    import scipy.linalg as sl
+
+    sizes = (401, 333, 367)
+    n = sum(sizes)
+    A = np.zeros((n, n))
+    o = 0
+    for k, m in enumerate(sizes):
+        A[o:o + m, o:o + m] = skew_random(m, 500 + k, scale=1.0 / np.sqrt(m))
+        o += m
+    E = skewgpu.exp(A)
+    np.testing.assert_allclose(E, sl.expm(A), atol=1e-11 * np.sqrt(n))
