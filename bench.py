@@ -36,7 +36,8 @@ sys.path.insert(0, os.path.join(ROOT, "skewlinearalgebra.jl_gb300"))
 
 # dram__bytes_read.sum + dram__bytes_write.sum over the six batch_kernel launches of one
 # step of the default workload (4096 matrices, even n in [16, 256]), from one ncu capture
-STEP_DRAM_BYTES = 45_104_311_808
+# of the timed step (-s 18 -c 6)
+STEP_DRAM_BYTES = 34_114_203_648
 METRIC = "batched log|Pf|+grad matrices/s & n=8192 hessenberg GFLOP/s vs plain GPU, err≤1e-11"
 UNIT = "matrices/s"
 COUNT = 4096
@@ -455,6 +456,8 @@ def main():
     eig_large = None
     if rank == 0 and args.large_n > 0:
         large = bench_hessenberg_large(args.large_n, 2, fp64_peak)
+        if not args.no_cpu:
+            large["leading_256_vs_cpu_port"] = leading_256_check(args.large_n)
         eig_large = leg_eigen_large(args.large_n, fp64_peak)
     legs = {}
     if rank == 0 and not args.no_legs:
@@ -488,6 +491,8 @@ def main():
                                         "(MEASURED_PEAKS.json has no FP64 figure)",
                          "algorithmic_flops_per_step": flops, "kernel": "batch_kernel"},
             "gpu_launches": int(args.steps * len(set(_bucket_ids(sizes)))),
+            "tuning": skewgpu.tuning_source(),
+            "fp64_pipes_tflops": skewgpu.measure_fp64_pipes(),
             "clocks": clk,
             "wall_s": wall,
         }
@@ -546,8 +551,57 @@ def bench_hessenberg_large(n, reps, fp64_peak):
     flops = 4.0 / 3.0 * n ** 3
     e = ev.cpu().numpy()
     fro_rel = abs(np.sqrt(2.0 * np.sum(e * e)) - np.linalg.norm(A)) / np.linalg.norm(A)
+    # logabspfaffian of the same matrix (skew_logabspf_d: the reduction, then log|Pf| and
+    # the sign from ev and tau), checked against 1/2 log|det A| from cuSOLVER's LU
+    out2 = torch.zeros(2, dtype=torch.float64, device="cuda")
+    lp_times = []
+    for r in range(reps + 1):
+        work.copy_(pristine)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        st = L.skew_logabspf_d(h, ctypes.c_void_p(work.data_ptr()), n, n, ctypes.c_void_p(out2.data_ptr()),
+                               ctypes.c_void_p(out2.data_ptr() + 8), 0, ctypes.c_void_p(info.data_ptr()))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        assert st == 0, st
+        if r > 0:
+            lp_times.append(e0.elapsed_time(e1) / 1e3)
+    lp, sg = (float(x) for x in out2.cpu().numpy())
+    sdet, ldet = torch.linalg.slogdet(pristine)
+    del work
     return {"n": n, "ms": sec * 1e3, "gflops": flops / sec / 1e9, "frac_fp64": flops / sec / 1e12 / fp64_peak,
-            "algorithmic_flops": flops, "reps": reps, "check_frobenius_rel": float(fro_rel)}
+            "algorithmic_flops": flops, "reps": reps, "check_frobenius_rel": float(fro_rel),
+            "logabspfaffian": {"ms": float(np.median(lp_times)) * 1e3, "logpf": lp, "sign": sg,
+                               "check_rel_vs_half_logdet": float(abs(lp - 0.5 * ldet.item()) / abs(0.5 * ldet.item())),
+                               "det_sign": float(sdet.item())}}
+
+
+def leading_256_check(n=8192, k=256):
+    """The single large dense matrix's leading k x k principal submatrix through the
+    single-matrix calls, next to the oracle's FP64 restatement of the reference
+    (the CPU port, one host core): hessenberg ev, eigvals (the reference's order) and
+    log|Pf|, with the port's times and the largest differences."""
+    import skewgpu
+    from oracle import oracle as O
+
+    A = np.ascontiguousarray(dense_skew_input(n)[:k, :k])
+    H = skewgpu.hessenberg(A)
+    ev = H.ev.cpu().numpy()
+    vals = skewgpu.eigvals(A).imag
+    lp, sg = skewgpu.logabspfaffian(A)
+    t0 = time.perf_counter()
+    _, _, evo = O.hessenberg(A)
+    t1 = time.perf_counter()
+    vo, _ = O.eigvals(A)
+    t2 = time.perf_counter()
+    lpo, sgo = O.logabspfaffian(A)
+    t3 = time.perf_counter()
+    return {"k": k, "cpu_port_ms": {"hessenberg": (t1 - t0) * 1e3, "eigvals": (t2 - t1) * 1e3,
+                                    "logabspfaffian": (t3 - t2) * 1e3, "cores": 1},
+            "max_rel_ev_vs_port": float(np.abs(ev - evo).max() / np.abs(evo).max()),
+            "max_rel_eigvals_vs_port_same_order": float(np.abs(vals - vo).max() / np.abs(vo).max()),
+            "logpf_rel_vs_port": float(abs(lp - lpo) / abs(lpo)), "sign_equal": bool(sg == sgo)}
 
 
 def leg_eigen_large(n, fp64_peak, reps=1):
@@ -1024,7 +1078,9 @@ def leg_exp_adjoint(fp64_peak, steps, count=512):
 
 
 def _bucket_ids(sizes):
-    edges = [32, 64, 96, 128, 152]  # size buckets of skew_batch_plan_create
+    import skewgpu
+
+    edges = skewgpu.tuning_get("bucket_edges")  # the size buckets of skew_batch_plan_create
     out = []
     for n in sizes:
         out.append(next((e for e in edges if n <= e), 1 << 30))

@@ -392,6 +392,11 @@ SKEW_API int skew_tuning_file_get(const char* path, const char* device, const ch
 /* Diagnostics: measured FP64 DFMA throughput of the current device in TFLOP/s
  * (runs a short microbenchmark on the handle's stream and synchronizes). */
 SKEW_API int skew_measure_fp64_peak(skew_handle_t h, double* tflops);
+/* Diagnostics: the FP64 tensor instruction (mma.sync f64) against DFMA, in TFLOP/s:
+ * tflops[0] DFMA, [1] mma m8n8k4, [2] mma m16n8k16, [3] half the warps DFMA and half
+ * m8n8k4 in one kernel, [4] half DFMA and half m16n8k16 (equal flops per warp).  If
+ * [3] and [4] are about [0], the two share one FP64 pipe (synchronises the stream). */
+SKEW_API int skew_measure_fp64_pipes(skew_handle_t h, double* tflops);
 
 #ifdef __cplusplus
 }

@@ -1938,4 +1938,76 @@ cudaError_t launch_dfma_probe(double* out, int blocks, int iters, cudaStream_t s
   dfma_probe_kernel<<<blocks, 128, 0, st>>>(out, iters, 1.0000001, 1e-9);
   return cudaGetLastError();
 }
+
+// The FP64 tensor instruction (mma.sync f64) against DFMA, alone and mixed in one
+// kernel.  mode 0: DFMA (eight chains per thread); 1: mma m8n8k4 (four
+// accumulators per warp); 2: mma m16n8k16 (two); 3: even warps DFMA, odd warps
+// m8n8k4; 4: even warps DFMA, odd warps m16n8k16.  it_f / it_m are the iterations
+// of the DFMA and mma loops (chosen so both halves of a mixed launch do the same flops).
+__global__ void fp64_pipe_probe_kernel(double* out, int it_f, int it_m, int mode, double a, double b) {
+  const int warp = threadIdx.x >> 5;
+  double x[8];
+#pragma unroll
+  for (int q = 0; q < 8; q++) x[q] = threadIdx.x * 1e-3 + q;
+  const bool mma = mode == 1 || mode == 2 || (mode >= 3 && (warp & 1));
+  if (!mma) {
+    for (int it = 0; it < it_f; it++) {
+#pragma unroll
+      for (int q = 0; q < 8; q++) x[q] = fma(x[q], a, b);
+    }
+  } else if (mode == 1 || mode == 3) {
+    for (int it = 0; it < it_m; it++) {
+#pragma unroll
+      for (int q = 0; q < 4; q++)
+        asm volatile("mma.sync.aligned.m8n8k4.row.col.f64.f64.f64.f64 {%0,%1}, {%2}, {%3}, {%0,%1};"
+                     : "+d"(x[2 * q]), "+d"(x[2 * q + 1])
+                     : "d"(a), "d"(b));
+    }
+  } else {
+    for (int it = 0; it < it_m; it++) {
+#pragma unroll
+      for (int q = 0; q < 2; q++)
+        asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f64.f64.f64.f64 {%0,%1,%2,%3}, {%4,%4,%4,%4,%4,%4,%4,%4}, "
+            "{%5,%5,%5,%5}, {%0,%1,%2,%3};"
+            : "+d"(x[4 * q]), "+d"(x[4 * q + 1]), "+d"(x[4 * q + 2]), "+d"(x[4 * q + 3])
+            : "d"(a), "d"(b));
+    }
+  }
+  double s = 0;
+#pragma unroll
+  for (int q = 0; q < 8; q++) s += x[q];
+  out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
 }  // namespace skew
+
+extern "C" int skew_measure_fp64_pipes(skew_handle_t h, double* tflops) {
+  if (!h || !tflops) return SKEW_BAD_ARG;
+  const int blocks = h->sms * 4, nt = 128, it_f = 4096;
+  int st = ensure_ws(h, sizeof(double) * (size_t)blocks * nt);
+  if (st) return st;
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  // flops per warp and iteration: DFMA 8 x 32 x 2 = 512, m8n8k4 4 x 512 = 2048,
+  // m16n8k16 2 x 4096 = 8192; the mma loops run it_f / 4 and it_f / 16 iterations
+  const double warps = (double)blocks * nt / 32, fl_f = 512.0 * it_f;
+  const int it_m[5] = {0, it_f / 4, it_f / 16, it_f / 4, it_f / 16};
+  for (int mode = 0; mode < 5; mode++) {
+    float best = 1e30f;
+    for (int r = 0; r < 6; r++) {  // the first launch warms up
+      CK(cudaEventRecord(e0, h->stream));
+      fp64_pipe_probe_kernel<<<blocks, nt, 0, h->stream>>>((double*)h->ws, it_f, it_m[mode], mode, 1.0000001, 1e-9);
+      CK(cudaGetLastError());
+      CK(cudaEventRecord(e1, h->stream));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (r) best = std::min(best, ms);
+    }
+    tflops[mode] = warps * fl_f / (best * 1e-3) / 1e12;  // every warp does fl_f flops
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return SKEW_OK;
+}

@@ -26,7 +26,10 @@
 //   Q_b M Q_b^T = M + V Z'^T - Z' V^T,
 // which is the same 2 n m FMAs per reflector as applying them one at a time, but
 // as register-tiled products that read M once per block instead of once per
-// reflector.
+// reflector.  Only the strictly lower triangle of M is kept while the blocks run
+// (M is skew): X reads the upper entries as -M^T, the update writes no mirror, and
+// one pass at the end fills the upper triangle.  That halves the gradient's live
+// set, so that two CTAs per SM on n = 256 matrices keep it in L2.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -401,17 +404,19 @@ __device__ void pfaffian_from_tridiag(int n, const Smem& s, double* logpf, doubl
 // Gradient
 // ---------------------------------------------------------------------------
 
-// M = -1/2 T^{-1} (even n, all odd-position ev nonzero), full storage.
+// M = -1/2 T^{-1} (even n, all odd-position ev nonzero), its lower triangle and
+// diagonal (the strictly upper triangle is filled at the end of the gradient).
 // With O = even 0-based indices and E = odd ones, T = [[0, B], [-B^T, 0]] where
 // B is lower bidiagonal (diag d_a = -ev[2a], sub s_a = ev[2a-1]) and
 // T^{-1} = [[0, -B^{-T}], [B^{-1}, 0]]:  T^{-1}[2a+1, 2b] = (B^{-1})_{ab}
-//   = (1/d_b) prod_{c=b+1..a} (-s_c/d_c)   for a >= b, zero otherwise.
+//   = (1/d_b) prod_{c=b+1..a} (-s_c/d_c)   for a >= b, zero otherwise; these are
+// the only nonzero entries below the diagonal.
 template <int NT>
 __device__ void tinv_init(const GMat& G, int n, const Smem& s) {
   const int64_t total = (int64_t)n * n;
   for (int64_t e = threadIdx.x; e < total; e += NT) {
     const int j = (int)(e / n), i = (int)(e - (int64_t)j * n);
-    G.at(i, j) = 0.0;
+    if (i >= j) G.at(i, j) = 0.0;
   }
   const int h = n / 2;
   double* ratio = s.Vs;  // -s_c/d_c = ev[2c-1]/ev[2c], 1 <= c < h
@@ -421,14 +426,15 @@ __device__ void tinv_init(const GMat& G, int n, const Smem& s) {
     double x = 0.5 / s.ev[2 * b];  // -1/2 * (1/d_b)
     for (int a = b; a < h; a++) {
       G.at(2 * a + 1, 2 * b) = x;
-      G.at(2 * b, 2 * a + 1) = neg(x);
       if (a + 1 < h) x *= ratio[a + 1];
     }
   }
   __syncthreads();
 }
 
-// G <- Q G Q^T, G holding -1/2 T^{-1} on entry; reflectors from W's lower part.
+// G <- Q G Q^T, G holding -1/2 T^{-1} on entry (its lower triangle and diagonal);
+// reflectors from W's lower part.  Only the lower triangle is read and written while
+// the blocks run; the upper triangle is written at the end as -G^T.
 template <int NT, class MW>
 __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
   constexpr int NW = NT / 32;
@@ -494,7 +500,9 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
         for (int l = 0; l < GNB; l++) acc[l] = 0.0;
         if (i < n) {
           for (int j = cb; j < ce; j++) {
-            const double g = G.at(i, j);
+            // G[i, j] from the lower triangle: G[j, i] negated above the diagonal
+            // (strided reads that hit L2: a load feeds GNB FMAs on the FP64 pipe)
+            const double g = (j < i) ? G.at(i, j) : ((j > i) ? neg(G.at(j, i)) : 0.0);
             const double* vj = Vs + (j - r0) * GNB;
 #pragma unroll
             for (int l = 0; l < GNB; l++) acc[l] = fma(g, vj[l], acc[l]);
@@ -589,7 +597,7 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
       for (int l = 0; l < GNB; l++) Zs[i * GNB + l] = z[l];
     }
     __syncthreads();
-    // 6. G[i,j] += V_i . Z'_j - Z'_i . V_j for i >= r0, j < i; mirrored.
+    // 6. G[i,j] += V_i . Z'_j - Z'_i . V_j for i >= r0, j < i (lower triangle only).
     //    Items: (row strip of 32, column block of 32) on or below the diagonal.
     //    Strip si holds rows [n - 32(si+1), n - 32 si) and the columns before its
     //    last row.  Aligned to the last row, the partial strip is the one next to
@@ -633,15 +641,21 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
                 a1 = fma(neg(zi[l + 1]), vj[l + 1], a1);
               }
             }
-            const double a = a0 + a1;
-            G.at(i, j) = a;
-            G.at(j, i) = neg(a);
+            G.at(i, j) = a0 + a1;
           }
         }
       }
       __syncthreads();
     }
   }
+  // the upper triangle: G[j, i] = -G[i, j] for j < i (consecutive threads write
+  // consecutive rows of a column; the reads are strided and hit L2)
+  const int64_t total = (int64_t)n * n;
+  for (int64_t e = tid; e < total; e += NT) {
+    const int i = (int)(e / n), j = (int)(e - (int64_t)i * n);
+    if (j < i) G.at(j, i) = neg(G.at(i, j));
+  }
+  __syncthreads();
 }
 
 template <int NT>

@@ -844,6 +844,15 @@ def measure_fp64_peak() -> float:
     return t.value
 
 
+def measure_fp64_pipes() -> dict:
+    """DFMA against the FP64 tensor instruction (mma.sync f64), alone and with half the
+    warps of one kernel on each (skew_measure_fp64_pipes), in TFLOP/s."""
+    t = (ctypes.c_double * 5)()
+    check(_lib.load().skew_measure_fp64_pipes(handle().bind(), t), "measure_fp64_pipes")
+    return {"dfma": t[0], "mma_m8n8k4": t[1], "mma_m16n8k16": t[2], "half_dfma_half_m8n8k4": t[3],
+            "half_dfma_half_m16n8k16": t[4]}
+
+
 class BatchPlan:
     """A batch of real skew matrices of sizes ``sizes`` (skew_batch_plan_create).
 

@@ -84,6 +84,7 @@ SIGNATURES = {
     "skew_batch_logabspf_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
     "skew_batch_logabspf_host_z": (_int, [_vp, _vp, _i64, _i64, _vp, _vp, _vp, _int, _vp]),
     "skew_measure_fp64_peak": (_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
+    "skew_measure_fp64_pipes": (_int, [_vp, ctypes.POINTER(ctypes.c_double)]),
     "skew_tuning_set": (_int, [_vp, ctypes.c_char_p, ctypes.c_int64]),
     "skew_tuning_set_list": (_int, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _int]),
     "skew_tuning_get": (_int, [_vp, ctypes.c_char_p, ctypes.POINTER(ctypes.c_int64), _int, ctypes.POINTER(_int)]),
