@@ -358,7 +358,7 @@ SKEW_API int skew_tridiag_svd_z(skew_handle_t h, const double* ev, const double*
  * (skew_tuning_key lists them): bucket_edges (list), batch_smem_nmax,
  * batch_smem_nt_small, batch_smem_nt_large, batch_global_nt,
  * batch_global_ctas_per_sm, batch_graph, func_chain_nmax, blocked_min_n,
- * blocked_persistent, persist_ctas, persist_tail, persist_items, zpersist_min_n,
+ * blocked_persistent, cluster_max_n, persist_ctas, persist_tail, persist_items, zpersist_min_n,
  * zpersist_ctas, zpersist_items, pfz_cta_max, pfz_nt, pfz_ctas, and the limits
  * wait_polls (grid-barrier polls before SKEW_TIMEOUT; 0: the default, seconds),
  * wait_skip_cta (>= 0: that CTA of a cooperative kernel skips its arrivals, so the

@@ -319,6 +319,15 @@ static int blocked(skew_handle_t h, double* A, int64_t n, int64_t lda, double* t
     ev = ws + wsd;
     tau = ws + wsd + n;
   }
+  // up to cluster_max_n: one 16-CTA cluster with the matrix in distributed shared
+  // memory (no device-wide barriers)
+  if (n >= 3 && n <= h->tune.cluster_max_n) {
+    if (info) CK(cudaMemsetAsync(info, 0, sizeof(int), h->stream));
+    cudaError_t e = cluster_hessenberg(A, lda, (int)n, tau, ev, info, h->stream);
+    if (e == cudaSuccess) return SKEW_OK;
+    if (e != cudaErrorNotSupported) return SKEW_CUDA_ERROR;
+    cudaGetLastError();
+  }
   // one cooperative launch for all panels when v fits in shared memory; the
   // multi-launch path otherwise (or with the tuning key blocked_persistent = 0)
   const bool persistent = n <= 24576 && h->tune.blocked_persistent != 0;

@@ -1,0 +1,293 @@
+// Householder tridiagonalisation of one moderate-size real skew matrix
+// (skewhess!, hessenberg.jl:70-90, with the reflectors of householder!,
+// :26-44) inside one thread-block cluster of 16 CTAs.
+//
+// The whole matrix lives in the cluster's distributed shared memory: CTA r
+// holds the columns j = r, r + 16, r + 32, ... in full (all n rows), so n <=
+// 640 fits (16 x 227 KB).  Dealing the columns cyclically keeps every CTA
+// busy as the trailing block shrinks.  Step k (reflector v_k on rows k+1..n-1)
+// is the unblocked two-sided update of the batched kernel, spread over the
+// cluster:
+//   a. every CTA forms the partial row products of its own columns,
+//      P_r[i] = sum_{own j > k} W[i,j] v_j;
+//   b. cluster barrier;
+//   c. every CTA sums the 16 partials itself, in rank order, so all CTAs hold
+//      the same p = tau_k sum_r P_r bit for bit;
+//   d. the CTA owning column k+1 updates that column with warp 0 and builds
+//      reflector k+1 from it (look-ahead), while every other warp of the
+//      cluster applies W += v p^T - p v^T to its own columns j > k+1;
+//   e. cluster barrier; every CTA copies v_{k+1} and tau_{k+1} from the owner.
+// The hardware cluster barrier replaces the two grid barriers per column of the
+// persistent multi-CTA reduction, whose L2 round trips bound it at 15-20 us per
+// column on this size.
+//
+// Skew-symmetry is kept exactly although the two triangles live in different
+// CTAs: an element below the diagonal takes fma(v_i, p_j, fma(-p_i, v_j, a)),
+// one above it fma(-v_j, p_i, fma(p_j, v_i, a)), which is the exact negation of
+// its partner's value (round-to-nearest is symmetric under negation).  The
+// diagonal stays zero.
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "skew_common.cuh"
+#include "skew_internal.h"
+
+namespace cg = cooperative_groups;
+
+namespace skew {
+
+constexpr int CL = 16;       // CTAs per cluster
+constexpr int CL_NT = 512;   // threads per CTA
+constexpr int CL_NW = CL_NT / 32;
+
+struct ClusterParams {
+  double* A;
+  int64_t lda;
+  int n;
+  double* tau;
+  double* ev;
+  int* info;
+};
+
+// shared memory of one CTA, in doubles: own columns, then the vectors
+__host__ __device__ inline size_t cluster_smem_doubles(int n) {
+  const int nq = (n + CL - 1) / CL;
+  return (size_t)nq * n + 5 * (size_t)n + CL_NT + 64 + 8;
+}
+
+// The reflector of a column held by this CTA (col: its n entries), computed by
+// one warp: alpha = col[c+1], x = col[c+2:n].  Writes v (v[c+1] = 1) into the
+// column and into vout, beta and tau into ev[c] and tau[c] (global) and tau into
+// *tau_out.  householder! (hessenberg.jl:26-44) via make_reflector.
+__device__ void cluster_reflector_warp(double* col, int n, int c, double* vout, double* tau_out, double* ev,
+                                       double* tau) {
+  const int lane = threadIdx.x & 31;
+  double part = 0.0;
+  for (int r = c + 2 + lane; r < n; r += 32) part = fma(col[r], col[r], part);
+  const double ss = warp_sum(part);
+  double xn = -1.0;
+  if (ss_needs_scaling(ss)) {  // warp-uniform rare path: the norm with scaling
+    double mx = 0.0;
+    for (int r = c + 2 + lane; r < n; r += 32) mx = fmax(mx, fabs(col[r]));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    double q = 0.0;
+    if (mx > 0.0)
+      for (int r = c + 2 + lane; r < n; r += 32) {
+        const double x = col[r] / mx;
+        q = fma(x, x, q);
+      }
+    xn = mx * sqrt(warp_sum(q));
+  }
+  const Reflector R = make_reflector(col[c + 1], ss, xn);
+  if (lane == 0) {
+    ev[c] = R.beta;
+    tau[c] = R.tau;
+    *tau_out = R.tau;
+  }
+  for (int r = c + 1 + lane; r < n; r += 32) {
+    const double vr = (R.tau == 0.0) ? 0.0 : (r == c + 1 ? 1.0 : col[r] * R.scale);
+    vout[r] = vr;
+    col[r] = vr;
+  }
+}
+
+__global__ void __launch_bounds__(CL_NT, 1) cluster_hess_kernel(ClusterParams P) {
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = (int)cl.block_rank();
+  const int n = P.n, nq = (n + CL - 1) / CL;
+  const int tid = threadIdx.x, w = tid >> 5;
+  extern __shared__ __align__(16) double sm[];
+  double* Wl = sm;                     // own column q (global j = rank + CL q) at Wl + q n
+  double* v = Wl + (size_t)nq * n;     // current reflector v_k
+  double* p = v + n;                   // tau_k W v_k
+  double* vnext = p + n;               // reflector built here (owner of its column)
+  double* Pp = vnext + n;              // [2][n] partial row products, by step parity
+  double* part = Pp + 2 * n;           // [CL_NT] split-column partials
+  double* scal = part + CL_NT + 64;    // [0] tau_k, [1] tau of the reflector built here
+  const int ncl = (n - rank + CL - 1) / CL;  // own columns
+
+  for (int64_t e = tid; e < (int64_t)ncl * n; e += CL_NT) {
+    const int q = (int)(e / n), i = (int)(e - (int64_t)q * n);
+    Wl[e] = P.A[i + (int64_t)(rank + CL * q) * P.lda];
+  }
+  for (int i = tid; i < n; i += CL_NT) v[i] = 0.0;
+  __syncthreads();
+  // reflector 0 from column 0 (rank 0, warp 0)
+  if (rank == 0 && w == 0) cluster_reflector_warp(Wl, n, 0, vnext, scal + 1, P.ev, P.tau);
+  cl.sync();
+  {
+    const double* src = cl.map_shared_rank(vnext, 0);
+    for (int i = 1 + tid; i < n; i += CL_NT) v[i] = src[i];
+    if (tid == 0) scal[0] = *cl.map_shared_rank(scal + 1, 0);
+  }
+  __syncthreads();
+
+  for (int k = 0; k + 2 < n; k++) {
+    const double tauk = scal[0];
+    double* Pk = Pp + (k & 1) * n;
+    const int m = n - (k + 1);  // active rows k+1 .. n-1
+    // first own column >= k+1 and >= k+2
+    const int qa = (k + 1 > rank) ? (k + 1 - rank + CL - 1) / CL : 0;
+    const int qb = (k + 2 > rank) ? (k + 2 - rank + CL - 1) / CL : 0;
+    // a. partial row products over own columns j >= k+1; with few rows the
+    //    columns are split between thread groups and combined through `part`
+    {
+      const int rows_pp = min(CL_NT, (m + 31) & ~31);
+      const int cs = CL_NT / rows_pp;
+      const int ri = tid % rows_pp, c = tid / rows_pp;
+      for (int i0 = 0; i0 < m; i0 += rows_pp) {
+        const int i = k + 1 + i0 + ri;
+        if (c < cs && i < n) {
+          double a0 = 0.0, a1 = 0.0;
+          int q = qa + c;
+          for (; q + cs < ncl; q += 2 * cs) {
+            a0 = fma(Wl[(size_t)q * n + i], v[rank + CL * q], a0);
+            a1 = fma(Wl[(size_t)(q + cs) * n + i], v[rank + CL * (q + cs)], a1);
+          }
+          if (q < ncl) a0 = fma(Wl[(size_t)q * n + i], v[rank + CL * q], a0);
+          if (cs == 1)
+            Pk[i] = (tauk != 0.0) ? a0 + a1 : 0.0;
+          else
+            part[c * rows_pp + ri] = a0 + a1;
+        }
+      }
+      if (cs > 1) {  // then m <= rows_pp: one pass
+        __syncthreads();
+        for (int i = k + 1 + tid; i < n; i += CL_NT) {
+          double s = 0.0;
+          for (int cc = 0; cc < cs; cc++) s += part[cc * rows_pp + (i - k - 1)];
+          Pk[i] = (tauk != 0.0) ? s : 0.0;
+        }
+      }
+    }
+    cl.sync();  // b
+    // c. p = tau_k sum_r P_r, the same order in every CTA
+    for (int i = k + 1 + tid; i < n; i += CL_NT) {
+      double t[CL];
+#pragma unroll
+      for (int r = 0; r < CL; r++) t[r] = cl.map_shared_rank(Pk, r)[i];
+      double s = 0.0;
+#pragma unroll
+      for (int r = 0; r < CL; r++) s += t[r];
+      p[i] = tauk * s;
+    }
+    __syncthreads();
+    // d. look-ahead on column k+1 (its owner's warp 0), bulk update of own columns j >= k+2
+    const int c1 = k + 1;
+    const int owner = c1 % CL;
+    const bool look = (rank == owner);
+    if (look && w == 0) {
+      double* col = Wl + (size_t)(c1 / CL) * n;
+      if (tauk != 0.0) {
+        const double vc = v[c1], pc = p[c1];
+        for (int i = c1 + 1 + (tid & 31); i < n; i += 32) col[i] = fma(v[i], pc, fma(neg(p[i]), vc, col[i]));
+        __syncwarp();
+      }
+      if (c1 + 2 < n) {
+        cluster_reflector_warp(col, n, c1, vnext, scal + 1, P.ev, P.tau);
+      } else if ((tid & 31) == 0) {  // the last step: the real 1 x 1 tail (hessenberg.jl:27-29)
+        P.ev[c1] = col[c1 + 1];
+        P.tau[c1] = 0.0;
+      }
+    } else if (tauk != 0.0 && qb < ncl) {
+      const int t0 = look ? tid - 32 : tid, T = look ? CL_NT - 32 : CL_NT;
+      const int64_t total = (int64_t)(ncl - qb) * m;
+      for (int64_t e0 = t0; e0 < total; e0 += 4 * (int64_t)T) {
+        double a[4];
+        int ii[4], jj[4];
+        size_t at[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int64_t e = e0 + (int64_t)u * T;
+          ii[u] = -1;
+          if (e < total) {
+            const int qq = qb + (int)(e / m);
+            ii[u] = k + 1 + (int)(e - (int64_t)(qq - qb) * m);
+            jj[u] = rank + CL * qq;
+            at[u] = (size_t)qq * n + ii[u];
+            a[u] = Wl[at[u]];
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int i = ii[u], j = jj[u];
+          if (i < 0 || i == j) continue;
+          double x;
+          if (i > j)
+            x = fma(v[i], p[j], fma(neg(p[i]), v[j], a[u]));
+          else
+            x = fma(neg(v[j]), p[i], fma(p[j], v[i], a[u]));
+          Wl[at[u]] = x;
+        }
+      }
+    }
+    cl.sync();  // e
+    if (c1 + 2 < n) {
+      const double* src = cl.map_shared_rank(vnext, owner);
+      for (int i = c1 + 1 + tid; i < n; i += CL_NT) v[i] = src[i];
+      if (tid == 0) scal[0] = *cl.map_shared_rank(scal + 1, owner);
+    }
+    __syncthreads();
+  }
+  if (n == 2 && rank == 0 && tid == 0) {  // no step: the 1 x 1 tail only
+    P.ev[0] = Wl[1];
+    P.tau[0] = 0.0;
+  }
+  // the reduced matrix back in place (reflectors below the subdiagonal)
+  for (int64_t e = tid; e < (int64_t)ncl * n; e += CL_NT) {
+    const int q = (int)(e / n), i = (int)(e - (int64_t)q * n);
+    P.A[i + (int64_t)(rank + CL * q) * P.lda] = Wl[e];
+  }
+  if (rank == 0 && tid == 0 && P.info) *P.info = SKEW_OK;
+  cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+size_t cluster_hess_smem_bytes(int n) { return sizeof(double) * cluster_smem_doubles(n); }
+
+// One cluster of 16 CTAs.  cudaErrorNotSupported (the caller then takes the
+// grid-wide reduction) if the device cannot run a 16-CTA cluster with this
+// much shared memory per CTA.
+cudaError_t cluster_hessenberg(double* A, int64_t lda, int n, double* tau, double* ev, int* info, cudaStream_t st) {
+  if (n < 3) return cudaErrorInvalidValue;
+  const size_t smem = cluster_hess_smem_bytes(n);
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return e;
+  if (smem > (size_t)optin) return cudaErrorNotSupported;
+  static std::atomic<uint64_t> configured{0};
+  const uint64_t bit = 1ull << (dev & 63);
+  if (!(configured.load(std::memory_order_acquire) & bit)) {
+    e = cudaFuncSetAttribute(cluster_hess_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    if (e != cudaSuccess) return e;
+    e = cudaFuncSetAttribute(cluster_hess_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    if (e != cudaSuccess) return e;
+    configured.fetch_or(bit, std::memory_order_release);
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(CL);
+  cfg.blockDim = dim3(CL_NT);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = CL;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int clusters = 0;
+  e = cudaOccupancyMaxActiveClusters(&clusters, (void*)cluster_hess_kernel, &cfg);
+  if (e != cudaSuccess || clusters < 1) {
+    cudaGetLastError();
+    return cudaErrorNotSupported;
+  }
+  ClusterParams P{A, lda, n, tau, ev, info};
+  return cudaLaunchKernelEx(&cfg, cluster_hess_kernel, P);
+}
+
+}  // namespace skew

@@ -49,6 +49,7 @@ struct Tuning {
   // one large real matrix
   int blocked_min_n;             // the blocked multi-CTA reduction from this n
   int blocked_persistent;        // 1: one cooperative launch for all panels
+  int cluster_max_n;             // up to this n, one 16-CTA cluster with the matrix in shared memory
   int persist_ctas;              // grid of the persistent reduction (0: chosen by n)
   int persist_tail;              // columns left to the one-CTA kernel (0: the default)
   int persist_items;             // matvec tiles per warp and column
@@ -277,6 +278,10 @@ size_t blocked_ws_doubles(int n);
 cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, double* ev, int* info, double* ws, int sms,
                                cudaStream_t st);
 size_t persist_ws_extra_doubles();
+// One moderate-size matrix (3 <= n, 16 x its shared memory per CTA) in one 16-CTA
+// thread-block cluster, the matrix in distributed shared memory (skew_cluster.cu);
+// cudaErrorNotSupported if the device cannot run that cluster.
+cudaError_t cluster_hessenberg(double* A, int64_t lda, int n, double* tau, double* ev, int* info, cudaStream_t st);
 // One cooperative launch for all panels (grid barriers with bounded waits); then the tail.
 cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double* tau, double* ev, int* info,
                                           double* ws, int sms, int* err_dev, const Tuning& T, cudaStream_t st);

@@ -44,6 +44,7 @@ void tuning_defaults(Tuning* T) {
   T->func_chain_nmax = 64;
   T->blocked_min_n = 192;
   T->blocked_persistent = 1;
+  T->cluster_max_n = 640;
   T->persist_ctas = 0;
   T->persist_tail = 0;
   T->persist_items = 8;
@@ -84,6 +85,7 @@ const Key kKeys[] = {
     {"func_chain_nmax", &Tuning::func_chain_nmax, 0, 1 << 20, nullptr, 0},
     {"blocked_min_n", &Tuning::blocked_min_n, 16, 1025, nullptr, 0},
     {"blocked_persistent", &Tuning::blocked_persistent, 0, 1, k01, 2},
+    {"cluster_max_n", &Tuning::cluster_max_n, 0, 640, nullptr, 0},
     {"persist_ctas", &Tuning::persist_ctas, 0, 1 << 16, nullptr, 0},
     {"persist_tail", &Tuning::persist_tail, 0, 1024, nullptr, 0},
     {"persist_items", &Tuning::persist_items, 1, 16, nullptr, 0},

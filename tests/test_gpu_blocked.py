@@ -81,3 +81,33 @@ def test_blocked_determinism(skewgpu):
     h1 = skewgpu.hessenberg(A).ev.cpu().numpy()
     h2 = skewgpu.hessenberg(A).ev.cpu().numpy()
     assert np.array_equal(h1, h2)
+
+
+@pytest.mark.parametrize("n", [16, 17, 31, 64, 97, 160, 255, 320, 511, 513, 640])
+def test_cluster_reduction_vs_oracle(skewgpu, oracle, n):
+    """The 16-CTA cluster reduction (the matrix in distributed shared memory), forced
+    down to n = 16 through the tuning key blocked_min_n: ev entrywise against the
+    oracle (binary128 up to n = 384, its FP64 restatement above), the same reflector
+    pattern, Q T Q^T = A and log|Pf|; and the same values as the grid-wide reduction
+    (cluster_max_n = 0) to rounding."""
+    A = skew_random(n, 1300 + n) / np.sqrt(n)
+    with skewgpu.tuned(blocked_min_n=16):
+        H = skewgpu.hessenberg(A)
+        lp, sg = skewgpu.logabspfaffian(A)
+        with skewgpu.tuned(cluster_max_n=0):
+            H2 = skewgpu.hessenberg(A)
+    ev = H.ev.cpu().numpy()
+    tau = H.tau.cpu().numpy()
+    _, tq, evq = oracle.hessenberg(A, quad=(n <= 384))
+    scale = np.abs(evq).max()
+    np.testing.assert_allclose(ev, evq, atol=RTOL * scale)
+    assert np.array_equal(tau != 0, tq != 0)
+    np.testing.assert_allclose(ev, H2.ev.cpu().numpy(), atol=1e-13 * scale)
+    Q = oracle.formq(skewgpu.from_device(H.factors), tau)
+    np.testing.assert_allclose(Q @ tridiag_dense(ev) @ Q.T, A, atol=1e-12 * np.abs(A).max() * np.sqrt(n))
+    rl, rs = oracle.logabspfaffian(A, quad=(n <= 384))
+    assert sg == rs
+    if np.isfinite(rl):
+        assert abs(lp - rl) <= RTOL * max(1.0, abs(rl))
+    else:
+        assert lp == rl
