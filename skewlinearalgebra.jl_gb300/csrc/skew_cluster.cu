@@ -11,8 +11,8 @@
 //   a. every CTA forms the partial row products of its own columns,
 //      P_r[i] = sum_{own j > k} W[i,j] v_j;
 //   b. cluster barrier;
-//   c. every CTA sums the 16 partials itself, in rank order, so all CTAs hold
-//      the same p = tau_k sum_r P_r bit for bit;
+//   c. every CTA sums the 16 partials itself, by the same pairwise tree, so all
+//      CTAs hold the same p = tau_k sum_r P_r bit for bit;
 //   d. the CTA owning column k+1 updates that column with warp 0 and builds
 //      reflector k+1 from it (look-ahead), while every other warp of the
 //      cluster applies W += v p^T - p v^T to its own columns j > k+1;
@@ -60,12 +60,16 @@ __host__ __device__ inline size_t cluster_smem_doubles(int n) {
 // The reflector of a column held by this CTA (col: its n entries), computed by
 // one warp: alpha = col[c+1], x = col[c+2:n].  Writes v (v[c+1] = 1) into the
 // column and into vout, beta and tau into ev[c] and tau[c] (global) and tau into
-// *tau_out.  householder! (hessenberg.jl:26-44) via make_reflector.
+// *tau_out.  householder! (hessenberg.jl:26-44) via make_reflector.  part is this
+// lane's share of |x|^2 (the lanes together covering rows c+2..n-1 once), or
+// negative to have it formed here.
 __device__ void cluster_reflector_warp(double* col, int n, int c, double* vout, double* tau_out, double* ev,
-                                       double* tau) {
+                                       double* tau, double part = -1.0) {
   const int lane = threadIdx.x & 31;
-  double part = 0.0;
-  for (int r = c + 2 + lane; r < n; r += 32) part = fma(col[r], col[r], part);
+  if (part < 0.0) {
+    part = 0.0;
+    for (int r = c + 2 + lane; r < n; r += 32) part = fma(col[r], col[r], part);
+  }
   const double ss = warp_sum(part);
   double xn = -1.0;
   if (ss_needs_scaling(ss)) {  // warp-uniform rare path: the norm with scaling
@@ -164,15 +168,17 @@ __global__ void __launch_bounds__(CL_NT, 1) cluster_hess_kernel(ClusterParams P)
       }
     }
     cl.sync();  // b
-    // c. p = tau_k sum_r P_r, the same order in every CTA
+    // c. p = tau_k sum_r P_r: a fixed pairwise tree (four dependent adds instead of
+    //    sixteen), the same in every CTA
     for (int i = k + 1 + tid; i < n; i += CL_NT) {
       double t[CL];
 #pragma unroll
       for (int r = 0; r < CL; r++) t[r] = cl.map_shared_rank(Pk, r)[i];
-      double s = 0.0;
 #pragma unroll
-      for (int r = 0; r < CL; r++) s += t[r];
-      p[i] = tauk * s;
+      for (int h = CL / 2; h >= 1; h >>= 1)
+#pragma unroll
+        for (int r = 0; r < h; r++) t[r] = t[r] + t[r + h];
+      p[i] = tauk * t[0];
     }
     __syncthreads();
     // d. look-ahead on column k+1 (its owner's warp 0), bulk update of own columns j >= k+2
@@ -181,13 +187,20 @@ __global__ void __launch_bounds__(CL_NT, 1) cluster_hess_kernel(ClusterParams P)
     const bool look = (rank == owner);
     if (look && w == 0) {
       double* col = Wl + (size_t)(c1 / CL) * n;
+      double part = 0.0;  // this lane's share of |x|^2 of the updated column, formed on the way
       if (tauk != 0.0) {
         const double vc = v[c1], pc = p[c1];
-        for (int i = c1 + 1 + (tid & 31); i < n; i += 32) col[i] = fma(v[i], pc, fma(neg(p[i]), vc, col[i]));
+        for (int i = c1 + 1 + (tid & 31); i < n; i += 32) {
+          const double a = fma(v[i], pc, fma(neg(p[i]), vc, col[i]));
+          col[i] = a;
+          if (i >= c1 + 2) part = fma(a, a, part);
+        }
         __syncwarp();
+      } else {
+        for (int i = c1 + 2 + (tid & 31); i < n; i += 32) part = fma(col[i], col[i], part);
       }
       if (c1 + 2 < n) {
-        cluster_reflector_warp(col, n, c1, vnext, scal + 1, P.ev, P.tau);
+        cluster_reflector_warp(col, n, c1, vnext, scal + 1, P.ev, P.tau, part);
       } else if ((tid & 31) == 0) {  // the last step: the real 1 x 1 tail (hessenberg.jl:27-29)
         P.ev[c1] = col[c1 + 1];
         P.tau[c1] = 0.0;

@@ -153,7 +153,7 @@ class Tuner:
         # the crossover from the one-CTA kernel to the blocked reduction
         rows = []
         best = None
-        for n in (96, 112, 128, 144, 160, 176, 192, 224, 256):
+        for n in (48, 64, 80, 96, 112, 128, 160, 192, 256):
             skewgpu.tuning_set("blocked_min_n", 1025)
             t1 = hess_time(n)
             skewgpu.tuning_set("blocked_min_n", 16)
