@@ -358,8 +358,10 @@ SKEW_API int skew_tridiag_svd_z(skew_handle_t h, const double* ev, const double*
  * (skew_tuning_key lists them): bucket_edges (list), batch_smem_nmax,
  * batch_smem_nt_small, batch_smem_nt_large, batch_global_nt,
  * batch_global_ctas_per_sm, batch_graph, func_chain_nmax, blocked_min_n,
- * blocked_persistent, cluster_max_n, persist_ctas, persist_tail, persist_items, zpersist_min_n,
- * zpersist_ctas, zpersist_items, pfz_cta_max, pfz_nt, pfz_ctas, and the limits
+ * blocked_persistent, cluster_max_n, persist_ctas, persist_tail, persist_items,
+ * persist_nb (panel width of the blocked reduction, 8..128; 64 at most on the
+ * multi-launch path), zpersist_min_n, zpersist_ctas, zpersist_items, zpersist_nb (the
+ * complex panel width, 4..32), pfz_cta_max, pfz_nt, pfz_ctas, and the limits
  * wait_polls (grid-barrier polls before SKEW_TIMEOUT; 0: the default, seconds),
  * wait_skip_cta (>= 0: that CTA of a cooperative kernel skips its arrivals, so the
  * bounded waits run out: a test of the timeout path; -1: off) and qr_max_iter (QR

@@ -338,7 +338,7 @@ static int blocked(skew_handle_t h, double* A, int64_t n, int64_t lda, double* t
     if (e != cudaErrorNotSupported && e != cudaErrorCooperativeLaunchTooLarge) return SKEW_CUDA_ERROR;
     cudaGetLastError();
   }
-  CK(blocked_hessenberg(A, lda, (int)n, tau, ev, info, ws, h->sms, h->stream));
+  CK(blocked_hessenberg(A, lda, (int)n, tau, ev, info, ws, h->sms, h->tune.persist_nb, h->stream));
   return SKEW_OK;
 }
 

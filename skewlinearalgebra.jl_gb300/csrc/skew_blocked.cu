@@ -28,7 +28,8 @@
 
 namespace skew {
 
-constexpr int BNB = 64;        // panel width
+constexpr int BNB = 64;        // largest panel width of the multi-launch path
+constexpr int PNB_MAX = 128;   // largest panel width of the persistent kernel
 constexpr int SYM_ROWS = 256;  // rows per sym CTA (one per thread)
 constexpr int FIN_ROWS = 64;   // rows per fin CTA (4 threads per row)
 constexpr int PF_ROWS = 16;    // persistent kernel, phase B: smallest row block
@@ -36,7 +37,7 @@ constexpr int UPD_T = 64;      // update tile edge
 constexpr int TAIL = 128;      // columns left to the one-CTA kernel
 
 struct BlockedWs {
-  double* W;      // n x BNB, column-major, ld n (rows indexed globally)
+  double* W;      // n x PNB_MAX, column-major, ld n (rows indexed globally)
   double* ypart;  // max_chunks x n
   double* upart;  // max_symtiles x (2 * BNB)
   double* sspart; // max_fintiles
@@ -49,7 +50,7 @@ size_t blocked_ws_doubles(int n) {
   const int max_chunks = 64;
   const int max_symtiles = (n + SYM_ROWS - 1) / SYM_ROWS;
   const int max_fintiles = (n + PF_ROWS - 1) / PF_ROWS;  // covers FIN_ROWS row tiles too
-  return (size_t)n * BNB + (size_t)max_chunks * n + (size_t)max_symtiles * 2 * BNB + max_fintiles + 3 * (size_t)n +
+  return (size_t)n * PNB_MAX + (size_t)max_chunks * n + (size_t)max_symtiles * 2 * BNB + max_fintiles + 3 * (size_t)n +
          8;
 }
 
@@ -60,7 +61,7 @@ static BlockedWs carve_ws(double* base, int n) {
   w.max_fintiles = (n + PF_ROWS - 1) / PF_ROWS;
   double* p = base;
   w.W = p;
-  p += (size_t)n * BNB;
+  p += (size_t)n * PNB_MAX;
   w.ypart = p;
   p += (size_t)w.max_chunks * n;
   w.upart = p;
@@ -485,9 +486,11 @@ cudaError_t launch_pf_from_tridiag(const double* ev, const double* tau, int n, d
 }
 
 // Host driver.  ws must hold blocked_ws_doubles(n) doubles; A is reduced in place.
+// Panels of nb columns (at most BNB).
 cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, double* ev, int* info, double* wsbase,
-                               int sms, cudaStream_t st) {
+                               int sms, int nb, cudaStream_t st) {
   BlockedWs ws = carve_ws(wsbase, n);
+  nb = std::max(1, std::min(BNB, nb));
   cudaError_t e = cudaMemsetAsync(ws.ticket, 0, sizeof(unsigned), st);
   if (e != cudaSuccess) return e;
   int p = 0;
@@ -497,7 +500,7 @@ cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, doubl
   }
   while (n - p > TAIL) {
     // panel columns p .. p+nbp-1; keep at least TAIL columns for the tail
-    const int nbp = min(BNB, n - TAIL - p);
+    const int nbp = min(nb, n - TAIL - p);
     for (int i = 0; i < nbp; i++) {
       const int c = p + i;
       const int m = n - (c + 1);
@@ -565,11 +568,12 @@ struct PersistParams {
   double* A;
   int64_t lda;
   int n, pend;  // panels cover reflector columns [0, pend)
+  int nb;       // panel width (<= the kernel's NBC)
   double* tau;
   double* ev;
-  double* W;       // n x BNB
+  double* W;       // n x nb
   double* ypart;   // maxck x n
-  double* u;       // 2 * BNB (u1, then u2 at BNB)
+  double* u;       // 2 * NBC (u1, then u2 at NBC)
   double* sspart;  // row-block norm partials
   unsigned* sync;  // [0] barrier count, [1] barrier generation, [2] item counter
   int* err;
@@ -754,12 +758,12 @@ __device__ void upd_tile(double* __restrict__ A, int64_t lda, int n, int p, int 
 // norm partials of its rows below the subdiagonal.  Blocks of 256 / TPR rows, TPR
 // threads per row; a thread's panel terms j = g + TPR t are loaded once and used
 // both for W and for the column update.
-template <int TPR>
+template <int TPR, int NBC>
 __device__ void rows_phase(const PersistParams& P, double* A, int64_t lda, int n, int p, int c, int i, int nck,
                            bool last, const Refl3& R, const double* psm, const double* su, const double* sWrow,
                            const double* sArow, double* red) {
   constexpr int ROWS = P_NT / TPR;
-  constexpr int NJ = BNB / TPR;
+  constexpr int NJ = NBC / TPR;
   const int tid = threadIdx.x;
   const int m = n - c - 1;
   const int nfb = (m + ROWS - 1) / ROWS;
@@ -792,7 +796,7 @@ __device__ void rows_phase(const PersistParams& P, double* A, int64_t lda, int n
 #pragma unroll
       for (int t = 0; t < NJ; t++) {
         const int j = g + TPR * t;
-        if (j < i) acc = fma(aj[t], su[j], fma(-wj[t], su[BNB + j], acc));
+        if (j < i) acc = fma(aj[t], su[j], fma(-wj[t], su[NBC + j], acc));
       }
     }
 #pragma unroll
@@ -825,11 +829,13 @@ __device__ void rows_phase(const PersistParams& P, double* A, int64_t lda, int n
   }
 }
 
+// NBC: compiled panel-width bound (64 or 128); the panels are P.nb <= NBC wide.
+template <int NBC>
 __global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
   extern __shared__ __align__(16) double psm[];  // v stage (n doubles) | update tile buffers
   __shared__ double red[P_NW];
-  __shared__ double su[2 * BNB];
-  __shared__ double sWrow[BNB + 1], sArow[BNB + 1];
+  __shared__ double su[2 * NBC];
+  __shared__ double sWrow[NBC + 1], sArow[NBC + 1];
   __shared__ int s_item, s_scal;
   __shared__ Refl3 s_R3;
   const int n = P.n;
@@ -846,7 +852,7 @@ __global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
   }
   int p = 0;
   while (p < P.pend) {
-    const int nbp = min(BNB, P.pend - p);
+    const int nbp = min(P.nb, P.pend - p);
     for (int i = 0; i < nbp; i++) {
       const int c = p + i, m = n - c - 1;
       // ---- A: stage v, then items from the shared counter
@@ -877,7 +883,7 @@ __global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
           }
           if (r < n) a0 = fma(ldg2(col + r), psm[r], a0);
           const double s = warp_sum(a0 + a1);
-          if (lane == 0) P.u[d < i ? d : BNB + j] = s;
+          if (lane == 0) P.u[d < i ? d : NBC + j] = s;
         } else {
           const int qq = (int)it - ndots;
           const int rt = qq / nck, ck = qq - rt * nck;
@@ -910,13 +916,13 @@ __global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
       if (!gsync(P)) return;
       // ---- B: rows
       const bool last = (i == nbp - 1);
-      for (int d = tid; d < 2 * i; d += P_NT) su[d < i ? d : BNB + d - i] = ldg2(P.u + (d < i ? d : BNB + d - i));
+      for (int d = tid; d < 2 * i; d += P_NT) su[d < i ? d : NBC + d - i] = ldg2(P.u + (d < i ? d : NBC + d - i));
       __syncthreads();
       if (w == 0) {
         const int r0 = c + 1;
         double acc = 0.0;
         for (int j = lane; j < i; j += 32)
-          acc = fma(ldg2(A + r0 + (int64_t)(p + j) * lda), su[j], fma(-ldg2(P.W + (size_t)j * n + r0), su[BNB + j], acc));
+          acc = fma(ldg2(A + r0 + (int64_t)(p + j) * lda), su[j], fma(-ldg2(P.W + (size_t)j * n + r0), su[NBC + j], acc));
         for (int q = lane; q < nck; q += 32) acc += ldg2(P.ypart + (size_t)q * n + r0);
         acc = warp_sum(acc);
         if (lane == 0) sWrow[i] = R.tau * acc;
@@ -928,19 +934,20 @@ __global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
       }
       __syncthreads();
       // rows in blocks, TPR threads per row: as many threads per row as keeps every
-      // block in one round of CTAs (16 at small m, fewer at large m)
+      // block in one round of CTAs (16 at small m, fewer at large m; at least 8 for
+      // 128-wide panels, whose 4-thread rows would hold 32 panel terms per thread)
       int nfb;
       {
         const int G = gridDim.x;
         if ((m + 15) / 16 <= G) {
           nfb = (m + 15) / 16;
-          rows_phase<16>(P, A, lda, n, p, c, i, nck, last, R, psm, su, sWrow, sArow, red);
-        } else if ((m + 31) / 32 <= G) {
+          rows_phase<16, NBC>(P, A, lda, n, p, c, i, nck, last, R, psm, su, sWrow, sArow, red);
+        } else if ((m + 31) / 32 <= G || NBC > 64) {
           nfb = (m + 31) / 32;
-          rows_phase<8>(P, A, lda, n, p, c, i, nck, last, R, psm, su, sWrow, sArow, red);
+          rows_phase<8, NBC>(P, A, lda, n, p, c, i, nck, last, R, psm, su, sWrow, sArow, red);
         } else {
           nfb = (m + 63) / 64;
-          rows_phase<4>(P, A, lda, n, p, c, i, nck, last, R, psm, su, sWrow, sArow, red);
+          rows_phase<4, NBC>(P, A, lda, n, p, c, i, nck, last, R, psm, su, sWrow, sArow, red);
         }
       }
       if (!gsync(P)) return;
@@ -998,7 +1005,7 @@ __global__ void __launch_bounds__(P_NT, 2) persist_kernel(PersistParams P) {
   }
 }
 
-size_t persist_ws_extra_doubles() { return 2 * BNB + 8; }
+size_t persist_ws_extra_doubles() { return 2 * PNB_MAX + 8; }
 
 // info <- SKEW_TIMEOUT if a grid barrier of the persistent kernel gave up.
 __global__ void merge_err_kernel(const int* err, int* info) {
@@ -1010,14 +1017,18 @@ __global__ void merge_err_kernel(const int* err, int* info) {
 cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double* tau, double* ev, int* info,
                                           double* wsbase, int sms, int* err_dev, const Tuning& T, cudaStream_t st) {
   BlockedWs ws = carve_ws(wsbase, n);
-  double* extra = wsbase + blocked_ws_doubles(n);  // u (2*BNB), 4 sync words, error flag
-  int* err_dev_local = (int*)(extra + 2 * BNB + 4);
+  double* extra = wsbase + blocked_ws_doubles(n);  // u (2*PNB_MAX), 4 sync words, error flag
+  int* err_dev_local = (int*)(extra + 2 * PNB_MAX + 4);
   if (!err_dev) err_dev = err_dev_local;
+  // panel width: the tuning key persist_nb (setnb, hessenberg.jl:133-142, decides it
+  // by rule); widths above 64 run the instantiation with 128-entry panel arrays
+  const int nb = std::max(8, std::min(PNB_MAX, T.persist_nb));
+  const void* kern = nb <= 64 ? (const void*)persist_kernel<64> : (const void*)persist_kernel<128>;
   const size_t smem = max((size_t)n * sizeof(double), (size_t)UPD_T * (UPD_T + 1) * sizeof(double));
-  cudaError_t e = cudaFuncSetAttribute(persist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (e != cudaSuccess) return e;
   int occ = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, persist_kernel, P_NT, smem);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, P_NT, smem);
   if (e != cudaSuccess) return e;
   if (occ < 1) return cudaErrorNotSupported;
   // Two CTAs per SM hide more load latency on large matrices; below that, the two
@@ -1035,13 +1046,14 @@ cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double*
   P.lda = lda;
   P.n = n;
   P.pend = n - tail;
+  P.nb = nb;
   P.tau = tau;
   P.ev = ev;
   P.W = ws.W;
   P.ypart = ws.ypart;
   P.u = extra;
   P.sspart = ws.sspart;
-  P.sync = (unsigned*)(extra + 2 * BNB);
+  P.sync = (unsigned*)(extra + 2 * PNB_MAX);
   P.err = err_dev;
   P.maxck = ws.max_chunks;
   // matvec tiles per warp and column: measured on GB300 at n = 8192, 8 gives 932 ms,
@@ -1055,7 +1067,7 @@ cudaError_t blocked_hessenberg_persistent(double* A, int64_t lda, int n, double*
   if (e != cudaSuccess) return e;
   if (P.pend > 0) {
     void* args[] = {&P};
-    e = cudaLaunchCooperativeKernel((const void*)persist_kernel, dim3(grid), dim3(P_NT), args, smem, st);
+    e = cudaLaunchCooperativeKernel(kern, dim3(grid), dim3(P_NT), args, smem, st);
     if (e != cudaSuccess) return e;
   }
   SingleParams S;

@@ -53,10 +53,12 @@ struct Tuning {
   int persist_ctas;              // grid of the persistent reduction (0: chosen by n)
   int persist_tail;              // columns left to the one-CTA kernel (0: the default)
   int persist_items;             // matvec tiles per warp and column
+  int persist_nb;                // panel width of the blocked reduction (setnb's role)
   // ComplexF64
   int zpersist_min_n;            // the persistent complex reduction from this n
   int zpersist_ctas;             // its grid (0: one CTA per SM)
   int zpersist_items;            // its matvec tiles per warp and column
+  int zpersist_nb;               // its panel width
   int pfz_cta_max;               // complex Pfaffian: one CTA per matrix up to this n, a grid above
   int pfz_nt;                    // threads per CTA of the one-CTA Pfaffian (0: chosen by n)
   int pfz_ctas;                  // grid of the cooperative Pfaffian (0: chosen by n)
@@ -276,7 +278,7 @@ cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st);
 // Multi-CTA blocked reduction of one large matrix (skew_blocked.cu).
 size_t blocked_ws_doubles(int n);
 cudaError_t blocked_hessenberg(double* A, int64_t lda, int n, double* tau, double* ev, int* info, double* ws, int sms,
-                               cudaStream_t st);
+                               int nb, cudaStream_t st);
 size_t persist_ws_extra_doubles();
 // One moderate-size matrix (3 <= n, 16 x its shared memory per CTA) in one 16-CTA
 // thread-block cluster, the matrix in distributed shared memory (skew_cluster.cu);

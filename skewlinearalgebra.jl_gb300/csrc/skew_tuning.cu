@@ -48,9 +48,11 @@ void tuning_defaults(Tuning* T) {
   T->persist_ctas = 0;
   T->persist_tail = 0;
   T->persist_items = 8;
+  T->persist_nb = 64;
   T->zpersist_min_n = 384;
   T->zpersist_ctas = 0;
   T->zpersist_items = 4;
+  T->zpersist_nb = 32;
   T->pfz_cta_max = 160;
   T->pfz_nt = 0;
   T->pfz_ctas = 0;
@@ -89,9 +91,11 @@ const Key kKeys[] = {
     {"persist_ctas", &Tuning::persist_ctas, 0, 1 << 16, nullptr, 0},
     {"persist_tail", &Tuning::persist_tail, 0, 1024, nullptr, 0},
     {"persist_items", &Tuning::persist_items, 1, 16, nullptr, 0},
+    {"persist_nb", &Tuning::persist_nb, 8, 128, nullptr, 0},
     {"zpersist_min_n", &Tuning::zpersist_min_n, 129, 1 << 15, nullptr, 0},
     {"zpersist_ctas", &Tuning::zpersist_ctas, 0, 1 << 16, nullptr, 0},
     {"zpersist_items", &Tuning::zpersist_items, 1, 8, nullptr, 0},
+    {"zpersist_nb", &Tuning::zpersist_nb, 4, 32, nullptr, 0},
     {"pfz_cta_max", &Tuning::pfz_cta_max, 0, 160, nullptr, 0},
     {"pfz_nt", &Tuning::pfz_nt, 0, 512, kpfz_nt, 5},
     {"pfz_ctas", &Tuning::pfz_ctas, 0, 1 << 16, nullptr, 0},

@@ -39,7 +39,7 @@ namespace {
 
 constexpr int ZP_NT = 256;
 constexpr int ZP_NW = ZP_NT / 32;
-constexpr int ZBNB = 32;   // panel width
+constexpr int ZBNB = 32;   // largest panel width
 constexpr int ZUT = 64;    // trailing-update tile edge
 constexpr int ZKC = 8;     // panel columns per shared-memory stage of the update
 constexpr int ZFIN = 16;   // smallest row block of phase B (sizes sspart)
@@ -95,6 +95,7 @@ struct ZPersistParams {
   zc* A;
   int64_t lda;
   int n, pend;  // panels cover reflector columns [0, pend)
+  int nb;       // panel width (<= ZBNB)
   zc* tau;
   double* ev;
   zc* W;          // n x ZBNB, column j at W + j * n
@@ -408,7 +409,7 @@ __global__ void __launch_bounds__(ZP_NT, 1) zpersist_kernel(ZPersistParams P) {
   }
   int p = 0;
   while (p < P.pend) {
-    const int nbp = min(ZBNB, P.pend - p);
+    const int nbp = min(P.nb, P.pend - p);
     for (int i = 0; i < nbp; i++) {
       const int c = p + i, m = n - c - 1;
       const bool zero = zzero(R.tau);
@@ -646,6 +647,7 @@ cudaError_t zhess_persistent(double* Ad, int64_t lda, int n, double* taud, doubl
   P.lda = lda;
   P.n = n;
   P.pend = n - 1 - ZTAILP;
+  P.nb = std::max(4, std::min(ZBNB, tune.zpersist_nb));
   P.tau = tau;
   P.ev = ev;
   const size_t nn = (size_t)n, maxck = (size_t)zp_maxck(n);

@@ -15,8 +15,10 @@ on seeded synthetic workloads shaped like the benchmark configurations:
   batch_smem_nt_small, batch_smem_nt_large, batch_global_nt,
   batch_global_ctas_per_sm;
 * single real matrices: blocked_min_n (the size from which the multi-CTA blocked
-  reduction beats the one-CTA kernel), persist_items and persist_ctas (n = 4096);
-* single complex matrices: zpersist_min_n and zpersist_items;
+  reduction beats the one-CTA kernel), persist_items and persist_ctas (n = 4096),
+  and the panel width persist_nb (total time at n = 2048 and 8192);
+* single complex matrices: zpersist_min_n, zpersist_items and the panel width
+  zpersist_nb (n = 2048);
 * batched exp adjoint over n in {32, 64, ..., 512}: func_chain_nmax.
 
 Every measurement is recorded in the table next to the chosen values.  Timing:
@@ -170,6 +172,10 @@ class Tuner:
         self.sweep("persist_items", [2, 4, 8, 16], lambda: hess_time(n))
         sms = torch.cuda.get_device_properties(0).multi_processor_count
         self.sweep("persist_ctas", [0, sms, 2 * sms], lambda: hess_time(n))
+        # the panel width (setnb's number in the reference): wider panels move work from
+        # the per-column phases into the rank-2nb trailing update
+        sizes = (1024, 2048) if self.quick else (2048, 8192)
+        self.sweep("persist_nb", [32, 48, 64, 96, 128], lambda: sum(hess_time(m) for m in sizes))
 
     # -- single complex matrices ------------------------------------------------------
     def single_complex(self) -> None:
@@ -210,6 +216,7 @@ class Tuner:
                                                 for r in rows) + f"  -> {skewgpu.tuning_get('zpersist_min_n')}",
               flush=True)
         self.sweep("zpersist_items", [2, 4, 8], lambda: zhess_time(1024 if self.quick else 2048))
+        self.sweep("zpersist_nb", [8, 16, 24, 32], lambda: zhess_time(1024 if self.quick else 2048))
 
     # -- batched exp adjoint --------------------------------------------------------------
     def functions(self) -> None:

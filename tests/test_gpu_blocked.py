@@ -111,3 +111,44 @@ def test_cluster_reduction_vs_oracle(skewgpu, oracle, n):
         assert abs(lp - rl) <= RTOL * max(1.0, abs(rl))
     else:
         assert lp == rl
+
+
+_PANEL_REF = {}
+
+
+def _panel_ref(oracle, n):
+    """Oracle reduction of the panel-width test matrix (binary128 up to n = 384)."""
+    if n not in _PANEL_REF:
+        A = skew_random(n, 1700 + n) / np.sqrt(n)
+        _, tq, evq = oracle.hessenberg(A, quad=(n <= 384))
+        _PANEL_REF[n] = (A, tq, evq, oracle.logabspfaffian(A, quad=(n <= 384)))
+    return _PANEL_REF[n]
+
+
+@pytest.mark.parametrize("n,path,nb", [
+    (300, "persistent", 8), (300, "persistent", 24), (300, "persistent", 64), (300, "persistent", 72),
+    (300, "persistent", 128), (300, "multilaunch", 8), (300, "multilaunch", 40), (300, "multilaunch", 128),
+    (1000, "persistent", 40), (1000, "persistent", 96), (1000, "persistent", 128)])
+def test_blocked_panel_width_vs_oracle(skewgpu, oracle, n, path, nb):
+    """The panel width of the blocked reduction (the tuning key persist_nb, the role of
+    setnb in hessenberg.jl:133-142) changes the order of the arithmetic, not the
+    result: for widths 8 .. 128 on the persistent kernel (the 64- and 128-entry
+    instantiations) and on the multi-launch path (which caps the width at 64), ev
+    entrywise against the oracle, the same reflector pattern, Q T Q^T = A and
+    log|Pf|.  The cluster reduction is switched off so these sizes reach the grid-wide
+    kernels."""
+    A, tq, evq, (rl, rs) = _panel_ref(oracle, n)
+    keys = dict(blocked_min_n=16, cluster_max_n=0, persist_nb=nb,
+                blocked_persistent=1 if path == "persistent" else 0)
+    with skewgpu.tuned(**keys):
+        H = skewgpu.hessenberg(A)
+        lp, sg = skewgpu.logabspfaffian(A)
+    ev = H.ev.cpu().numpy()
+    tau = H.tau.cpu().numpy()
+    scale = np.abs(evq).max()
+    np.testing.assert_allclose(ev, evq, atol=RTOL * scale)
+    assert np.array_equal(tau != 0, tq != 0)
+    Q = oracle.formq(skewgpu.from_device(H.factors), tau)
+    np.testing.assert_allclose(Q @ tridiag_dense(ev) @ Q.T, A, atol=1e-12 * np.abs(A).max() * np.sqrt(n))
+    assert sg == rs
+    assert abs(lp - rl) <= RTOL * max(1.0, abs(rl))

@@ -77,6 +77,27 @@ def test_hessenberg_complex_persistent_vs_oracle(skewgpu, oracle, n):
     np.testing.assert_allclose(Q.conj().T @ A @ Q, Hc.H(), atol=1e-13 * scale * n)
 
 
+@pytest.mark.parametrize("nb", [4, 12, 32])
+def test_hessenberg_complex_panel_width(skewgpu, oracle, nb):
+    """The complex persistent reduction at panel widths 4, 12 and 32 (the tuning key
+    zpersist_nb): the same checks as at the default width."""
+    n = 300
+    A = skewh_random(n, 1900 + n)
+    with skewgpu.tuned(zpersist_min_n=130, zpersist_nb=nb):
+        Hc = skewgpu.hessenberg_complex(A)
+    ev = Hc.ev.cpu().numpy()
+    dvim = Hc.dvim.cpu().numpy()
+    tau = Hc.tau.cpu().numpy()
+    F = skewgpu.from_device_complex(Hc.factors)
+    scale = max(1.0, np.abs(A).max())
+    _, tq, eq, dq = oracle.hessenberg_complex(A, quad=False)
+    np.testing.assert_allclose(ev, eq, atol=1e-11 * scale * np.sqrt(n))
+    np.testing.assert_allclose(dvim, dq, atol=1e-11 * scale * np.sqrt(n))
+    np.testing.assert_allclose(tau, tq, atol=1e-10)
+    Q = formq_complex(F, tau)
+    np.testing.assert_allclose(Q.conj().T @ A @ Q, Hc.H(), atol=1e-13 * scale * n)
+
+
 def test_hessenberg_complex_not_skew(skewgpu):
     A = skewh_random(8, 1)
     A[0, 0] += 0.5  # a real diagonal part: not skew-Hermitian
