@@ -30,6 +30,15 @@
 // (M is skew): X reads the upper entries as -M^T, the update writes no mirror, and
 // one pass at the end fills the upper triangle.  That halves the gradient's live
 // set, so that two CTAs per SM on n = 256 matrices keep it in L2.
+//
+// Zero structure.  T^{-1} is nonzero only where row and column differ in parity,
+// and below the diagonal only at (odd row, even column).  With r0 the first row of
+// the current block, the rows and columns above r0 are untouched except through
+// the updates of the blocks already applied, and by induction over the blocks the
+// odd columns j < r0 of M stay zero in every row >= r0 (so the odd rows i < r0 are
+// zero in every column >= r0).  Hence X_i = 0 for odd i < r0 and the update leaves
+// the odd columns j < r0 unchanged (its term there is V_i . Z'_j with Z'_j = 0).
+// Skipping both is exact and cuts the gradient from n^3 to 5/6 n^3 FMAs.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -486,19 +495,23 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
       }
       __syncthreads();
     }
-    // 3. X = G[:, r0:n] V  (n x GNB), lanes = rows, (strip, chunk) items
+    // 3. X = G[:, r0:n] V  (n x GNB), lanes = rows, (strip, chunk) items.  Only the
+    //    rows >= r0 and the even rows above r0 are computed (the odd ones are zero):
+    //    virtual row t is row r0 + t for t < m and row 2 (t - m) after that.
+    const int nvr = m + ((r0 + 1) >> 1);
     {
-      const int S = (n + 31) >> 5;
+      const int S = (nvr + 31) >> 5;
       const int C = S >= NW ? 1 : NW / S;
       const int chunk = (m + C - 1) / C;
       for (int item = w; item < S * C; item += NW) {
         const int si = item / C, ci = item - si * C;
-        const int i = si * 32 + lane;
+        const int t = si * 32 + lane;
+        const int i = t < m ? r0 + t : 2 * (t - m);
         const int cb = r0 + ci * chunk, ce = min(n, cb + chunk);
         double acc[GNB];
 #pragma unroll
         for (int l = 0; l < GNB; l++) acc[l] = 0.0;
-        if (i < n) {
+        if (t < nvr) {
           for (int j = cb; j < ce; j++) {
             // G[i, j] from the lower triangle: G[j, i] negated above the diagonal
             // (strided reads that hit L2: a load feeds GNB FMAs on the FP64 pipe)
@@ -516,14 +529,19 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
           }
         }
       }
+      for (int idx = tid; idx < (r0 >> 1) * GNB; idx += NT) {  // the odd rows above r0
+        const int i = 2 * (idx / GNB) + 1, l = idx % GNB;
+        Zs[i * GNB + l] = 0.0;
+      }
       __syncthreads();
       if (C > 1) {
-        for (int idx = tid; idx < n * GNB; idx += NT) {
-          const int i = idx / GNB, l = idx - i * GNB;
-          const int si = i >> 5, ln = i & 31;
+        for (int idx = tid; idx < nvr * GNB; idx += NT) {
+          const int t = idx / GNB, l = idx - t * GNB;
+          const int i = t < m ? r0 + t : 2 * (t - m);
+          const int si = t >> 5, ln = t & 31;
           double x = 0.0;
           for (int c = 0; c < C; c++) x += Xp[((si * C + c) * 32 + ln) * GNB + l];
-          Zs[idx] = x;
+          Zs[i * GNB + l] = x;
         }
         __syncthreads();
       }
@@ -569,8 +587,10 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
       }
       __syncthreads();
     }
-    // 5. Z' = X T^T + V Ch  (only rows of V get the V Ch term)
-    for (int i = tid; i < n; i += NT) {
+    // 5. Z' = X T^T + V Ch  (only rows of V get the V Ch term; the odd rows above r0
+    //    stay zero)
+    for (int t = tid; t < nvr; t += NT) {
+      const int i = t < m ? r0 + t : 2 * (t - m);
       double x[GNB], z[GNB];
 #pragma unroll
       for (int l = 0; l < GNB; l++) x[l] = Zs[i * GNB + l];
@@ -598,50 +618,66 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
     }
     __syncthreads();
     // 6. G[i,j] += V_i . Z'_j - Z'_i . V_j for i >= r0, j < i (lower triangle only).
-    //    Items: (row strip of 32, column block of 32) on or below the diagonal.
-    //    Strip si holds rows [n - 32(si+1), n - 32 si) and the columns before its
-    //    last row.  Aligned to the last row, the partial strip is the one next to
-    //    r0, which has the fewest columns: a warp instruction costs the FP64 pipe
-    //    the same with idle lanes, so they belong in the shortest strip.
+    //    Items: (row strip of 32, column block) on or below the diagonal.  Strip si
+    //    holds rows [n - 32(si+1), n - 32 si); its columns are the even ones below r0
+    //    (the odd ones do not change), in blocks of 32, then [r0, last row) in blocks
+    //    of 32.  Aligned to the last row, the partial strip is the one next to r0,
+    //    which has the fewest columns: a warp instruction costs the FP64 pipe the same
+    //    with idle lanes, so they belong in the shortest strip.
     {
       const int S = (m + 31) >> 5;
+      const int nec = (r0 + 1) >> 1;  // even columns below r0
+      const int eb = (nec + 31) >> 5;
       int total = 0;
-      for (int si = 0; si < S; si++) total += (n - 32 * si - 1 + 31) / 32;
+      for (int si = 0; si < S; si++) total += eb + (n - 32 * si - 1 - r0 + 31) / 32;
       for (int item = w; item < total; item += NW) {
         int si = 0, rem = item;
         for (;;) {
-          const int nbk = (n - 32 * si - 1 + 31) / 32;
+          const int nbk = eb + (n - 32 * si - 1 - r0 + 31) / 32;
           if (rem < nbk) break;
           rem -= nbk;
           si++;
         }
         const int i = n - 32 * (si + 1) + lane;  // below r0 in the partial strip: idle
-        const int jb = rem * 32;
-        const int je = min(jb + 32, n - 32 * si - 1);
         if (i >= r0) {
-          double vi[GNB], zi[GNB];
+          double vi[GNB];
 #pragma unroll
-          for (int l = 0; l < GNB; l++) {
-            vi[l] = Vs[(i - r0) * GNB + l];
-            zi[l] = Zs[i * GNB + l];
-          }
-          for (int j = jb; j < je && j < i; j++) {
-            const double* zj = Zs + j * GNB;
-            double a0 = G.at(i, j), a1 = 0.0;
+          for (int l = 0; l < GNB; l++) vi[l] = Vs[(i - r0) * GNB + l];
+          if (rem < eb) {  // even columns j < r0: V_j = 0, only V_i . Z'_j
+            const int qe = min(32 * rem + 32, nec);
+            for (int q = 32 * rem; q < qe; q++) {
+              const int j = 2 * q;
+              const double* zj = Zs + j * GNB;
+              double a0 = G.at(i, j), a1 = 0.0;
 #pragma unroll
-            for (int l = 0; l < GNB; l += 2) {
-              a0 = fma(vi[l], zj[l], a0);
-              a1 = fma(vi[l + 1], zj[l + 1], a1);
+              for (int l = 0; l < GNB; l += 2) {
+                a0 = fma(vi[l], zj[l], a0);
+                a1 = fma(vi[l + 1], zj[l + 1], a1);
+              }
+              G.at(i, j) = a0 + a1;
             }
-            if (j >= r0) {
+          } else {
+            double zi[GNB];
+#pragma unroll
+            for (int l = 0; l < GNB; l++) zi[l] = Zs[i * GNB + l];
+            const int jb = r0 + 32 * (rem - eb);
+            const int je = min(jb + 32, n - 32 * si - 1);
+            for (int j = jb; j < je && j < i; j++) {
+              const double* zj = Zs + j * GNB;
               const double* vj = Vs + (j - r0) * GNB;
+              double a0 = G.at(i, j), a1 = 0.0;
+#pragma unroll
+              for (int l = 0; l < GNB; l += 2) {
+                a0 = fma(vi[l], zj[l], a0);
+                a1 = fma(vi[l + 1], zj[l + 1], a1);
+              }
 #pragma unroll
               for (int l = 0; l < GNB; l += 2) {
                 a0 = fma(neg(zi[l]), vj[l], a0);
                 a1 = fma(neg(zi[l + 1]), vj[l + 1], a1);
               }
+              G.at(i, j) = a0 + a1;
             }
-            G.at(i, j) = a0 + a1;
           }
         }
       }
