@@ -78,9 +78,12 @@ struct Smem {
   int nmax;
 };
 
+// Forward view: vb0, vb1, p (nmax each), then row-product partials (up to
+// (nw + strips - 1) x 32).  Gradient view: V and Z (GNB x nmax each), then the
+// partials of X = G V (2 nw slots of 32 x GNB).
 __host__ __device__ inline int union_doubles(int nmax, int nw) {
   const int f = (3 + nw) * nmax;
-  const int g = 2 * GNB * nmax + nw * 32 * GNB;
+  const int g = 2 * GNB * nmax + 2 * nw * 32 * GNB;
   return f > g ? f : g;
 }
 __host__ __device__ inline int fixed_doubles(int nmax) { return 2 * nmax + 64 + 4 * GNB * GNB; }
@@ -267,48 +270,76 @@ __device__ void lookahead_warp(const MW& W, int n, int k, const double* v, const
   }
 }
 
-// p_i = tau * sum_{j >= c0} W[i,j] v_j for i >= r0.  Lanes are rows; warps take
-// (row strip, column chunk) items so that every warp has work when the block is
-// small.  Ends with p visible to the whole block.
+// Row products over S strips of 32 rows (lanes = rows) and mc columns.  When the
+// strips do not divide evenly over the NW warps, the (strip, column) units, strip
+// by strip, are cut into NW equal runs, one per warp: a run covers a piece of one
+// or more strips, and piece (warp w, strip si) writes its partial sums to slot
+// w + si, which no other piece uses (the runs are ordered), so at most NW + S - 1
+// slots.  The partials of a row are then added in warp order.
+struct StripSplit {
+  int U;   // units per warp (0: whole strips, round robin)
+  int mc;  // columns per strip
+  __device__ __forceinline__ int first_warp(int si) const { return (si * mc) / U; }
+  __device__ __forceinline__ int last_warp(int si) const { return ((si + 1) * mc - 1) / U; }
+};
+
+template <int NW>
+__device__ __forceinline__ StripSplit strip_split(int S, int mc, int max_slots) {
+  StripSplit sp;
+  sp.mc = mc;
+  sp.U = (S % NW == 0 || NW + S - 1 > max_slots) ? 0 : (S * mc + NW - 1) / NW;
+  return sp;
+}
+
+// Dot of row i of W with v over columns [cb, ce), four loads in flight.
+template <class MW>
+__device__ __forceinline__ double row_dot(const MW& W, int i, int cb, int ce, const double* v) {
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  int j = cb;
+  for (; j + 3 < ce; j += 4) {
+    const double w0 = W.at(i, j), w1 = W.at(i, j + 1), w2 = W.at(i, j + 2), w3 = W.at(i, j + 3);
+    a0 = fma(w0, v[j], a0);
+    a1 = fma(w1, v[j + 1], a1);
+    a2 = fma(w2, v[j + 2], a2);
+    a3 = fma(w3, v[j + 3], a3);
+  }
+  for (; j < ce; j++) a0 = fma(W.at(i, j), v[j], a0);
+  return (a0 + a1) + (a2 + a3);
+}
+
+// p_i = tau * sum_{j >= c0} W[i,j] v_j for i >= r0.  Lanes are rows; whole strips per
+// warp when they divide evenly, else the balanced split above.  Ends with p visible
+// to the whole block.
 template <int NT, class MW>
 __device__ void rowprod(const MW& W, int n, int r0, int c0, const double* v, double tau, const Smem& s) {
   constexpr int NW = NT / 32;
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int mr = n - r0, mc = n - c0;
   const int S = (mr + 31) >> 5;
-  const int C = S >= NW ? 1 : NW / S;
-  const int chunk = (mc + C - 1) / C;
-  for (int item = w; item < S * C; item += NW) {
-    const int si = item / C, ci = item - si * C;
-    const int i = r0 + si * 32 + lane;
-    const int cb = c0 + ci * chunk, ce = min(n, cb + chunk);
-    if (i < n) {
-      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-      int j = cb;
-      for (; j + 3 < ce; j += 4) {
-        const double w0 = W.at(i, j), w1 = W.at(i, j + 1), w2 = W.at(i, j + 2), w3 = W.at(i, j + 3);
-        a0 = fma(w0, v[j], a0);
-        a1 = fma(w1, v[j + 1], a1);
-        a2 = fma(w2, v[j + 2], a2);
-        a3 = fma(w3, v[j + 3], a3);
-      }
-      for (; j < ce; j++) a0 = fma(W.at(i, j), v[j], a0);
-      const double y = (a0 + a1) + (a2 + a3);
-      if (C == 1)
-        s.p[i] = tau * y;
-      else
-        s.ypart[ci * s.nmax + i] = y;
-    }
-  }
-  __syncthreads();
-  if (C > 1) {
-    for (int i = r0 + (int)threadIdx.x; i < n; i += NT) {
-      double y = s.ypart[i];
-      for (int c = 1; c < C; c++) y += s.ypart[c * s.nmax + i];
-      s.p[i] = tau * y;
+  const StripSplit sp = strip_split<NW>(S, mc, 1 << 30);
+  if (sp.U == 0) {
+    for (int si = w; si < S; si += NW) {
+      const int i = r0 + si * 32 + lane;
+      if (i < n) s.p[i] = tau * row_dot(W, i, c0, n, v);
     }
     __syncthreads();
+    return;
   }
+  const int u1 = min(S * mc, (w + 1) * sp.U);
+  for (int u = w * sp.U; u < u1;) {
+    const int si = u / mc;
+    const int i = r0 + si * 32 + lane;
+    if (i < n) s.ypart[(w + si) * 32 + lane] = row_dot(W, i, c0 + (u - si * mc), c0 + min(mc, u1 - si * mc), v);
+    u = (si + 1) * mc;
+  }
+  __syncthreads();
+  for (int i = r0 + (int)threadIdx.x; i < n; i += NT) {
+    const int t = i - r0, si = t >> 5, ln = t & 31;
+    double y = 0.0;
+    for (int ww = sp.first_warp(si); ww <= sp.last_warp(si); ww++) y += s.ypart[(ww + si) * 32 + ln];
+    s.p[i] = tau * y;
+  }
+  __syncthreads();
 }
 
 // Rank-2 skew update of the lower triangle {jstart <= j < i <= n-1}, mirrored.
@@ -498,35 +529,47 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
     // 3. X = G[:, r0:n] V  (n x GNB), lanes = rows, (strip, chunk) items.  Only the
     //    rows >= r0 and the even rows above r0 are computed (the odd ones are zero):
     //    virtual row t is row r0 + t for t < m and row 2 (t - m) after that.
+    //    Strips are split over the warps as in rowprod (partials: 2 NW slots).
     const int nvr = m + ((r0 + 1) >> 1);
     {
       const int S = (nvr + 31) >> 5;
-      const int C = S >= NW ? 1 : NW / S;
-      const int chunk = (m + C - 1) / C;
-      for (int item = w; item < S * C; item += NW) {
-        const int si = item / C, ci = item - si * C;
-        const int t = si * 32 + lane;
-        const int i = t < m ? r0 + t : 2 * (t - m);
-        const int cb = r0 + ci * chunk, ce = min(n, cb + chunk);
-        double acc[GNB];
+      const StripSplit sp = strip_split<NW>(S, m, 2 * NW);
+      // X row i over columns [cb, ce): G[i, j] from the lower triangle, G[j, i] negated
+      // above the diagonal (strided reads that hit L2: a load feeds GNB FMAs)
+      auto xrow = [&](int i, int cb, int ce, double* acc) {
 #pragma unroll
         for (int l = 0; l < GNB; l++) acc[l] = 0.0;
-        if (t < nvr) {
-          for (int j = cb; j < ce; j++) {
-            // G[i, j] from the lower triangle: G[j, i] negated above the diagonal
-            // (strided reads that hit L2: a load feeds GNB FMAs on the FP64 pipe)
-            const double g = (j < i) ? G.at(i, j) : ((j > i) ? neg(G.at(j, i)) : 0.0);
-            const double* vj = Vs + (j - r0) * GNB;
+        for (int j = cb; j < ce; j++) {
+          const double g = (j < i) ? G.at(i, j) : ((j > i) ? neg(G.at(j, i)) : 0.0);
+          const double* vj = Vs + (j - r0) * GNB;
 #pragma unroll
-            for (int l = 0; l < GNB; l++) acc[l] = fma(g, vj[l], acc[l]);
-          }
-          if (C == 1) {
+          for (int l = 0; l < GNB; l++) acc[l] = fma(g, vj[l], acc[l]);
+        }
+      };
+      if (sp.U == 0) {
+        for (int si = w; si < S; si += NW) {
+          const int t = si * 32 + lane;
+          if (t < nvr) {
+            const int i = t < m ? r0 + t : 2 * (t - m);
+            double acc[GNB];
+            xrow(i, r0, n, acc);
 #pragma unroll
             for (int l = 0; l < GNB; l++) Zs[i * GNB + l] = acc[l];
-          } else {
-#pragma unroll
-            for (int l = 0; l < GNB; l++) Xp[(item * 32 + lane) * GNB + l] = acc[l];
           }
+        }
+      } else {
+        const int u1 = min(S * m, (w + 1) * sp.U);
+        for (int u = w * sp.U; u < u1;) {
+          const int si = u / m;
+          const int t = si * 32 + lane;
+          if (t < nvr) {
+            const int i = t < m ? r0 + t : 2 * (t - m);
+            double acc[GNB];
+            xrow(i, r0 + (u - si * m), r0 + min(m, u1 - si * m), acc);
+#pragma unroll
+            for (int l = 0; l < GNB; l++) Xp[((w + si) * 32 + lane) * GNB + l] = acc[l];
+          }
+          u = (si + 1) * m;
         }
       }
       for (int idx = tid; idx < (r0 >> 1) * GNB; idx += NT) {  // the odd rows above r0
@@ -534,13 +577,13 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
         Zs[i * GNB + l] = 0.0;
       }
       __syncthreads();
-      if (C > 1) {
+      if (sp.U != 0) {
         for (int idx = tid; idx < nvr * GNB; idx += NT) {
           const int t = idx / GNB, l = idx - t * GNB;
           const int i = t < m ? r0 + t : 2 * (t - m);
           const int si = t >> 5, ln = t & 31;
           double x = 0.0;
-          for (int c = 0; c < C; c++) x += Xp[((si * C + c) * 32 + ln) * GNB + l];
+          for (int ww = sp.first_warp(si); ww <= sp.last_warp(si); ww++) x += Xp[((ww + si) * 32 + ln) * GNB + l];
           Zs[i * GNB + l] = x;
         }
         __syncthreads();
