@@ -661,32 +661,64 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
     }
     __syncthreads();
     // 6. G[i,j] += V_i . Z'_j - Z'_i . V_j for i >= r0, j < i (lower triangle only).
-    //    Items: (row strip of 32, column block) on or below the diagonal.  Strip si
-    //    holds rows [n - 32(si+1), n - 32 si); its columns are the even ones below r0
-    //    (the odd ones do not change), in blocks of 32, then [r0, last row) in blocks
-    //    of 32.  Aligned to the last row, the partial strip is the one next to r0,
-    //    which has the fewest columns: a warp instruction costs the FP64 pipe the same
-    //    with idle lanes, so they belong in the shortest strip.
+    //    Row strips of 32, strip si holding rows [ib, ib + 32), ib = n - 32(si+1)
+    //    (aligned to the last row, the partial strip is the one next to r0, which
+    //    has the fewest columns).  Items of a strip: the even columns below r0 in
+    //    blocks of 32 (the odd ones do not change; V_j = 0 there, so only V_i . Z'_j),
+    //    the columns [r0, ib) in blocks of 32 ending at ib (below every row of the
+    //    strip: no per-lane bound), and the diagonal triangle.  A warp instruction
+    //    costs the FP64 pipe the same with idle lanes, so the triangle (31 steps at
+    //    half the lanes row by row) runs as a 16 x 16 square, two 8 x 8 squares and
+    //    four 8-row triangles: 8 + 4 + 7 steps.
     {
       const int S = (m + 31) >> 5;
       const int nec = (r0 + 1) >> 1;  // even columns below r0
       const int eb = (nec + 31) >> 5;
+      auto nfull = [&](int si) {
+        const int ib = n - 32 * (si + 1);
+        return ib > r0 ? (ib - r0 + 31) >> 5 : 0;
+      };
+      // G[i, j] += V_i . Z'_j - Z'_i . V_j (j >= r0)
+      auto elem = [&](int i, int j, const double* vi, const double* zi) {
+        const double* zj = Zs + j * GNB;
+        const double* vj = Vs + (j - r0) * GNB;
+        double a0 = G.at(i, j), a1 = 0.0;
+#pragma unroll
+        for (int l = 0; l < GNB; l += 2) {
+          a0 = fma(vi[l], zj[l], a0);
+          a1 = fma(vi[l + 1], zj[l + 1], a1);
+        }
+#pragma unroll
+        for (int l = 0; l < GNB; l += 2) {
+          a0 = fma(neg(zi[l]), vj[l], a0);
+          a1 = fma(neg(zi[l + 1]), vj[l + 1], a1);
+        }
+        G.at(i, j) = a0 + a1;
+      };
+      auto load_row = [&](int i, double* vi, double* zi) {
+#pragma unroll
+        for (int l = 0; l < GNB; l++) {
+          vi[l] = Vs[(i - r0) * GNB + l];
+          zi[l] = Zs[i * GNB + l];
+        }
+      };
       int total = 0;
-      for (int si = 0; si < S; si++) total += eb + (n - 32 * si - 1 - r0 + 31) / 32;
+      for (int si = 0; si < S; si++) total += eb + nfull(si) + 1;
       for (int item = w; item < total; item += NW) {
         int si = 0, rem = item;
         for (;;) {
-          const int nbk = eb + (n - 32 * si - 1 - r0 + 31) / 32;
+          const int nbk = eb + nfull(si) + 1;
           if (rem < nbk) break;
           rem -= nbk;
           si++;
         }
-        const int i = n - 32 * (si + 1) + lane;  // below r0 in the partial strip: idle
-        if (i >= r0) {
-          double vi[GNB];
+        const int ib = n - 32 * (si + 1);
+        double vi[GNB], zi[GNB];
+        if (rem < eb) {  // even columns j < r0
+          const int i = ib + lane;  // below r0 in the partial strip: idle
+          if (i >= r0) {
 #pragma unroll
-          for (int l = 0; l < GNB; l++) vi[l] = Vs[(i - r0) * GNB + l];
-          if (rem < eb) {  // even columns j < r0: V_j = 0, only V_i . Z'_j
+            for (int l = 0; l < GNB; l++) vi[l] = Vs[(i - r0) * GNB + l];
             const int qe = min(32 * rem + 32, nec);
             for (int q = 32 * rem; q < qe; q++) {
               const int j = 2 * q;
@@ -699,28 +731,37 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
               }
               G.at(i, j) = a0 + a1;
             }
-          } else {
-            double zi[GNB];
-#pragma unroll
-            for (int l = 0; l < GNB; l++) zi[l] = Zs[i * GNB + l];
-            const int jb = r0 + 32 * (rem - eb);
-            const int je = min(jb + 32, n - 32 * si - 1);
-            for (int j = jb; j < je && j < i; j++) {
-              const double* zj = Zs + j * GNB;
-              const double* vj = Vs + (j - r0) * GNB;
-              double a0 = G.at(i, j), a1 = 0.0;
-#pragma unroll
-              for (int l = 0; l < GNB; l += 2) {
-                a0 = fma(vi[l], zj[l], a0);
-                a1 = fma(vi[l + 1], zj[l + 1], a1);
-              }
-#pragma unroll
-              for (int l = 0; l < GNB; l += 2) {
-                a0 = fma(neg(zi[l]), vj[l], a0);
-                a1 = fma(neg(zi[l + 1]), vj[l + 1], a1);
-              }
-              G.at(i, j) = a0 + a1;
-            }
+          }
+        } else if (rem < eb + nfull(si)) {  // columns [jb, je) below the strip (ib > r0)
+          const int je = ib - 32 * (rem - eb), jb = max(r0, je - 32);
+          const int i = ib + lane;
+          load_row(i, vi, zi);
+          for (int j = jb; j < je; j++) elem(i, j, vi, zi);
+        } else if (ib >= r0) {  // the diagonal triangle of rows and columns [ib, ib + 32)
+          {  // rows 16..31 x columns 0..15: two lanes per row, 8 columns each
+            const int i = ib + 16 + (lane & 15), j0 = ib + ((lane >> 4) << 3);
+            load_row(i, vi, zi);
+#pragma unroll 1
+            for (int q = 0; q < 8; q++) elem(i, j0 + q, vi, zi);
+          }
+          {  // rows 8..15 x columns 0..7 and rows 24..31 x columns 16..23: 4 columns each
+            const int k = lane & 15, h = lane >> 4;
+            const int i = ib + 16 * h + 8 + (k & 7), j0 = ib + 16 * h + ((k >> 3) << 2);
+            load_row(i, vi, zi);
+#pragma unroll 1
+            for (int q = 0; q < 4; q++) elem(i, j0 + q, vi, zi);
+          }
+          {  // the four 8-row triangles on the diagonal
+            const int t = lane >> 3, r = lane & 7;
+            const int i = ib + 8 * t + r, j0 = ib + 8 * t;
+            load_row(i, vi, zi);
+            for (int q = 0; q < r; q++) elem(i, j0 + q, vi, zi);
+          }
+        } else {  // the partial strip: rows [r0, ib + 32), columns [r0, row)
+          const int i = ib + lane;
+          if (i >= r0) {
+            load_row(i, vi, zi);
+            for (int j = r0; j < i; j++) elem(i, j, vi, zi);
           }
         }
       }
