@@ -201,6 +201,56 @@ def cpu_reference(sizes_all, steps, warmup, sample, nthreads, rank):
     return len(sizes) / float(np.mean(times)), out, float(np.mean(times))
 
 
+def _lapack_share(job):
+    """One worker process: LAPACK through scipy's OpenBLAS (one thread) on its share of
+    the workload's sizes, entries of the same distribution: dsytrd (Householder
+    tridiagonalisation, the same 4/3 n^3 as the skew reduction; LAPACK has no skew
+    routine) and dgetrf + dgetri (the inverse that gives the gradient, 2 n^3).
+    Returns the seconds spent in the LAPACK calls."""
+    sizes, seed = job
+    from scipy.linalg import lapack
+
+    rng = np.random.default_rng(seed)
+    mats = []
+    for n in sizes:
+        B = rng.standard_normal((int(n), int(n))) / np.sqrt(n)
+        mats.append(np.asfortranarray((B - B.T) / 2))
+    t0 = time.perf_counter()
+    for A in mats:
+        lapack.dsytrd(A, lower=1)
+        lu, piv, _ = lapack.dgetrf(A)
+        lapack.dgetri(lu, piv)
+    return time.perf_counter() - t0
+
+
+def lapack_context(sizes, procs):
+    """BLAS-backed CPU context for the headline: the same sizes through LAPACK, one
+    single-threaded process per core (spawned), matrices dealt round robin; one
+    untimed pass (imports, page faults), then one timed pass.  Matrices/s over the
+    slowest process."""
+    import multiprocessing as mp
+
+    saved = {k: os.environ.get(k) for k in ("OPENBLAS_NUM_THREADS", "OMP_NUM_THREADS")}
+    os.environ["OPENBLAS_NUM_THREADS"] = "1"  # inherited by the spawned workers
+    os.environ["OMP_NUM_THREADS"] = "1"
+    try:
+        with mp.get_context("spawn").Pool(procs) as pool:
+            shares = [sizes[i::procs] for i in range(procs)]
+            pool.map(_lapack_share, [(sh, 100 + i) for i, sh in enumerate(shares)])
+            secs = pool.map(_lapack_share, [(sh, 200 + i) for i, sh in enumerate(shares)])
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+    return {"value": len(sizes) / max(secs), "unit": UNIT, "cores": procs,
+            "calls": "per matrix: dsytrd + dgetrf + dgetri (scipy's OpenBLAS, one thread per process)",
+            "sample": f"all {len(sizes)} matrices of the workload's sizes, entries of the same distribution",
+            "note": "context only: LAPACK's symmetric tridiagonalisation has the skew reduction's cost; "
+                    "the inverse gives the gradient"}
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -440,6 +490,10 @@ def main():
                "sample": f"first {args.cpu_sample} of the {count} matrices of the workload, one pass; oracle FP64 "
                          "restatement of logabspfaffian + FP64 Gauss-Jordan gradient, OpenMP over matrices, "
                          "scalar C++ -O3 without BLAS"}
+        try:
+            cpu["lapack_context"] = lapack_context(sizes, nthreads)
+        except Exception as e:  # scipy missing: the context is optional
+            cpu["lapack_context"] = {"unavailable": f"{type(e).__name__}: {e}"}
         k = args.cpu_sample
         glp = logpf[:k].cpu().numpy()
         gsg = sign[:k].cpu().numpy()

@@ -9,10 +9,13 @@
 // is the unblocked two-sided update of the batched kernel, spread over the
 // cluster:
 //   a. every CTA forms the partial row products of its own columns,
-//      P_r[i] = sum_{own j > k} W[i,j] v_j;
+//      P_r[i] = sum_{own j > k} W[i,j] v_j, and stores each into the shared memory
+//      of the CTA that owns row i's slice (the m active rows cut into 16 slices);
 //   b. cluster barrier;
-//   c. every CTA sums the 16 partials itself, by the same pairwise tree, so all
-//      CTAs hold the same p = tau_k sum_r P_r bit for bit;
+//   c. each CTA sums the 16 partials of its slice by a fixed pairwise tree,
+//      p_i = tau_k sum_r P_r[i], and stores p_i into every CTA; cluster barrier.
+//      Every row is summed once, so all CTAs hold the same p bit for bit, and each
+//      CTA moves 2 m values instead of reading 16 m;
 //   d. the CTA owning column k+1 updates that column with warp 0 and builds
 //      reflector k+1 from it (look-ahead), while every other warp of the
 //      cluster applies W += v p^T - p v^T to its own columns j > k+1;
@@ -51,10 +54,14 @@ struct ClusterParams {
   int* info;
 };
 
-// shared memory of one CTA, in doubles: own columns, then the vectors
+// rows per slice of the partial-product exchange (the m <= n - 1 active rows in CL slices)
+__host__ __device__ inline int cluster_slice_max(int n) { return (n + CL - 1) / CL; }
+
+// shared memory of one CTA, in doubles: own columns, then the vectors and the
+// receive buffer of the partial row products (CL x slice)
 __host__ __device__ inline size_t cluster_smem_doubles(int n) {
   const int nq = (n + CL - 1) / CL;
-  return (size_t)nq * n + 5 * (size_t)n + CL_NT + 64 + 8;
+  return (size_t)nq * n + 3 * (size_t)n + (size_t)CL * cluster_slice_max(n) + CL_NT + 64 + 8;
 }
 
 // The reflector of a column held by this CTA (col: its n entries), computed by
@@ -108,8 +115,9 @@ __global__ void __launch_bounds__(CL_NT, 1) cluster_hess_kernel(ClusterParams P)
   double* v = Wl + (size_t)nq * n;     // current reflector v_k
   double* p = v + n;                   // tau_k W v_k
   double* vnext = p + n;               // reflector built here (owner of its column)
-  double* Pp = vnext + n;              // [2][n] partial row products, by step parity
-  double* part = Pp + 2 * n;           // [CL_NT] split-column partials
+  const int smax = cluster_slice_max(n);
+  double* Pin = vnext + n;             // [CL][smax] partial row products of this CTA's slice
+  double* part = Pin + (size_t)CL * smax;  // [CL_NT] split-column partials
   double* scal = part + CL_NT + 64;    // [0] tau_k, [1] tau of the reflector built here
   const int ncl = (n - rank + CL - 1) / CL;  // own columns
 
@@ -131,8 +139,13 @@ __global__ void __launch_bounds__(CL_NT, 1) cluster_hess_kernel(ClusterParams P)
 
   for (int k = 0; k + 2 < n; k++) {
     const double tauk = scal[0];
-    double* Pk = Pp + (k & 1) * n;
     const int m = n - (k + 1);  // active rows k+1 .. n-1
+    const int L = (m + CL - 1) / CL;  // rows per slice: slice s holds rows k+1+sL ..
+    // partial of active row i (offset t = i - k - 1) into its slice owner's buffer
+    auto put_partial = [&](int t, double val) {
+      const int s = t / L;
+      cl.map_shared_rank(Pin, s)[rank * smax + (t - s * L)] = val;
+    };
     // first own column >= k+1 and >= k+2
     const int qa = (k + 1 > rank) ? (k + 1 - rank + CL - 1) / CL : 0;
     const int qb = (k + 2 > rank) ? (k + 2 - rank + CL - 1) / CL : 0;
@@ -153,7 +166,7 @@ __global__ void __launch_bounds__(CL_NT, 1) cluster_hess_kernel(ClusterParams P)
           }
           if (q < ncl) a0 = fma(Wl[(size_t)q * n + i], v[rank + CL * q], a0);
           if (cs == 1)
-            Pk[i] = (tauk != 0.0) ? a0 + a1 : 0.0;
+            put_partial(i - k - 1, (tauk != 0.0) ? a0 + a1 : 0.0);
           else
             part[c * rows_pp + ri] = a0 + a1;
         }
@@ -163,24 +176,32 @@ __global__ void __launch_bounds__(CL_NT, 1) cluster_hess_kernel(ClusterParams P)
         for (int i = k + 1 + tid; i < n; i += CL_NT) {
           double s = 0.0;
           for (int cc = 0; cc < cs; cc++) s += part[cc * rows_pp + (i - k - 1)];
-          Pk[i] = (tauk != 0.0) ? s : 0.0;
+          put_partial(i - k - 1, (tauk != 0.0) ? s : 0.0);
         }
       }
     }
     cl.sync();  // b
-    // c. p = tau_k sum_r P_r: a fixed pairwise tree (four dependent adds instead of
-    //    sixteen), the same in every CTA
-    for (int i = k + 1 + tid; i < n; i += CL_NT) {
-      double t[CL];
+    // c. this CTA's slice: p = tau_k sum_r P_r by a fixed pairwise tree (four
+    //    dependent adds instead of sixteen), then p_i into every CTA
+    {
+      const int t0 = rank * L, nl = max(0, min(m, t0 + L) - t0);
+      if (tid < nl) {
+        double t[CL];
 #pragma unroll
-      for (int r = 0; r < CL; r++) t[r] = cl.map_shared_rank(Pk, r)[i];
+        for (int r = 0; r < CL; r++) t[r] = Pin[r * smax + tid];
 #pragma unroll
-      for (int h = CL / 2; h >= 1; h >>= 1)
+        for (int h = CL / 2; h >= 1; h >>= 1)
 #pragma unroll
-        for (int r = 0; r < h; r++) t[r] = t[r] + t[r + h];
-      p[i] = tauk * t[0];
+          for (int r = 0; r < h; r++) t[r] = t[r] + t[r + h];
+        part[tid] = tauk * t[0];  // part is free after a
+      }
+      __syncthreads();
+      for (int e = tid; e < nl * CL; e += CL_NT) {
+        const int tt = e / CL, d = e - tt * CL;  // row of the slice, destination CTA
+        cl.map_shared_rank(p, d)[k + 1 + t0 + tt] = part[tt];
+      }
     }
-    __syncthreads();
+    cl.sync();  // c
     // d. look-ahead on column k+1 (its owner's warp 0), bulk update of own columns j >= k+2
     const int c1 = k + 1;
     const int owner = c1 % CL;
@@ -206,22 +227,32 @@ __global__ void __launch_bounds__(CL_NT, 1) cluster_hess_kernel(ClusterParams P)
         P.tau[c1] = 0.0;
       }
     } else if (tauk != 0.0 && qb < ncl) {
+      // elements e = t0, t0 + T, ... of the own block (column qb + e / m, row
+      // k + 1 + e % m), four per pass; the quotient and remainder are stepped, not
+      // divided
       const int t0 = look ? tid - 32 : tid, T = look ? CL_NT - 32 : CL_NT;
-      const int64_t total = (int64_t)(ncl - qb) * m;
-      for (int64_t e0 = t0; e0 < total; e0 += 4 * (int64_t)T) {
+      const int cols = ncl - qb;
+      const int Tq = T / m, Tr = T - Tq * m;
+      int qd = t0 / m, ir = t0 - qd * m;
+      while (qd < cols) {
         double a[4];
         int ii[4], jj[4];
         size_t at[4];
 #pragma unroll
         for (int u = 0; u < 4; u++) {
-          const int64_t e = e0 + (int64_t)u * T;
           ii[u] = -1;
-          if (e < total) {
-            const int qq = qb + (int)(e / m);
-            ii[u] = k + 1 + (int)(e - (int64_t)(qq - qb) * m);
+          if (qd < cols) {
+            const int qq = qb + qd;
+            ii[u] = k + 1 + ir;
             jj[u] = rank + CL * qq;
             at[u] = (size_t)qq * n + ii[u];
             a[u] = Wl[at[u]];
+            qd += Tq;
+            ir += Tr;
+            if (ir >= m) {
+              ir -= m;
+              qd++;
+            }
           }
         }
 #pragma unroll
