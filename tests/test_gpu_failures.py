@@ -47,7 +47,9 @@ def test_timeout_real_persistent_reduction(skewgpu, oracle):
     ev = torch.zeros(n, dtype=torch.float64, device="cuda")
     info = torch.full((1,), -1, dtype=torch.int32, device="cuda")
     work = skewgpu.to_device(A)
-    with skewgpu.tuned(wait_polls=20000, wait_skip_cta=3):
+    # n = 512 is in the cluster reduction's range (hardware cluster barriers, no
+    # polls of ours): cluster_max_n = 0 sends it to the persistent grid-wide kernel
+    with skewgpu.tuned(wait_polls=20000, wait_skip_cta=3, cluster_max_n=0):
         assert L.skew_hessenberg_d(h, _P(work), n, n, _P(tau), _P(ev), _P(info)) == 0
         torch.cuda.synchronize()
     assert int(info.item()) == SKEW_TIMEOUT
