@@ -81,6 +81,7 @@ struct skew_batch_plan_st {
   double** e_p_work = nullptr;     // work + off_w per matrix
   int* e_status = nullptr;
   unsigned* e_counter = nullptr;
+  int* e_fsel = nullptr;  // exp adjoint: per matrix, real Schur-basis (1) or complex (0) form
   // one instantiated CUDA graph per batched operation, keyed on its arguments
   struct GraphSlot {
     bool valid = false;
@@ -597,7 +598,7 @@ int skew_batch_plan_destroy(skew_batch_plan_t P) {
   if (P->d_gws) cudaFreeAsync(P->d_gws, st);
   void* eig[] = {P->e_refl, P->e_tau, P->e_evb, P->e_G, P->e_log, P->e_work, P->e_vr, P->e_vi, P->e_vals,
                  P->e_off_log, P->e_cap_log, P->e_log_len, P->e_off_w, P->e_p_refl, P->e_p_vr, P->e_p_vi,
-                 P->e_p_vals, P->e_p_scratch, P->e_p_work, P->e_status, P->e_counter};
+                 P->e_p_vals, P->e_p_scratch, P->e_p_work, P->e_status, P->e_fsel, P->e_counter};
   for (void* q : eig)
     if (q) cudaFreeAsync(q, st);
   if (P->fv_idx) cudaFreeAsync(P->fv_idx, st);
@@ -891,6 +892,7 @@ static int eigen_ws(skew_batch_plan_t P) {
   alloc((void**)&P->e_p_scratch, sizeof(double*) * 8);
   alloc((void**)&P->e_p_work, sizeof(double*) * count);
   alloc((void**)&P->e_status, sizeof(int) * count);
+  alloc((void**)&P->e_fsel, sizeof(int) * count);
   alloc((void**)&P->e_counter, sizeof(unsigned));
   if (!ok) return SKEW_NO_MEMORY;
   int64_t* d_off_sq = nullptr;
@@ -1101,6 +1103,7 @@ static int func_issue(skew_batch_plan_t P, const double* const* A, double* const
   E.out = out;
   E.cot = cot;
   E.func = func;
+  E.fsel = P->e_fsel;
   CK(launch_eigen_func(E, mode, P->h->stream));
   return finish_status(P, status);
 }
@@ -1254,6 +1257,7 @@ static int func_large(skew_handle_t h, double* A, const double* ev, int64_t n, d
   E.out = ptrs + 4;
   E.cot = (const double* const*)(ptrs + 5);
   E.func = func;
+  E.fsel = status + 1;  // in the aux tail after status (16 bytes: n, status, fsel)
   CK(launch_eigen_func(E, mode, s));
   if (info) {
     copy_status_kernel<<<1, 1, 0, s>>>(status, info);

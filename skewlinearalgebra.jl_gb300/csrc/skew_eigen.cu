@@ -23,7 +23,10 @@
 //   cis     V diag(exp(-Im lambda)) V^H (exp.jl:99-110), two real products.
 //   vjp     d<Gbar, exp(A)>/dA = Re(V (conj(Phi) o (V^H Gbar V)) V^H) with the
 //           Daleckii-Krein divided differences Phi_jk of exp on the i*mu
-//           spectrum, evaluated as exp(i(mu_j+mu_k)/2) sinc((mu_j-mu_k)/2).
+//           spectrum, evaluated as exp(i(mu_j+mu_k)/2) sinc((mu_j-mu_k)/2);
+//           computed in the real Schur basis (four real products, see below),
+//           the complex form only for matrices whose spectrum does not split
+//           into conjugate pairs cleanly.
 #include <cuda_runtime.h>
 #include <math.h>
 #include <stdint.h>
@@ -644,6 +647,8 @@ struct BOperand {
 struct BGemm {
   const int32_t* n;
   const int* status;  // matrices with SKEW_NO_CONVERGENCE are skipped
+  const int* sel;     // non-null: only matrices with sel[b] == sel_val
+  int sel_val;
   int nterms;         // C_b = sum_t s_t op(A_t,b) op(B_t,b)
   BOperand A[2], B[2];
   double s[2];
@@ -663,6 +668,7 @@ __global__ void __launch_bounds__(256) bgemm_kernel(BGemm P) {
   const int b = blockIdx.y;
   const int n = P.n[b];
   if (P.status && P.status[b] == SKEW_NO_CONVERGENCE) return;
+  if (P.sel && P.sel[b] != P.sel_val) return;
   const int nt = (n + BG_T - 1) / BG_T;
   if ((int)blockIdx.x >= nt * nt) return;
   const int i0 = (blockIdx.x % nt) * BG_T, j0 = (blockIdx.x / nt) * BG_T;
@@ -740,6 +746,7 @@ __global__ void __launch_bounds__(256) bgemm_kernel(BGemm P) {
 __global__ void func_elem_kernel(EigenBatch E, int mode) {
   const int b = blockIdx.y;
   if (E.status[b] == SKEW_NO_CONVERGENCE) return;
+  if (mode == 2 && E.fsel && E.fsel[b] != 0) return;  // real Schur-basis path
   const int n = E.n[b];
   const int64_t nn = (int64_t)n * n;
   const double* mu = E.vals[b];
@@ -806,10 +813,12 @@ static BOperand bop(const double* const* p, int add_sq, int trans) {
 
 static cudaError_t bgemm(const EigenBatch& E, int nterms, BOperand A0, BOperand B0, double s0, BOperand A1,
                          BOperand B1, double s1, double* const* C, int c_add_sq, int c_add, int c_step,
-                         cudaStream_t st) {
+                         cudaStream_t st, int sel_val = -1) {
   BGemm P;
   P.n = E.n;
   P.status = E.status;
+  P.sel = (sel_val >= 0) ? E.fsel : nullptr;
+  P.sel_val = sel_val;
   P.nterms = nterms;
   P.A[0] = A0;
   P.B[0] = B0;
@@ -884,6 +893,188 @@ cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStrea
   return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// exp adjoint in the real Schur basis
+// ---------------------------------------------------------------------------
+// The eigenvectors of a real skew matrix come in conjugate pairs.  For mu > 0 the
+// column u = (x + i y)/sqrt(2) gives the orthonormal pair (x, y) = sqrt(2) (Re u,
+// Im u) with A x = -mu y and A y = mu x; its partner conj(u) adds nothing.  A zero
+// eigenvalue's column is real up to its layout (Re u + Im u).  With Q = [x_1, y_1,
+// ..., z_1, ...], A = Q S Q^T (S: blocks mu J, J = [[0, 1], [-1, 0]], and zeros), and
+// the adjoint of the Frechet derivative of exp at A is
+//   G = Q T' Q^T,  T' = int_0^1 e^{-(1-s) S} (Q^T C Q) e^{-s S} ds,
+// block by block in closed form.  A 2 x 2 block M splits into P = aI + bJ, which
+// commutes with J, and N = cK + dL (K = diag(1, -1), L = [[0, 1], [1, 0]]), which
+// anticommutes with it; rotations pass through P and flip through N, so
+//   T'_ab = P (c1 I + s1 J) + N (c2 I + s2 J),
+// where (c, s) = sinc(delta) (cos m, sin m) for a rotation angle running linearly
+// from phi0 to phi1 (m the mean, delta half the difference): -mu_a -> -mu_b for P,
+// mu_a -> -mu_b for N.  A 1 x 2, 2 x 1 or 1 x 1 block (zero eigenvalue) takes the
+// same with mu = 0.  Four real n x n products instead of the twelve of the complex
+// form.  The spectrum splits into pairs when, with tol = 64 eps max|mu|, the
+// columns with mu > tol (two each) and |mu| <= tol (one each) number n; otherwise,
+// and for n < 4, the matrix takes the complex form.
+//
+// Workspace per matrix (pwork, 4 n^2): Q | T' (and C Q) | T (and Q T') | metadata:
+// per eigenvector column its first Q column (-1: skipped), per block its mu and
+// first Q column (negative - 1 for a single column), and the block count.
+
+constexpr int SB_NT = 256;
+
+__device__ __forceinline__ void rot_mean(double phi0, double phi1, double* c, double* s) {
+  const double d = 0.5 * (phi1 - phi0);
+  const double sc = (fabs(d) < 1e-8) ? fma(-d * d, 1.0 / 6.0, 1.0) : sin(d) / d;
+  double sn, cs;
+  sincos(0.5 * (phi0 + phi1), &sn, &cs);
+  *c = cs * sc;
+  *s = sn * sc;
+}
+
+// One CTA per matrix: the column map (block-wide scans of the widths 2 / 1 / 0).
+// colp[j] = 2 p + 1 for a pair starting at Q column p, 2 p for a single column,
+// -1 for a skipped partner.
+__global__ void __launch_bounds__(SB_NT) schur_scan_kernel(EigenBatch E) {
+  const int b = blockIdx.x;
+  const int n = E.n[b];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (E.status[b] == SKEW_NO_CONVERGENCE || n < 4) {
+    if (tid == 0) E.fsel[b] = 0;
+    return;
+  }
+  __shared__ double red[SB_NT / 32];
+  __shared__ long long wsum[SB_NT / 32];
+  const double* mu = E.vals[b];
+  const int64_t nn = (int64_t)n * n;
+  double* meta = E.pwork[b] + 3 * nn;
+  double* colp = meta;       // per eigenvector column
+  double* bmu = meta + n;    // per block
+  double* bst = meta + 2 * n;
+  double mx = 0.0;
+  for (int j = tid; j < n; j += SB_NT) mx = fmax(mx, fabs(mu[j]));
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if (lane == 0) red[w] = mx;
+  __syncthreads();
+  mx = 0.0;
+  for (int q = 0; q < SB_NT / 32; q++) mx = fmax(mx, red[q]);
+  const double tol = 64.0 * 2.220446049250313e-16 * mx;
+  long long base = 0, nblk = 0;
+  for (int j0 = 0; j0 < n; j0 += SB_NT) {
+    const int j = j0 + tid;
+    int wdt = 0;
+    if (j < n) wdt = (mu[j] > tol) ? 2 : ((mu[j] < -tol) ? 0 : 1);
+    // inclusive scan of (width, is-block) packed as width + 2^32 is-block
+    const long long v = (long long)wdt + ((long long)(wdt > 0) << 32);
+    long long incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const long long y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    __syncthreads();  // the previous chunk's wsum has been read
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    long long before = 0, total = 0;
+    for (int q = 0; q < SB_NT / 32; q++) {
+      if (q < w) before += wsum[q];
+      total += wsum[q];
+    }
+    const long long excl = before + incl - v;
+    if (j < n) {
+      const long long p = base + (excl & 0xffffffffLL), a = nblk + (excl >> 32);
+      colp[j] = (wdt == 0) ? -1.0 : (double)(2 * p + (wdt == 2 ? 1 : 0));
+      if (wdt > 0) {
+        bmu[a] = (wdt == 2) ? mu[j] : 0.0;
+        bst[a] = (double)(2 * p + (wdt == 2 ? 1 : 0));
+      }
+    }
+    base += total & 0xffffffffLL;
+    nblk += total >> 32;
+  }
+  if (tid == 0) {
+    meta[3 * n] = (double)nblk;
+    E.fsel[b] = (base == n) ? 1 : 0;
+  }
+}
+
+// Q from the eigenvectors, grid (chunks, count): a pair column j gives Q columns
+// p, p + 1 = sqrt(2) Re u_j, sqrt(2) Im u_j; a single one gives Re u_j + Im u_j.
+__global__ void schur_fill_kernel(EigenBatch E) {
+  const int b = blockIdx.y;
+  if (E.fsel[b] != 1) return;
+  const int n = E.n[b];
+  const int64_t nn = (int64_t)n * n;
+  double* Q = E.pwork[b];
+  const double* colp = Q + 3 * nn;
+  const double* Vr = E.Vr[b];
+  const double* Vi = E.Vi[b];
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < nn; k += (int64_t)gridDim.x * blockDim.x) {
+    const int j = (int)(k / n), r = (int)(k - (int64_t)j * n);
+    const double c = colp[j];
+    if (c < 0.0) continue;
+    const int64_t code = (int64_t)c, p = code >> 1;
+    const double xr = Vr[k], xi = Vi[k];
+    if (code & 1) {
+      Q[r + p * n] = 1.4142135623730951 * xr;
+      Q[r + (p + 1) * n] = 1.4142135623730951 * xi;
+    } else {
+      Q[r + p * n] = xr + xi;
+    }
+  }
+}
+
+// T' from T block by block, grid (chunks, count): one thread per block pair (a, b).
+// T in work block 2, T' into work block 1.
+__global__ void schur_map_kernel(EigenBatch E) {
+  const int bm = blockIdx.y;
+  if (E.fsel[bm] != 1) return;
+  const int n = E.n[bm];
+  const int64_t nn = (int64_t)n * n;
+  const double* meta = E.pwork[bm] + 3 * nn;
+  const double* bmu = meta + n;
+  const double* bst = meta + 2 * n;
+  const int64_t nb = (int64_t)meta[3 * n];
+  const double* T = E.pwork[bm] + 2 * nn;
+  double* Tp = E.pwork[bm] + nn;
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nb * nb; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t ia = q % nb, ib = q / nb;  // consecutive threads: consecutive block rows
+    const int64_t ca = (int64_t)bst[ia], cb = (int64_t)bst[ib];
+    const int64_t ra = ca >> 1, rb = cb >> 1;  // first row (column) of each block
+    const bool pa = ca & 1, pb = cb & 1;
+    const double ma = bmu[ia], mb = bmu[ib];
+    auto t = [&](int64_t i, int64_t j) -> double { return T[i + j * n]; };
+    auto o = [&](int64_t i, int64_t j) -> double& { return Tp[i + j * n]; };
+    if (pa && pb) {
+      const double m00 = t(ra, rb), m01 = t(ra, rb + 1), m10 = t(ra + 1, rb), m11 = t(ra + 1, rb + 1);
+      const double al = 0.5 * (m00 + m11), be = 0.5 * (m01 - m10);
+      const double ga = 0.5 * (m00 - m11), ep = 0.5 * (m01 + m10);
+      double c1, s1, c2, s2;
+      rot_mean(-ma, -mb, &c1, &s1);
+      rot_mean(ma, -mb, &c2, &s2);
+      const double A = fma(al, c1, -(be * s1)), B = fma(al, s1, be * c1);
+      const double Gm = fma(ga, c2, -(ep * s2)), Ep = fma(ga, s2, ep * c2);
+      o(ra, rb) = A + Gm;
+      o(ra, rb + 1) = B + Ep;
+      o(ra + 1, rb) = Ep - B;
+      o(ra + 1, rb + 1) = A - Gm;
+    } else if (pb) {  // single row a, pair b
+      double c1, s1;
+      rot_mean(0.0, -mb, &c1, &s1);
+      const double m0 = t(ra, rb), m1 = t(ra, rb + 1);
+      o(ra, rb) = fma(m0, c1, -(m1 * s1));
+      o(ra, rb + 1) = fma(m0, s1, m1 * c1);
+    } else if (pa) {  // pair a, single column b
+      double c1, s1;
+      rot_mean(-ma, 0.0, &c1, &s1);
+      const double m0 = t(ra, rb), m1 = t(ra + 1, rb);
+      o(ra, rb) = fma(c1, m0, s1 * m1);
+      o(ra + 1, rb) = fma(c1, m1, -(s1 * m0));
+    } else {
+      o(ra, rb) = t(ra, rb);
+    }
+  }
+}
+
 cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st) {
   if (E.count <= 0) return cudaSuccess;
   const int64_t nn = (int64_t)E.nmax * E.nmax;
@@ -909,24 +1100,41 @@ cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     return bgemm(E, 2, bop(Vi, 0, 0), bop(W, 0, 1), 1.0, bop(Vr, 0, 0), bop(W, 1, 1), -1.0, E.out, 0, 1, 2, st);
   }
-  // adjoint: Y = Cbar V, M = V^H Y, M <- conj(Phi) o M, Z = V M, G = Re(Z V^H)
   const double* const* C = E.cot;
   double* const* Wm = E.pwork;
-  if ((e = bgemm(E, 1, bop(C, 0, 0), bop(Vr, 0, 0), 1.0, bop(C, 0, 0), bop(Vr, 0, 0), 0.0, Wm, 0, 0, 1, st)))
+  // real Schur basis (matrices with fsel = 1): Q, T = Q^T (C Q), T', G = (Q T') Q^T
+  const int cx = E.fsel ? 0 : -1;  // the complex form runs for fsel = 0 (every matrix without fsel)
+  if (E.fsel) {
+    schur_scan_kernel<<<E.count, SB_NT, 0, st>>>(E);
+    schur_fill_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = bgemm(E, 1, bop(C, 0, 0), bop(W, 0, 0), 1.0, bop(C, 0, 0), bop(W, 0, 0), 0.0, Wm, 1, 0, 1, st, 1)))
+      return e;  // C Q
+    if ((e = bgemm(E, 1, bop(W, 0, 1), bop(W, 1, 0), 1.0, bop(W, 0, 1), bop(W, 1, 0), 0.0, Wm, 2, 0, 1, st, 1)))
+      return e;  // T = Q^T (C Q)
+    schur_map_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = bgemm(E, 1, bop(W, 0, 0), bop(W, 1, 0), 1.0, bop(W, 0, 0), bop(W, 1, 0), 0.0, Wm, 2, 0, 1, st, 1)))
+      return e;  // Q T'
+    if ((e = bgemm(E, 1, bop(W, 2, 0), bop(W, 0, 1), 1.0, bop(W, 2, 0), bop(W, 0, 1), 0.0, E.out, 0, 0, 1, st, 1)))
+      return e;  // G = (Q T') Q^T
+  }
+  // complex form: Y = Cbar V, M = V^H Y, M <- conj(Phi) o M, Z = V M, G = Re(Z V^H)
+  if ((e = bgemm(E, 1, bop(C, 0, 0), bop(Vr, 0, 0), 1.0, bop(C, 0, 0), bop(Vr, 0, 0), 0.0, Wm, 0, 0, 1, st, cx)))
     return e;  // Yr
-  if ((e = bgemm(E, 1, bop(C, 0, 0), bop(Vi, 0, 0), 1.0, bop(C, 0, 0), bop(Vi, 0, 0), 0.0, Wm, 1, 0, 1, st)))
+  if ((e = bgemm(E, 1, bop(C, 0, 0), bop(Vi, 0, 0), 1.0, bop(C, 0, 0), bop(Vi, 0, 0), 0.0, Wm, 1, 0, 1, st, cx)))
     return e;  // Yi
-  if ((e = bgemm(E, 2, bop(Vr, 0, 1), bop(W, 0, 0), 1.0, bop(Vi, 0, 1), bop(W, 1, 0), 1.0, Wm, 2, 0, 1, st)))
+  if ((e = bgemm(E, 2, bop(Vr, 0, 1), bop(W, 0, 0), 1.0, bop(Vi, 0, 1), bop(W, 1, 0), 1.0, Wm, 2, 0, 1, st, cx)))
     return e;  // Mr = Qr^T Yr + Qi^T Yi
-  if ((e = bgemm(E, 2, bop(Vr, 0, 1), bop(W, 1, 0), 1.0, bop(Vi, 0, 1), bop(W, 0, 0), -1.0, Wm, 3, 0, 1, st)))
+  if ((e = bgemm(E, 2, bop(Vr, 0, 1), bop(W, 1, 0), 1.0, bop(Vi, 0, 1), bop(W, 0, 0), -1.0, Wm, 3, 0, 1, st, cx)))
     return e;  // Mi = Qr^T Yi - Qi^T Yr
   func_elem_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E, 2);
   if ((e = cudaGetLastError())) return e;
-  if ((e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 2, 0), 1.0, bop(Vi, 0, 0), bop(W, 3, 0), -1.0, Wm, 0, 0, 1, st)))
+  if ((e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 2, 0), 1.0, bop(Vi, 0, 0), bop(W, 3, 0), -1.0, Wm, 0, 0, 1, st, cx)))
     return e;  // Zr = Qr Mr - Qi Mi
-  if ((e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 3, 0), 1.0, bop(Vi, 0, 0), bop(W, 2, 0), 1.0, Wm, 1, 0, 1, st)))
+  if ((e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 3, 0), 1.0, bop(Vi, 0, 0), bop(W, 2, 0), 1.0, Wm, 1, 0, 1, st, cx)))
     return e;  // Zi = Qr Mi + Qi Mr
-  return bgemm(E, 2, bop(W, 0, 0), bop(Vr, 0, 1), 1.0, bop(W, 1, 0), bop(Vi, 0, 1), 1.0, E.out, 0, 0, 1, st);
+  return bgemm(E, 2, bop(W, 0, 0), bop(Vr, 0, 1), 1.0, bop(W, 1, 0), bop(Vi, 0, 1), 1.0, E.out, 0, 0, 1, st, cx);
 }
 
 }  // namespace skew

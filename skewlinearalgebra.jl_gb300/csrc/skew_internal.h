@@ -248,6 +248,8 @@ struct EigenBatch {
   int chain_nmax;            // matrices with n > chain_nmax skip the QR chain and its vectors
                              // (their eigenpairs come from bisection and twisted vectors)
   int max_iter = 0;          // QR sweeps before SKEW_NO_CONVERGENCE (0: 30 n, skeweigen.jl:340)
+  int* fsel = nullptr;       // [count] exp adjoint: 1 real Schur-basis path, 0 complex path
+                             // (null: the complex path for every matrix)
 };
 // Eigenpairs of G skew tridiagonals of one size n (subdiagonals e_g, n apart) by
 // bisection (values descending, exact +-pairs, also into vals_out[idx[mb]]) and
