@@ -1088,10 +1088,10 @@ def exp_adjoint_flops(n):
 
 def exp_adjoint_flops_executed(n):
     """FP64 work the exp adjoint executes: reduction 4/3 n^3, back-transformation of
-    Vr and Vi 4 n^3, and the four real n x n products of the real Schur-basis
-    assembly 8 n^3 (G = Q T' Q^T with T = Q^T C Q)."""
+    the real Schur basis Q 2 n^3, and the four real n x n products of the assembly
+    8 n^3 (G = Q T' Q^T with T = Q^T C Q)."""
     n = np.asarray(n, dtype=np.float64)
-    return (4.0 / 3.0 + 4.0 + 8.0) * n ** 3
+    return (4.0 / 3.0 + 2.0 + 8.0) * n ** 3
 
 
 def leg_exp_adjoint(fp64_peak, steps, count=512):

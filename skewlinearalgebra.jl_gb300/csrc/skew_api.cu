@@ -1000,9 +1000,12 @@ static int fv_issue(skew_batch_plan_t P, const EigenBatch& E) {
   return SKEW_OK;
 }
 
+// back_q: the exp adjoint's path, which needs only the real Schur basis: Q is built in
+// the tridiagonal basis before the back-transformation, which then takes Q (n columns)
+// instead of Vr and Vi (2n) for the matrices that split into pairs.
 static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const* vals, double* const* Vr,
                      double* const* Vi, EigenBatch* Eout, const double* const* ev_in = nullptr,
-                     int chain_nmax = 1 << 30) {
+                     int chain_nmax = 1 << 30, bool back_q = false) {
   int s = eigen_ws(P);
   if (s) return s;
   cudaStream_t st = P->h->stream;
@@ -1046,6 +1049,11 @@ static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const*
   if (E.chain_nmax < P->nmax) {
     s = fv_issue(P, E);
     if (s) return s;
+  }
+  if (back_q && !ev_in) {
+    E.fsel = P->e_fsel;
+    E.back_q = 1;
+    CK(launch_schur_basis(E, st));
   }
   if (!ev_in) CK(launch_eigen_back(E, grid, P->nmax, st));
   *Eout = E;
@@ -1098,7 +1106,7 @@ static int func_issue(skew_batch_plan_t P, const double* const* A, double* const
   EigenBatch E;
   int s = fv_setup(P, func_chain_nmax(P));
   if (s) return s;
-  s = eigen_run(P, A, nullptr, nullptr, nullptr, &E, nullptr, func_chain_nmax(P));
+  s = eigen_run(P, A, nullptr, nullptr, nullptr, &E, nullptr, func_chain_nmax(P), mode == 2);
   if (s) return s;
   E.out = out;
   E.cot = cot;

@@ -552,6 +552,14 @@ __global__ void __launch_bounds__(ENT) eigen_back_kernel(EigenBatch E) {
     const double* R = E.refl[b];  // n x n, ld n
     const double* tau = E.tau + E.off_n[b];
     if (E.status[b] == SKEW_NO_CONVERGENCE || n < 3) continue;
+    // the columns to transform: Vr and Vi, or the real Schur basis Q (work block 0) alone
+    const bool qonly = E.back_q && E.fsel && E.fsel[b] == 1;
+    const int ncol = qonly ? n : 2 * n;
+    double* const Xq = E.pwork[b];
+    auto colp = [&](int col) -> double* {
+      if (qonly) return Xq + (int64_t)col * n;
+      return (col < n) ? (E.Vr[b] + (int64_t)col * ldv) : (E.Vi[b] + (int64_t)(col - n) * ldv);
+    };
     const int nref = n - 2;
     for (int kend = nref; kend > 0; kend -= EB) {
       const int k0 = max(0, kend - EB), nb = kend - k0;
@@ -595,9 +603,9 @@ __global__ void __launch_bounds__(ENT) eigen_back_kernel(EigenBatch E) {
         }
         __syncthreads();
       }
-      // Y = V^T X (EB x 2n), then Z = T Y; thread per column of X = [Vr | Vi]
-      for (int col = threadIdx.x; col < 2 * n; col += ENT) {
-        const double* x = (col < n) ? (E.Vr[b] + (int64_t)col * ldv) : (E.Vi[b] + (int64_t)(col - n) * ldv);
+      // Y = V^T X (EB x ncol), then Z = T Y; thread per column of X = [Vr | Vi] or Q
+      for (int col = threadIdx.x; col < ncol; col += ENT) {
+        const double* x = colp(col);
         double y[EB];
 #pragma unroll
         for (int l = 0; l < EB; l++) y[l] = 0.0;
@@ -616,8 +624,8 @@ __global__ void __launch_bounds__(ENT) eigen_back_kernel(EigenBatch E) {
       }
       __syncthreads();
       // X[r, col] -= sum_l V[r, l] Z[l, col] for r >= r0; lanes are rows
-      for (int col = threadIdx.x >> 5; col < 2 * n; col += ENW) {
-        double* x = (col < n) ? (E.Vr[b] + (int64_t)col * ldv) : (E.Vi[b] + (int64_t)(col - n) * ldv);
+      for (int col = threadIdx.x >> 5; col < ncol; col += ENW) {
+        double* x = colp(col);
         double z[EB];
 #pragma unroll
         for (int l = 0; l < EB; l++) z[l] = Zs[l * 2 * n + col];
@@ -1075,6 +1083,15 @@ __global__ void schur_map_kernel(EigenBatch E) {
   }
 }
 
+cudaError_t launch_schur_basis(const EigenBatch& E, cudaStream_t st) {
+  if (E.count <= 0 || !E.fsel) return cudaSuccess;
+  const int64_t nn = (int64_t)E.nmax * E.nmax;
+  const int chunks = (int)std::min<int64_t>((nn + 255) / 256, 512);
+  schur_scan_kernel<<<E.count, SB_NT, 0, st>>>(E);
+  schur_fill_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st) {
   if (E.count <= 0) return cudaSuccess;
   const int64_t nn = (int64_t)E.nmax * E.nmax;
@@ -1105,9 +1122,7 @@ cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st) {
   // real Schur basis (matrices with fsel = 1): Q, T = Q^T (C Q), T', G = (Q T') Q^T
   const int cx = E.fsel ? 0 : -1;  // the complex form runs for fsel = 0 (every matrix without fsel)
   if (E.fsel) {
-    schur_scan_kernel<<<E.count, SB_NT, 0, st>>>(E);
-    schur_fill_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E);
-    if ((e = cudaGetLastError())) return e;
+    if (!E.back_q && (e = launch_schur_basis(E, st))) return e;
     if ((e = bgemm(E, 1, bop(C, 0, 0), bop(W, 0, 0), 1.0, bop(C, 0, 0), bop(W, 0, 0), 0.0, Wm, 1, 0, 1, st, 1)))
       return e;  // C Q
     if ((e = bgemm(E, 1, bop(W, 0, 1), bop(W, 1, 0), 1.0, bop(W, 0, 1), bop(W, 1, 0), 0.0, Wm, 2, 0, 1, st, 1)))

@@ -250,6 +250,9 @@ struct EigenBatch {
   int max_iter = 0;          // QR sweeps before SKEW_NO_CONVERGENCE (0: 30 n, skeweigen.jl:340)
   int* fsel = nullptr;       // [count] exp adjoint: 1 real Schur-basis path, 0 complex path
                              // (null: the complex path for every matrix)
+  int back_q = 0;            // 1: the real Schur basis Q was built in the tridiagonal basis
+                             // (pwork block 0): the back-transformation takes Q alone for the
+                             // matrices with fsel = 1, and the adjoint starts from it
 };
 // Eigenpairs of G skew tridiagonals of one size n (subdiagonals e_g, n apart) by
 // bisection (values descending, exact +-pairs, also into vals_out[idx[mb]]) and
@@ -276,6 +279,8 @@ cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStrea
 // exp / cis / exp adjoint from (vals, Vr, Vi): elementwise kernels and tiled
 // batched products over the whole GPU (tiles of every matrix in one launch).
 cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st);
+// exp adjoint: the real Schur basis Q (and fsel) from vals, Vr, Vi into pwork
+cudaError_t launch_schur_basis(const EigenBatch& E, cudaStream_t st);
 
 // Multi-CTA blocked reduction of one large matrix (skew_blocked.cu).
 size_t blocked_ws_doubles(int n);
