@@ -544,7 +544,7 @@ def main():
                          "peak_source": "FP64 DFMA peak measured live by skew_measure_fp64_peak "
                                         "(MEASURED_PEAKS.json has no FP64 figure)",
                          "algorithmic_flops_per_step": flops, "kernel": "batch_kernel"},
-            "gpu_launches": int(args.steps * len(set(_bucket_ids(sizes)))),
+            "gpu_launches": int(args.steps * _launches_per_call(sizes)),
             "tuning": skewgpu.tuning_source(),
             "fp64_pipes_tflops": skewgpu.measure_fp64_pipes(),
             "clocks": clk,
@@ -1132,14 +1132,23 @@ def leg_exp_adjoint(fp64_peak, steps, count=512):
             "complex_part": "reported separately as exp_adjoint_complex_64x256"}
 
 
-def _bucket_ids(sizes):
+def _launches_per_call(sizes):
+    """batch_kernel launches of one batched call: one per size bucket of
+    skew_batch_plan_create (tuning key bucket_edges), the buckets whose working copies
+    live in global memory (above batch_smem_nmax) merged into one launch when
+    batch_merge_global is set."""
     import skewgpu
 
-    edges = skewgpu.tuning_get("bucket_edges")  # the size buckets of skew_batch_plan_create
-    out = []
+    edges = skewgpu.tuning_get("bucket_edges")
+    smem_nmax = skewgpu.tuning_get("batch_smem_nmax")
+    merge = skewgpu.tuning_get("batch_merge_global")
+    buckets = {next((e for e in edges if n <= e), 1 << 30): 0 for n in sizes}
     for n in sizes:
-        out.append(next((e for e in edges if n <= e), 1 << 30))
-    return out
+        e = next((e for e in edges if n <= e), 1 << 30)
+        buckets[e] = max(buckets[e], int(n))
+    smem = sum(1 for e, nmax in buckets.items() if nmax <= smem_nmax)
+    glob = len(buckets) - smem
+    return smem + (min(glob, 1) if merge else glob)
 
 
 if __name__ == "__main__":

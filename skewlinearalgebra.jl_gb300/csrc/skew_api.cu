@@ -545,6 +545,24 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
     // 16..256 workload +1.5 %).  The tuning key batch_smem_nmax moves the limit.
     B.smem_matrix = (smem_full <= 227 * 1024 && B.nmax <= T.batch_smem_nmax) ? 1 : 0;
     B.nt = bucket_threads(T, B.nmax, B.smem_matrix != 0);
+    // Consecutive global-memory buckets with the same threads per CTA run as one launch
+    // (tuning key batch_merge_global): the CTAs take matrices largest first from one
+    // counter, so the smaller sizes fill the tail of the larger ones instead of each
+    // bucket ending on a partly empty round of CTAs.  The slots keep the first (largest)
+    // size.
+    if (T.batch_merge_global && !B.smem_matrix) {
+      while (u < count) {
+        const int e2 = edge_of(P->n_host[order[u]]);
+        int64_t u2 = u;
+        while (u2 < count && edge_of(P->n_host[order[u2]]) == e2) u2++;
+        const int nm2 = std::max<int32_t>(P->n_host[order[u]], 1);
+        const size_t sf2 = batch_smem_bytes(nm2, true, bucket_threads(T, nm2, true));
+        const bool sm2 = sf2 <= 227 * 1024 && nm2 <= T.batch_smem_nmax;
+        if (sm2 || bucket_threads(T, nm2, false) != B.nt) break;
+        u = u2;
+      }
+      B.end = (int)u;
+    }
     int occ = batch_occupancy(B.nmax, B.smem_matrix != 0, B.nt);
     if (!B.smem_matrix) occ = std::max(1, std::min(occ, T.batch_global_ctas_per_sm));
     B.grid = (int)std::min<int64_t>((int64_t)h->sms * occ, u - t);

@@ -45,6 +45,7 @@ struct Tuning {
   int batch_global_nt;           // threads per CTA of global-memory buckets
   int batch_global_ctas_per_sm;  // resident CTAs per SM for global-memory buckets
   int batch_graph;               // 1: batched calls record and replay CUDA graphs
+  int batch_merge_global;        // 1: consecutive global-memory buckets run as one launch
   int func_chain_nmax;           // function paths: the QR chain up to this n, bisection above
   // one large real matrix
   int blocked_min_n;             // the blocked multi-CTA reduction from this n
