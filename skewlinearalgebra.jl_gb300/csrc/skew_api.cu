@@ -940,13 +940,13 @@ static int eigen_ws(skew_batch_plan_t P) {
 // A != null: dense matrices (reduction, QR of skewtrieigen_divided!, vectors,
 // back-transformation).  ev_in != null instead: the subdiagonals of
 // SkewHermTridiagonal matrices (skewtrieigen_merged!, no reduction, Q = I).
-// Above this size the batched function paths take bisection and twisted vectors
-// (SKEW_FUNC_CHAIN_NMAX overrides; the eigenvalue order does not matter there).
+// Above this size (the tuning key func_chain_nmax) the batched function paths take
+// bisection and twisted vectors; the eigenvalue order does not matter there.
 // The QR chain runs one matrix per thread, O(n^2) with a long dependency chain:
 // for n = 512 it takes 0.30 s on GB300, where bisection and twisted vectors take
 // a few milliseconds.  Measured on the 512-matrix exp-adjoint workload (n in
-// {32, ..., 512}): 745 ms per step with 64, 768 with 160, 813 with 256, 1013 with
-// the chain for every size.
+// {32, ..., 512}, complex form of the adjoint): 745 ms per step with 64, 768 with
+// 160, 813 with 256, 1013 with the chain for every size.
 static int func_chain_nmax(skew_batch_plan_t P) { return P->h->tune.func_chain_nmax; }
 
 // Size groups of the matrices above thr, their device index list and the workspace
