@@ -6,6 +6,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <cstdlib>
 #include <cstring>
 #include <new>
@@ -39,6 +40,7 @@ struct skew_handle_st {
 struct Bucket {
   int begin, end, nmax, smem_matrix, grid, nt;
   int64_t gws_slot;  // doubles per CTA slot (global bucket)
+  int split = 0;     // > begin: the work median of the slice (two regions, see batch_kernel)
   size_t gws_off;    // offset of the bucket's slots in the plan workspace (doubles)
 };
 
@@ -565,6 +567,23 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
     }
     int occ = batch_occupancy(B.nmax, B.smem_matrix != 0, B.nt);
     if (!B.smem_matrix) occ = std::max(1, std::min(occ, T.batch_global_ctas_per_sm));
+    // Global-memory slices with two CTAs per SM: two regions, the first holding the
+    // largest matrices with batch_split_pct % of the work (sum of n^3), see
+    // batch_kernel.  Measured on GB300 (4096 matrices, even n in [16, 256]): 71.3 ms
+    // per step at 50 % against 73.3 ms with one region, DRAM traffic 20.8 GB against
+    // 34.5 GB; taking from the two ends of one region instead cut the traffic to
+    // 14.4 GB but ended on mid-size matrices (74.1 ms).
+    if (!B.smem_matrix && T.batch_split_pct > 0 && occ >= 2 && u - t >= 2) {
+      double total = 0.0, run = 0.0;
+      for (int64_t q = t; q < u; q++) total += std::pow((double)P->n_host[order[q]], 3.0);
+      const double first = 0.01 * T.batch_split_pct * total;
+      int64_t q = t;
+      while (q < u - 1 && run + std::pow((double)P->n_host[order[q]], 3.0) <= first) {
+        run += std::pow((double)P->n_host[order[q]], 3.0);
+        q++;
+      }
+      B.split = (int)std::max<int64_t>(q, t + 1);
+    }
     B.grid = (int)std::min<int64_t>((int64_t)h->sms * occ, u - t);
     B.gws_slot = B.smem_matrix ? 0 : (int64_t)B.nmax * (B.nmax | 1);
     B.gws_off = gws_total;
@@ -578,7 +597,7 @@ int skew_batch_plan_create(skew_handle_t h, const int64_t* n, int64_t count, ske
   ok &= cudaMallocAsync(&P->d_n, sizeof(int32_t) * std::max<int64_t>(count, 1), st) == cudaSuccess;
   ok &= cudaMallocAsync(&P->d_order, sizeof(int32_t) * std::max<int64_t>(count, 1), st) == cudaSuccess;
   ok &= cudaMallocAsync(&P->d_ev_off, sizeof(int64_t) * std::max<int64_t>(count, 1), st) == cudaSuccess;
-  ok &= cudaMallocAsync(&P->d_counters, sizeof(unsigned) * std::max<size_t>(P->buckets.size(), 1), st) ==
+  ok &= cudaMallocAsync(&P->d_counters, 2 * sizeof(unsigned) * std::max<size_t>(P->buckets.size(), 1), st) ==
         cudaSuccess;
   ok &= cudaMallocAsync(&P->d_ev, sizeof(double) * std::max<int64_t>(P->ev_total, 1), st) == cudaSuccess;
   ok &= cudaMallocAsync(&P->d_fallback, sizeof(unsigned) * (2 + 2 * (size_t)std::max<int64_t>(count, 1)), st) ==
@@ -634,7 +653,7 @@ static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logp
                        double* const* refl_out = nullptr, bool host_in = false,
                        double* const* grad_host = nullptr) {
   cudaStream_t st = P->h->stream;
-  CK(cudaMemsetAsync(P->d_counters, 0, sizeof(unsigned) * std::max<size_t>(P->buckets.size(), 1), st));
+  CK(cudaMemsetAsync(P->d_counters, 0, 2 * sizeof(unsigned) * std::max<size_t>(P->buckets.size(), 1), st));
   for (size_t i = 0; i < P->buckets.size(); i++) {
     const Bucket& B = P->buckets[i];
     BatchParams bp;
@@ -649,7 +668,8 @@ static int run_buckets(skew_batch_plan_t P, const double* const* A, double* logp
     bp.check = 0;
     bp.gws = P->d_gws ? P->d_gws + B.gws_off : nullptr;
     bp.gws_slot = B.gws_slot;
-    bp.counter = P->d_counters + i;
+    bp.counter = P->d_counters + 2 * i;
+    bp.split = B.split;
     bp.logpf = logpf;
     bp.sign = sign;
     bp.grad = grad;

@@ -887,7 +887,14 @@ __device__ void run_job(const Job& J, const MW& W, bool inplace, const Smem& s) 
 // ---------------------------------------------------------------------------
 
 // Persistent batched kernel over order[begin:end) (matrices sorted largest
-// first); CTAs take the next matrix from an atomic counter.
+// first); CTAs take the next matrix from an atomic counter.  With a split, the
+// slice is two regions, [begin, split) holding the largest matrices (half the work)
+// and [split, end) the rest, each with its own counter.  The CTAs of the first half
+// of the grid start in the first region and those of the second half in the second
+// (one CTA of each per SM), both largest first; a CTA whose region is empty takes
+// from the other.  Co-resident CTAs then hold a large and a smaller working copy
+// instead of two large ones in the same phase (less L2 overflow), and the launch
+// still ends on the smallest matrices.
 // HOST: the inputs are read from, and the gradients written to, page-locked host
 // memory (a separate instantiation, so the device-resident kernels are unchanged).
 template <int NT, bool SM, bool HOST>
@@ -896,7 +903,23 @@ __global__ void __launch_bounds__(NT) batch_kernel(BatchParams P, int tridiag_on
   const int woff = smem_doubles(P.nmax, NT / 32);
   __shared__ int s_next;
   for (;;) {
-    if (threadIdx.x == 0) s_next = (int)atomicAdd(P.counter, 1u) + P.begin;
+    if (threadIdx.x == 0) {
+      if (P.split > P.begin) {
+        const int second = blockIdx.x >= (gridDim.x >> 1) ? 1 : 0;
+        int t = P.end;
+        for (int pass = 0; pass < 2; pass++) {
+          const int r = second ^ pass;  // region: 0 [begin, split), 1 [split, end)
+          const int x = (int)atomicAdd(P.counter + r, 1u) + (r ? P.split : P.begin);
+          if (x < (r ? P.end : P.split)) {
+            t = x;
+            break;
+          }
+        }
+        s_next = t;
+      } else {
+        s_next = (int)atomicAdd(P.counter, 1u) + P.begin;
+      }
+    }
     __syncthreads();
     const int t = s_next;
     __syncthreads();

@@ -46,6 +46,7 @@ struct Tuning {
   int batch_global_ctas_per_sm;  // resident CTAs per SM for global-memory buckets
   int batch_graph;               // 1: batched calls record and replay CUDA graphs
   int batch_merge_global;        // 1: consecutive global-memory buckets run as one launch
+  int batch_split_pct;           // global-memory launches: first region holds this % of the work (0: one)
   int func_chain_nmax;           // function paths: the QR chain up to this n, bisection above
   // one large real matrix
   int blocked_min_n;             // the blocked multi-CTA reduction from this n
@@ -85,7 +86,7 @@ struct BatchParams {
   int32_t check;           // verify A == -A^T
   double* gws;             // global workspace (one slot per CTA) when !smem_matrix
   int64_t gws_slot;        // doubles per slot
-  unsigned* counter;       // work counter, zero before the launch
+  unsigned* counter;       // work counter (two words, 8-byte aligned), zero before the launch
   double* logpf;           // [count] or null
   double* sign;            // [count] or null
   double* const* grad;     // [count] device pointers or null
@@ -98,6 +99,9 @@ struct BatchParams {
   int32_t host_in = 0;     // A[] point into page-locked host memory (read with more loads in flight)
   double* const* grad_host = nullptr;  // [count] page-locked host destinations: the finished
                                        // gradient is copied there by the CTA that formed it
+  int32_t split = 0;       // > begin: two regions [begin, split) and [split, end) with a
+                           // counter each (counter[0], counter[1]); the first half of the CTAs
+                           // starts in the first, the second half in the second
 };
 
 struct SingleParams {

@@ -42,6 +42,7 @@ void tuning_defaults(Tuning* T) {
   T->batch_global_ctas_per_sm = 2;
   T->batch_graph = 1;
   T->batch_merge_global = 1;
+  T->batch_split_pct = 50;
   T->func_chain_nmax = 64;
   T->blocked_min_n = 192;
   T->blocked_persistent = 1;
@@ -86,6 +87,7 @@ const Key kKeys[] = {
     {"batch_global_ctas_per_sm", &Tuning::batch_global_ctas_per_sm, 1, 4, nullptr, 0},
     {"batch_graph", &Tuning::batch_graph, 0, 1, k01, 2},
     {"batch_merge_global", &Tuning::batch_merge_global, 0, 1, k01, 2},
+    {"batch_split_pct", &Tuning::batch_split_pct, 0, 95, nullptr, 0},
     {"func_chain_nmax", &Tuning::func_chain_nmax, 0, 1 << 20, nullptr, 0},
     {"blocked_min_n", &Tuning::blocked_min_n, 16, 1025, nullptr, 0},
     {"blocked_persistent", &Tuning::blocked_persistent, 0, 1, k01, 2},

@@ -11,7 +11,7 @@ candidates with the other keys held at their current best (coordinate descent),
 on seeded synthetic workloads shaped like the benchmark configurations:
 
 * batched log|Pf| + gradient over uneven sizes (even n in [16, 256], entries of
-  (B - B^T)/2 with B ~ N(0, 1/n)): batch_merge_global, bucket_edges,
+  (B - B^T)/2 with B ~ N(0, 1/n)): batch_merge_global, batch_split_pct, bucket_edges,
   batch_smem_nmax, batch_smem_nt_small, batch_smem_nt_large, batch_global_nt,
   batch_global_ctas_per_sm;
 * single real matrices: blocked_min_n (the size from which the multi-CTA blocked
@@ -122,6 +122,7 @@ class Tuner:
                 plan.close()
 
         self.sweep("batch_merge_global", [1, 0], measure)
+        self.sweep("batch_split_pct", [0, 30, 40, 50, 60], measure)
         self.sweep("bucket_edges", [[32, 64, 96, 128, 152], [32, 64, 96, 128, 152, 192],
                                     [24, 48, 72, 96, 128, 152], [32, 64, 96, 128, 152, 192, 224],
                                     [16, 32, 48, 64, 96, 128, 152, 200]], measure)
