@@ -1144,12 +1144,13 @@ static int func_issue(skew_batch_plan_t P, const double* const* A, double* const
   EigenBatch E;
   int s = fv_setup(P, func_chain_nmax(P));
   if (s) return s;
-  s = eigen_run(P, A, nullptr, nullptr, nullptr, &E, nullptr, func_chain_nmax(P), mode == 2);
+  const bool schur = P->h->tune.func_real_schur != 0;
+  s = eigen_run(P, A, nullptr, nullptr, nullptr, &E, nullptr, func_chain_nmax(P), schur);
   if (s) return s;
   E.out = out;
   E.cot = cot;
   E.func = func;
-  E.fsel = P->e_fsel;
+  E.fsel = schur ? P->e_fsel : nullptr;
   CK(launch_eigen_func(E, mode, P->h->stream));
   return finish_status(P, status);
 }
@@ -1303,7 +1304,7 @@ static int func_large(skew_handle_t h, double* A, const double* ev, int64_t n, d
   E.out = ptrs + 4;
   E.cot = (const double* const*)(ptrs + 5);
   E.func = func;
-  E.fsel = status + 1;  // in the aux tail after status (16 bytes: n, status, fsel)
+  E.fsel = h->tune.func_real_schur ? status + 1 : nullptr;  // aux tail after status: n, status, fsel
   CK(launch_eigen_func(E, mode, s));
   if (info) {
     copy_status_kernel<<<1, 1, 0, s>>>(status, info);

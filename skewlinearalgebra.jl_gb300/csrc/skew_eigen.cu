@@ -754,7 +754,7 @@ __global__ void __launch_bounds__(256) bgemm_kernel(BGemm P) {
 __global__ void func_elem_kernel(EigenBatch E, int mode) {
   const int b = blockIdx.y;
   if (E.status[b] == SKEW_NO_CONVERGENCE) return;
-  if (mode == 2 && E.fsel && E.fsel[b] != 0) return;  // real Schur-basis path
+  if (E.fsel && E.fsel[b] != 0) return;  // real Schur-basis path
   const int n = E.n[b];
   const int64_t nn = (int64_t)n * n;
   const double* mu = E.vals[b];
@@ -919,9 +919,15 @@ cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStrea
 // from phi0 to phi1 (m the mean, delta half the difference): -mu_a -> -mu_b for P,
 // mu_a -> -mu_b for N.  A 1 x 2, 2 x 1 or 1 x 1 block (zero eigenvalue) takes the
 // same with mu = 0.  Four real n x n products instead of the twelve of the complex
-// form.  The spectrum splits into pairs when, with tol = 64 eps max|mu|, the
-// columns with mu > tol (two each) and |mu| <= tol (one each) number n; otherwise,
-// and for n < 4, the matrix takes the complex form.
+// form.  With tol = 64 eps max|mu|, the columns with mu > tol give two Q columns,
+// |mu| <= tol one and mu < -tol none.  A zero eigenvalue that a full tridiagonal
+// solve returns as a few ulps (several odd blocks, the Jacobi fallback) is then a
+// real single column, not half of a pair; its function value is f(0) (singular for
+// log, cot and coth).  If the columns do not number n (+-values that are not
+// partners), and for n < 4, the matrix takes the complex form.  The other matrix
+// functions use the same basis: for a real function f (f(conj z) = conj f(z)),
+// f(mu J) = Re f(i mu) I + Im f(i mu) J, so f(A) = (Q f(S)) Q^T is one product, and
+// cis(A) = exp(i A) = Q (cosh(mu) I + i sinh(mu) J) Q^T two.
 //
 // Workspace per matrix (pwork, 4 n^2): Q | T' (and C Q) | T (and Q T') | metadata:
 // per eigenvector column its first Q column (-1: skipped), per block its mu and
@@ -1083,6 +1089,50 @@ __global__ void schur_map_kernel(EigenBatch E) {
   }
 }
 
+// Q f(S) (mode 0: f = E.func, into work block 1) or Q cosh(S) and Q i sinh(S) (mode 1:
+// blocks 1 and 2), grid (chunks, count); one thread per (row, block).
+__global__ void schur_func_kernel(EigenBatch E, int mode) {
+  const int bm = blockIdx.y;
+  if (E.fsel[bm] != 1) return;
+  const int n = E.n[bm];
+  const int64_t nn = (int64_t)n * n;
+  const double* Q = E.pwork[bm];
+  double* P1 = E.pwork[bm] + nn;
+  double* P2 = E.pwork[bm] + 2 * nn;
+  const double* meta = Q + 3 * nn;
+  const double* bmu = meta + n;
+  const double* bst = meta + 2 * n;
+  const int64_t nb = (int64_t)meta[3 * n];
+  for (int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; q < nb * n; q += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t a = q / n, r = q - a * n;  // consecutive threads: consecutive rows
+    const int64_t code = (int64_t)bst[a], p = code >> 1;
+    const bool pair = code & 1;
+    const double mu = bmu[a];
+    const double x = Q[r + p * n];
+    const double y = pair ? Q[r + (p + 1) * n] : 0.0;
+    if (mode == 0) {  // [x, y] (a I + b J) = [a x - b y, b x + a y] with f(i mu) = a + i b
+      double fa, fb;
+      bool sing = false;
+      skew_scalar_func(E.func, mu, &fa, &fb, &sing);
+      if (sing && r == 0) E.status[bm] = SKEW_SINGULAR;
+      if (pair) {
+        P1[r + p * n] = fma(fa, x, -(fb * y));
+        P1[r + (p + 1) * n] = fma(fb, x, fa * y);
+      } else {
+        P1[r + p * n] = fa * x;
+      }
+    } else {  // cosh(mu) [x, y] and sinh(mu) [x, y] J = sinh(mu) [-y, x]
+      const double ch = cosh(mu), sh = sinh(mu);
+      P1[r + p * n] = ch * x;
+      P2[r + p * n] = -(sh * y);
+      if (pair) {
+        P1[r + (p + 1) * n] = ch * y;
+        P2[r + (p + 1) * n] = sh * x;
+      }
+    }
+  }
+}
+
 cudaError_t launch_schur_basis(const EigenBatch& E, cudaStream_t st) {
   if (E.count <= 0 || !E.fsel) return cudaSuccess;
   const int64_t nn = (int64_t)E.nmax * E.nmax;
@@ -1100,9 +1150,21 @@ cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st) {
   const double* const* Vi = E.Vi;
   const double* const* W = E.pwork;
   cudaError_t e;
+  const int cx = E.fsel ? 0 : -1;  // the complex form runs for fsel = 0 (every matrix without fsel)
+  if (E.fsel && mode != 2) {  // real Schur basis: F = (Q f(S)) Q^T, cis = Q (cosh S + i sinh(S) J) Q^T
+    if (!E.back_q && (e = launch_schur_basis(E, st))) return e;
+    schur_func_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E, mode);
+    if ((e = cudaGetLastError())) return e;
+    const int step = mode == 0 ? 1 : 2;
+    if ((e = bgemm(E, 1, bop(W, 1, 0), bop(W, 0, 1), 1.0, bop(W, 1, 0), bop(W, 0, 1), 0.0, E.out, 0, 0, step, st, 1)))
+      return e;
+    if (mode == 1 &&
+        (e = bgemm(E, 1, bop(W, 2, 0), bop(W, 0, 1), 1.0, bop(W, 2, 0), bop(W, 0, 1), 0.0, E.out, 0, 1, 2, st, 1)))
+      return e;
+  }
   if (mode == 0) {  // F = Qr P^T + Qi R^T = Re(V f V^H), then its (skew-)symmetric part
     func_elem_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E, 0);
-    e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 0, 1), 1.0, bop(Vi, 0, 0), bop(W, 1, 1), 1.0, E.out, 0, 0, 1, st);
+    e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 0, 1), 1.0, bop(Vi, 0, 0), bop(W, 1, 1), 1.0, E.out, 0, 0, 1, st, cx);
     if (e != cudaSuccess) return e;
     const int sym = skew_func_symmetry(E.func);
     if (sym != 0) {
@@ -1113,14 +1175,13 @@ cudaError_t launch_eigen_func(const EigenBatch& E, int mode, cudaStream_t st) {
   }
   if (mode == 1) {  // Re = Qr P^T + Qi R^T, Im = Qi P^T - Qr R^T, interleaved
     func_elem_kernel<<<dim3(chunks, E.count), 256, 0, st>>>(E, 1);
-    e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 0, 1), 1.0, bop(Vi, 0, 0), bop(W, 1, 1), 1.0, E.out, 0, 0, 2, st);
+    e = bgemm(E, 2, bop(Vr, 0, 0), bop(W, 0, 1), 1.0, bop(Vi, 0, 0), bop(W, 1, 1), 1.0, E.out, 0, 0, 2, st, cx);
     if (e != cudaSuccess) return e;
-    return bgemm(E, 2, bop(Vi, 0, 0), bop(W, 0, 1), 1.0, bop(Vr, 0, 0), bop(W, 1, 1), -1.0, E.out, 0, 1, 2, st);
+    return bgemm(E, 2, bop(Vi, 0, 0), bop(W, 0, 1), 1.0, bop(Vr, 0, 0), bop(W, 1, 1), -1.0, E.out, 0, 1, 2, st, cx);
   }
   const double* const* C = E.cot;
   double* const* Wm = E.pwork;
   // real Schur basis (matrices with fsel = 1): Q, T = Q^T (C Q), T', G = (Q T') Q^T
-  const int cx = E.fsel ? 0 : -1;  // the complex form runs for fsel = 0 (every matrix without fsel)
   if (E.fsel) {
     if (!E.back_q && (e = launch_schur_basis(E, st))) return e;
     if ((e = bgemm(E, 1, bop(C, 0, 0), bop(W, 0, 0), 1.0, bop(C, 0, 0), bop(W, 0, 0), 0.0, Wm, 1, 0, 1, st, 1)))

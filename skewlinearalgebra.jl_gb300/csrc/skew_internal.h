@@ -48,6 +48,7 @@ struct Tuning {
   int batch_merge_global;        // 1: consecutive global-memory buckets run as one launch
   int batch_split_pct;           // global-memory launches: first region holds this % of the work (0: one)
   int func_chain_nmax;           // function paths: the QR chain up to this n, bisection above
+  int func_real_schur;           // 1: functions of real matrices in the real Schur basis
   // one large real matrix
   int blocked_min_n;             // the blocked multi-CTA reduction from this n
   int blocked_persistent;        // 1: one cooperative launch for all panels

@@ -44,6 +44,7 @@ void tuning_defaults(Tuning* T) {
   T->batch_merge_global = 1;
   T->batch_split_pct = 50;
   T->func_chain_nmax = 64;
+  T->func_real_schur = 1;
   T->blocked_min_n = 192;
   T->blocked_persistent = 1;
   T->cluster_max_n = 640;
@@ -89,6 +90,7 @@ const Key kKeys[] = {
     {"batch_merge_global", &Tuning::batch_merge_global, 0, 1, k01, 2},
     {"batch_split_pct", &Tuning::batch_split_pct, 0, 95, nullptr, 0},
     {"func_chain_nmax", &Tuning::func_chain_nmax, 0, 1 << 20, nullptr, 0},
+    {"func_real_schur", &Tuning::func_real_schur, 0, 1, k01, 2},
     {"blocked_min_n", &Tuning::blocked_min_n, 16, 1025, nullptr, 0},
     {"blocked_persistent", &Tuning::blocked_persistent, 0, 1, k01, 2},
     {"cluster_max_n", &Tuning::cluster_max_n, 0, 640, nullptr, 0},

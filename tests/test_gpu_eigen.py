@@ -252,3 +252,50 @@ def test_functions_several_odd_blocks(skewgpu):
         _, Lf = sl.expm_frechet(A.T, cots[b])
         assert np.abs(skewgpu.from_device(Go[b]) - Lf).max() <= 1e-8 * np.abs(Lf).max(), n
         np.testing.assert_allclose(skewgpu.exp(A), sl.expm(A), atol=1e-11 * np.sqrt(n))
+
+
+def test_function_forms_agree(skewgpu, oracle):
+    """exp, cis and the exp adjoint in the real Schur basis (the default) and in the
+    complex form Re(V f V^H) (tuning key func_real_schur = 0, the form a matrix takes
+    when its spectrum does not split into exact +- pairs): both against the oracle,
+    on the QR-chain sizes and the bisection sizes, odd and even."""
+    import torch
+
+    sizes = [5, 16, 33, 64, 97, 130]
+    rng = np.random.default_rng(31)
+    mats, cots = [], []
+    for k, n in enumerate(sizes):
+        A = skew_random(n, 9100 + k, scale=1.0)
+        rho = np.abs(np.linalg.eigvals(A)).max()
+        mats.append(A * (rng.uniform(0.5, 8.0) / rho))
+        cots.append(rng.standard_normal((n, n)))
+
+    def run():
+        plan = skewgpu.BatchPlan(sizes)
+        devs = [skewgpu.to_device(A) for A in mats]
+        cd = [skewgpu.to_device(C) for C in cots]
+        Eo = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in sizes]
+        Co = [torch.zeros((n, n), dtype=torch.complex128, device="cuda") for n in sizes]
+        Go = [torch.zeros((n, n), dtype=torch.float64, device="cuda") for n in sizes]
+        st = [plan.exp(plan.pointer_array(devs), plan.pointer_array(Eo)),
+              plan.cis(plan.pointer_array(devs), plan.pointer_array(Co)),
+              plan.exp_vjp(plan.pointer_array(devs), plan.pointer_array(cd), plan.pointer_array(Go))]
+        torch.cuda.synchronize()
+        assert all((s.cpu().numpy() == 0).all() for s in st)
+        out = ([skewgpu.from_device(E) for E in Eo], [skewgpu.from_device_complex(C) for C in Co],
+               [skewgpu.from_device(G) for G in Go])
+        plan.close()
+        return out
+
+    forms = [run()]
+    with skewgpu.tuned(func_real_schur=0):
+        forms.append(run())
+    for E, C, G in forms:
+        for b, A in enumerate(mats):
+            n = sizes[b]
+            Eq = oracle.expm(A)
+            np.testing.assert_allclose(E[b], Eq, atol=1e-11 * np.sqrt(n) * max(1, np.abs(Eq).max()))
+            Cq = oracle.cis(A)
+            np.testing.assert_allclose(C[b], Cq, atol=1e-11 * np.sqrt(n) * max(1, np.abs(Cq).max()))
+            Gq = oracle.exp_vjp(A, cots[b])
+            assert np.abs(G[b] - Gq).max() <= 1e-8 * np.abs(Gq).max(), n
