@@ -357,7 +357,10 @@ SKEW_API int skew_tridiag_svd_z(skew_handle_t h, const double* ev, const double*
  * libskewgpu.so, written by the autotuner (skewgpu/autotune.py).  Keys
  * (skew_tuning_key lists them): bucket_edges (list), batch_smem_nmax,
  * batch_smem_nt_small, batch_smem_nt_large, batch_global_nt,
- * batch_global_ctas_per_sm, batch_graph, func_chain_nmax, blocked_min_n,
+ * batch_global_ctas_per_sm, batch_graph, batch_merge_global (the global-memory size
+ * buckets as one launch), batch_split_pct (that launch in two regions, the first with
+ * this share of the work), func_chain_nmax, func_real_schur (functions of real
+ * matrices in the real Schur basis), blocked_min_n,
  * blocked_persistent, cluster_max_n, persist_ctas, persist_tail, persist_items,
  * persist_nb (panel width of the blocked reduction, 8..128; 64 at most on the
  * multi-launch path), zpersist_min_n, zpersist_ctas, zpersist_items, zpersist_nb (the
