@@ -84,6 +84,8 @@ struct skew_batch_plan_st {
   int* e_status = nullptr;
   unsigned* e_counter = nullptr;
   int* e_fsel = nullptr;  // exp adjoint: per matrix, real Schur-basis (1) or complex (0) form
+  int32_t* e_back_off = nullptr;  // back-transformation items before each matrix (processing order)
+  int32_t back_items = 0;
   // one instantiated CUDA graph per batched operation, keyed on its arguments
   struct GraphSlot {
     bool valid = false;
@@ -635,7 +637,8 @@ int skew_batch_plan_destroy(skew_batch_plan_t P) {
   if (P->d_gws) cudaFreeAsync(P->d_gws, st);
   void* eig[] = {P->e_refl, P->e_tau, P->e_evb, P->e_G, P->e_log, P->e_work, P->e_vr, P->e_vi, P->e_vals,
                  P->e_off_log, P->e_cap_log, P->e_log_len, P->e_off_w, P->e_p_refl, P->e_p_vr, P->e_p_vi,
-                 P->e_p_vals, P->e_p_scratch, P->e_p_work, P->e_status, P->e_fsel, P->e_counter};
+                 P->e_p_vals, P->e_p_scratch, P->e_p_work, P->e_status, P->e_fsel, P->e_back_off,
+                 P->e_counter};
   for (void* q : eig)
     if (q) cudaFreeAsync(q, st);
   if (P->fv_idx) cudaFreeAsync(P->fv_idx, st);
@@ -931,6 +934,7 @@ static int eigen_ws(skew_batch_plan_t P) {
   alloc((void**)&P->e_p_work, sizeof(double*) * count);
   alloc((void**)&P->e_status, sizeof(int) * count);
   alloc((void**)&P->e_fsel, sizeof(int) * count);
+  alloc((void**)&P->e_back_off, sizeof(int32_t) * (count + 1));
   alloc((void**)&P->e_counter, sizeof(unsigned));
   if (!ok) return SKEW_NO_MEMORY;
   int64_t* d_off_sq = nullptr;
@@ -941,6 +945,14 @@ static int eigen_ws(skew_batch_plan_t P) {
   ok &= cudaMemcpyAsync(P->e_cap_log, cap_log.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, st) ==
         cudaSuccess;
   ok &= cudaMemcpyAsync(P->e_off_w, off_w.data(), sizeof(int64_t) * count, cudaMemcpyHostToDevice, st) ==
+        cudaSuccess;
+  // back-transformation items in the processing order (the plan's largest-first order)
+  std::vector<int32_t> ord(count), boff(count + 1, 0);
+  std::iota(ord.begin(), ord.end(), 0);
+  std::stable_sort(ord.begin(), ord.end(), [&](int32_t a, int32_t c) { return P->n_host[a] > P->n_host[c]; });
+  for (int64_t t = 0; t < count; t++) boff[t + 1] = boff[t] + back_items_of(P->n_host[ord[t]]);
+  P->back_items = boff[count];
+  ok &= cudaMemcpyAsync(P->e_back_off, boff.data(), sizeof(int32_t) * (count + 1), cudaMemcpyHostToDevice, st) ==
         cudaSuccess;
   if (!ok) return SKEW_CUDA_ERROR;
   const int g = (int)((count + 255) / 256);
@@ -1093,7 +1105,14 @@ static int eigen_run(skew_batch_plan_t P, const double* const* A, double* const*
     E.back_q = 1;
     CK(launch_schur_basis(E, st));
   }
-  if (!ev_in) CK(launch_eigen_back(E, grid, P->nmax, st));
+  if (!ev_in) {
+    // back-transformation: column chunks of every matrix, so the largest matrices do not
+    // leave most of the GPU idle at the end
+    E.back_off = P->e_back_off;
+    E.back_items = P->back_items;
+    const int bgrid = (int)std::max<int64_t>(1, std::min<int64_t>(2 * (int64_t)P->h->sms, P->back_items));
+    CK(launch_eigen_back(E, bgrid, P->nmax, st));
+  }
   *Eout = E;
   return SKEW_OK;
 }

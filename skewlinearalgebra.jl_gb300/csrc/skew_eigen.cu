@@ -540,10 +540,29 @@ __global__ void __launch_bounds__(ENT) eigen_back_kernel(EigenBatch E) {
   extern __shared__ __align__(16) double esm[];  // Vs (nmax x EB, row-major) | Zs (EB x 2 nmax)
   double* Vs = esm;
   double* Zs = esm + (size_t)E.nmax * EB;
+  __shared__ int s_chunk;
   for (;;) {
-    if (threadIdx.x == 0) s_next = (int)atomicAdd(E.counter, 1u);
+    // work item: (matrix in the processing order, chunk of kBackCols columns), the
+    // largest matrices first; without back_off, one item per matrix
+    if (threadIdx.x == 0) {
+      const int item = (int)atomicAdd(E.counter, 1u);
+      if (!E.back_off) {
+        s_next = item;
+        s_chunk = -1;
+      } else if (item >= E.back_items) {
+        s_next = E.count;
+      } else {
+        int lo = 0, hi = E.count;  // back_off[lo] <= item < back_off[hi]
+        while (hi - lo > 1) {
+          const int mid = (lo + hi) >> 1;
+          if (E.back_off[mid] <= item) lo = mid; else hi = mid;
+        }
+        s_next = lo;
+        s_chunk = item - E.back_off[lo];
+      }
+    }
     __syncthreads();
-    const int t = s_next;
+    const int t = s_next, chunk = s_chunk;
     __syncthreads();
     if (t >= E.count) break;
     const int b = E.order[t];
@@ -552,9 +571,13 @@ __global__ void __launch_bounds__(ENT) eigen_back_kernel(EigenBatch E) {
     const double* R = E.refl[b];  // n x n, ld n
     const double* tau = E.tau + E.off_n[b];
     if (E.status[b] == SKEW_NO_CONVERGENCE || n < 3) continue;
-    // the columns to transform: Vr and Vi, or the real Schur basis Q (work block 0) alone
+    // the columns to transform: Vr and Vi, or the real Schur basis Q (work block 0) alone;
+    // this item takes [c0, c1) of them
     const bool qonly = E.back_q && E.fsel && E.fsel[b] == 1;
-    const int ncol = qonly ? n : 2 * n;
+    const int ncol_all = qonly ? n : 2 * n;
+    const int c0 = chunk < 0 ? 0 : chunk * kBackCols;
+    const int c1 = chunk < 0 ? ncol_all : min(ncol_all, c0 + kBackCols);
+    if (c0 >= c1) continue;
     double* const Xq = E.pwork[b];
     auto colp = [&](int col) -> double* {
       if (qonly) return Xq + (int64_t)col * n;
@@ -603,8 +626,8 @@ __global__ void __launch_bounds__(ENT) eigen_back_kernel(EigenBatch E) {
         }
         __syncthreads();
       }
-      // Y = V^T X (EB x ncol), then Z = T Y; thread per column of X = [Vr | Vi] or Q
-      for (int col = threadIdx.x; col < ncol; col += ENT) {
+      // Y = V^T X (EB x the item's columns), then Z = T Y; thread per column of X
+      for (int col = c0 + (int)threadIdx.x; col < c1; col += ENT) {
         const double* x = colp(col);
         double y[EB];
 #pragma unroll
@@ -623,17 +646,23 @@ __global__ void __launch_bounds__(ENT) eigen_back_kernel(EigenBatch E) {
         }
       }
       __syncthreads();
-      // X[r, col] -= sum_l V[r, l] Z[l, col] for r >= r0; lanes are rows
-      for (int col = threadIdx.x >> 5; col < ncol; col += ENW) {
-        double* x = colp(col);
-        double z[EB];
+      // X[r, col] -= sum_l V[r, l] Z[l, col] for r >= r0; lanes are rows.  Each lane
+      // holds its row of V in registers across the warp's columns (read from shared
+      // memory once per 32-row chunk: the rows are EB doubles apart, so a warp-wide
+      // read of them conflicts), and Z[., col] is a broadcast.
+      for (int rr0 = 0; rr0 < m; rr0 += 32) {
+        const int rr = rr0 + (threadIdx.x & 31);
+        if (rr < m) {
+          double vr[EB];
 #pragma unroll
-        for (int l = 0; l < EB; l++) z[l] = Zs[l * 2 * n + col];
-        for (int rr = threadIdx.x & 31; rr < m; rr += 32) {
-          double acc = x[r0 + rr];
+          for (int l = 0; l < EB; l++) vr[l] = Vs[rr * EB + l];
+          for (int col = c0 + (int)(threadIdx.x >> 5); col < c1; col += ENW) {
+            double* x = colp(col);
+            double acc = x[r0 + rr];
 #pragma unroll
-          for (int l = 0; l < EB; l++) acc = fma(-Vs[rr * EB + l], z[l], acc);
-          x[r0 + rr] = acc;
+            for (int l = 0; l < EB; l++) acc = fma(-vr[l], Zs[l * 2 * n + col], acc);
+            x[r0 + rr] = acc;
+          }
         }
       }
       __syncthreads();

@@ -256,6 +256,9 @@ struct EigenBatch {
   int max_iter = 0;          // QR sweeps before SKEW_NO_CONVERGENCE (0: 30 n, skeweigen.jl:340)
   int* fsel = nullptr;       // [count] exp adjoint: 1 real Schur-basis path, 0 complex path
                              // (null: the complex path for every matrix)
+  const int32_t* back_off = nullptr;  // [count + 1] back-transformation items before each matrix
+                             // of the processing order (null: one item per matrix)
+  int32_t back_items = 0;    // total items (chunks of kBackCols columns)
   int back_q = 0;            // 1: the real Schur basis Q was built in the tridiagonal basis
                              // (pwork block 0): the back-transformation takes Q alone for the
                              // matrices with fsel = 1, and the adjoint starts from it
@@ -279,6 +282,9 @@ cudaError_t launch_copy_ev(const double* const* ev_in, const int32_t* n, const i
                            cudaStream_t st);
 // doubles of per-matrix work the eigen kernels need (4 n^2, or more for the fallback of small n)
 size_t eigen_work_doubles(int n);
+// Columns per work item of the batched back-transformation (of [Vr | Vi], 2n columns).
+constexpr int kBackCols = 64;
+inline int back_items_of(int n) { return n < 3 ? 0 : (2 * n + kBackCols - 1) / kBackCols; }
 cudaError_t launch_eigen_chain(const EigenBatch& E, cudaStream_t st);
 cudaError_t launch_eigen_vectors(const EigenBatch& E, int grid, cudaStream_t st);
 cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStream_t st);
