@@ -52,8 +52,8 @@ ScratchSlot g_slot[kMaxDevices];
 std::mutex g_slot_mu;
 
 // Id of the calling thread's current CUDA context (unique for the process's
-// lifetime), or 0 if there is none; through the driver entry points the runtime
-// hands out, so the library does not link the driver library itself.
+// lifetime), or 0 if there is none; through the CUDA driver-API entry points that
+// the runtime hands out, so the library does not link libcuda itself.
 unsigned long long current_context_id() {
   typedef int (*GetCurrentFn)(void**);
   typedef int (*GetIdFn)(void*, unsigned long long*);
