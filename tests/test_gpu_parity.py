@@ -279,3 +279,31 @@ def test_batch_eigvals_stagnation_fallback(skewgpu, oracle):
         np.testing.assert_allclose(np.sort(v), np.sort(vq), atol=RTOL * scale)
         np.testing.assert_allclose(v, vd, atol=1e-11 * scale)  # same order as the reference
     plan.close()
+
+
+def test_batch_schedule_invariance(skewgpu, oracle):
+    """Every matrix of a batch is reduced, and its gradient formed, by one CTA with the
+    same arithmetic whichever CTA takes it.  So the launch shape (global-memory size
+    buckets merged into one launch or not, the two regions split at different shares
+    of the work or not at all) must not change a single bit of log|Pf|, sign or
+    gradient; the default is also checked against the oracle on a sample."""
+    rng = np.random.default_rng(404)
+    sizes = [int(2 * rng.integers(8, 129)) for _ in range(700)] + [256, 255, 97, 96, 2, 1, 0]
+    mats = [skew_random(n, 5000 + k) / max(1.0, np.sqrt(n)) for k, n in enumerate(sizes)]
+    ref = _batch(skewgpu, mats)
+    for keys in ({"batch_merge_global": 0}, {"batch_split_pct": 0}, {"batch_split_pct": 30},
+                 {"batch_merge_global": 0, "batch_split_pct": 0}):
+        with skewgpu.tuned(**keys):
+            out = _batch(skewgpu, mats)
+        assert np.array_equal(out[0], ref[0], equal_nan=True), keys
+        assert np.array_equal(out[1], ref[1], equal_nan=True), keys
+        assert np.array_equal(out[2], ref[2]), keys
+        for g, h in zip(out[3], ref[3]):
+            assert np.array_equal(g, h, equal_nan=True), keys
+    for k in list(range(0, 700, 97)) + [700, 701]:
+        lp, sg = oracle.logabspfaffian(mats[k])
+        assert ref[1][k] == sg
+        if np.isfinite(lp):
+            assert abs(ref[0][k] - lp) <= 1e-11 * max(1.0, abs(lp))
+        else:
+            assert ref[0][k] == lp
