@@ -931,7 +931,7 @@ cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStrea
 }
 
 // ---------------------------------------------------------------------------
-// exp adjoint in the real Schur basis
+// Matrix functions and the exp adjoint in the real Schur basis
 // ---------------------------------------------------------------------------
 // The eigenvectors of a real skew matrix come in conjugate pairs.  For mu > 0 the
 // column u = (x + i y)/sqrt(2) gives the orthonormal pair (x, y) = sqrt(2) (Re u,
@@ -958,9 +958,10 @@ cudaError_t launch_eigen_back(const EigenBatch& E, int grid, int nmax, cudaStrea
 // f(mu J) = Re f(i mu) I + Im f(i mu) J, so f(A) = (Q f(S)) Q^T is one product, and
 // cis(A) = exp(i A) = Q (cosh(mu) I + i sinh(mu) J) Q^T two.
 //
-// Workspace per matrix (pwork, 4 n^2): Q | T' (and C Q) | T (and Q T') | metadata:
-// per eigenvector column its first Q column (-1: skipped), per block its mu and
-// first Q column (negative - 1 for a single column), and the block count.
+// Workspace per matrix (pwork, 4 n^2): Q | T' (and C Q, Q f(S)) | T (and Q T', Q i sinh)
+// | metadata: per eigenvector column and per block a code, 2 p + 1 for a pair starting
+// at Q column p and 2 p for a single column (-1: a skipped partner column), per block
+// its mu, and the block count.
 
 constexpr int SB_NT = 256;
 
