@@ -307,4 +307,3 @@ def test_batch_schedule_invariance(skewgpu, oracle):
             assert abs(ref[0][k] - lp) <= 1e-11 * max(1.0, abs(lp))
         else:
             assert ref[0][k] == lp
-
