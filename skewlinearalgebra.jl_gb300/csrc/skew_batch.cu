@@ -546,13 +546,48 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
           for (int l = 0; l < GNB; l++) acc[l] = fma(g, vj[l], acc[l]);
         }
       };
+      // the rows of strip si over columns [cb, ce), one row per lane.  A strip of at
+      // most 16 rows (the last one) would leave lanes idle for the whole column loop,
+      // so groups of p2 lanes (p2 the power of two >= its rows) take slices of the
+      // columns and add their partials by xor shuffles; lane L < rows then holds row
+      // 32 si + L.  Returns the strip's rows.
+      auto xstrip = [&](int si, int cb, int ce, double* acc) -> int {
+        const int rs = min(32, nvr - 32 * si);
+        if (rs > 16) {
+          const int t = si * 32 + lane;
+          if (lane < rs) {
+            xrow(t < m ? r0 + t : 2 * (t - m), cb, ce, acc);
+          } else {
+#pragma unroll
+            for (int l = 0; l < GNB; l++) acc[l] = 0.0;
+          }
+          return rs;
+        }
+        int p2 = 1;
+        while (p2 < rs) p2 <<= 1;
+        const int g = lane / p2, rl = lane - g * p2, groups = 32 / p2;
+        const int seg = (ce - cb + groups - 1) / groups;
+        const int sb = cb + g * seg, se = min(ce, sb + seg);
+        const int t = si * 32 + rl;
+        if (rl < rs && sb < se) {
+          xrow(t < m ? r0 + t : 2 * (t - m), sb, se, acc);
+        } else {
+#pragma unroll
+          for (int l = 0; l < GNB; l++) acc[l] = 0.0;
+        }
+        for (int o = p2; o < 32; o <<= 1) {
+#pragma unroll
+          for (int l = 0; l < GNB; l++) acc[l] += __shfl_xor_sync(0xffffffffu, acc[l], o);
+        }
+        return rs;
+      };
       if (sp.U == 0) {
         for (int si = w; si < S; si += NW) {
+          double acc[GNB];
+          const int rs = xstrip(si, r0, n, acc);
           const int t = si * 32 + lane;
-          if (t < nvr) {
+          if (lane < rs) {
             const int i = t < m ? r0 + t : 2 * (t - m);
-            double acc[GNB];
-            xrow(i, r0, n, acc);
 #pragma unroll
             for (int l = 0; l < GNB; l++) Zs[i * GNB + l] = acc[l];
           }
@@ -561,11 +596,9 @@ __device__ void gradient(const MW& W, const GMat& G, int n, const Smem& s) {
         const int u1 = min(S * m, (w + 1) * sp.U);
         for (int u = w * sp.U; u < u1;) {
           const int si = u / m;
-          const int t = si * 32 + lane;
-          if (t < nvr) {
-            const int i = t < m ? r0 + t : 2 * (t - m);
-            double acc[GNB];
-            xrow(i, r0 + (u - si * m), r0 + min(m, u1 - si * m), acc);
+          double acc[GNB];
+          const int rs = xstrip(si, r0 + (u - si * m), r0 + min(m, u1 - si * m), acc);
+          if (lane < rs) {
 #pragma unroll
             for (int l = 0; l < GNB; l++) Xp[((w + si) * 32 + lane) * GNB + l] = acc[l];
           }
