@@ -37,7 +37,7 @@ sys.path.insert(0, os.path.join(ROOT, "skewlinearalgebra.jl_gb300"))
 # dram__bytes_read.sum + dram__bytes_write.sum over the four batch_kernel launches of one
 # step of the default workload (4096 matrices, even n in [16, 256]), from one ncu capture
 # of the timed step (-s 12 -c 4)
-STEP_DRAM_BYTES = 34_450_157_056
+STEP_DRAM_BYTES = 20_753_729_792
 METRIC = "batched log|Pf|+grad matrices/s & n=8192 hessenberg GFLOP/s vs plain GPU, err≤1e-11"
 UNIT = "matrices/s"
 COUNT = 4096
